@@ -1,0 +1,369 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 kD-tree Barnes-Hut step.
+
+Workload (one line of JSON on rank 0): the 10,000,000-body ring (body 0: mass 1 at the
+origin; bodies 1..N-1: mass 1e-14, r ~ U[0.8, 1.2], phi ~ U[0, 2 pi), z ~ Normal(0, 1e-4),
+circular velocities), theta = 0.3, leaf size 7, dt = 1e-3, mixed precision.  A "step" is one
+simulation step: tree build, centre-of-mass pass, force walk, kick-drift.
+
+* ``value``: body-steps/s of the mixed path with the bodies resident in HBM (640 MB of
+  bodies > 129 MB L2, so no L2 flush is needed between steps).
+* ``e2e``: the same metric through the reference-shaped C-ABI call with host buffers: every
+  step copies the bodies from pinned host memory (kd_set_bodies), runs one step
+  (kd_simple_sim), and copies them back (kd_get_bodies).
+* ``fp64``: the plain FP64 path on the same bodies (the reference's arithmetic), and the
+  mixed/FP64 speed ratio.
+* ``accuracy``: max / RMS relative acceleration error of the mixed walk against an FP64
+  direct sum on 4,096 seeded bodies (body 0, whose acceleration is a near-cancelling
+  residual, is reported separately).
+* ``roofline``: the force walk (the dominant kernel) against the FP32 rate of the GPU;
+  ``roofline_build``: the build against measured HBM bandwidth.
+* ``cpu_baseline``: the CPU oracle's step loop (the reference's algorithm, OpenMP,
+  fork-join build) on one step of the same workload.
+
+``--impl reference`` times the reference's CPU algorithm (the oracle port, all host
+threads) on the same workload and prints the same line with ``"impl": "reference"``.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "body-steps/s @N=10M mixed vs FP64 plain, accel err<=1e-4; adjoint/forward time"
+UNIT = "body-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=10_000_000)
+    ap.add_argument("--theta", type=float, default=0.3)
+    ap.add_argument("--leaf", type=int, default=7)
+    ap.add_argument("--dt", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--err-samples", type=int, default=4096)
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="only the headline timing (used for profiling captures)")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ distributed (replicas)
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v: float) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ CPU reference arm
+
+def cpu_step_rate(bodies, steps: int, leaf: int, theta: float, dt: float):
+    """The oracle's step loop (reference algorithm: fork-join PAR4 build, parallel walk)
+    on all host threads.  Returns (body-steps/s, threads, seconds)."""
+    from oracle import Oracle
+    orc = Oracle()
+    threads = orc.threads()
+    b = bodies.copy()
+    t0 = time.perf_counter()
+    orc.simple_sim(b, dt, steps, leaf=leaf, layout="par4", theta=theta)
+    t = time.perf_counter() - t0
+    return len(b) * steps / t, threads, t
+
+
+def run_reference(a, ws, rank):
+    if rank != 0:
+        return
+    import multilanguagekdtree_gb300.array_particle as ap
+    bodies = ap.ring(a.n, seed=a.seed)
+    # one untimed step warms caches and page tables; each timed step is one full step of
+    # the same 10M-body workload, capped so the run stays within a few minutes
+    rate_w, threads, tw = cpu_step_rate(bodies, 1, a.leaf, a.theta, a.dt)
+    steps = max(1, min(a.steps, int(150.0 / max(tw, 1e-3))))
+    rate, threads, t = cpu_step_rate(bodies, steps, a.leaf, a.theta, a.dt)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": a.gpus,
+        "steps": steps, "warmup": 1, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"ring N={a.n} theta={a.theta} leaf={a.leaf} dt={a.dt} "
+                               "(reference algorithm: FP64, fork-join median build, "
+                               "recursive walk)", "n_bodies": a.n},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} full step(s) of the {a.n}-body ring"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def pinned_bodies(n):
+    import torch
+    from multilanguagekdtree_gb300 import PARTICLE_DTYPE
+    t = torch.empty(n * 64, dtype=torch.uint8, pin_memory=True)
+    return t, t.numpy().view(PARTICLE_DTYPE)
+
+
+def run_ours(a, ws, rank, local):
+    import torch
+
+    import multilanguagekdtree_gb300 as kd
+    dev = local
+    torch.cuda.set_device(dev)
+    bodies = kd.ring(a.n, seed=a.seed + rank)
+    n = a.n
+
+    # ---- headline: mixed precision, bodies resident
+    sim = kd.KDTreeSim(n, leaf_size=a.leaf, layout="dfs", precision="mixed", theta=a.theta,
+                       dt=a.dt, device=dev)
+    sim.set_bodies(bodies)
+    sim.simple_sim(a.dt, a.warmup)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.simple_sim(a.dt, a.steps)
+    torch.cuda.synchronize()
+    host_s = time.perf_counter() - t0
+    barrier(ws)
+    clk = clocks.stop()
+    st = sim.stats()
+    dev_s = st["total_ms"] / 1e3
+    launches = int(st["launches"])
+    t_max = max_over_ranks(ws, dev_s)
+    value = ws * n * a.steps / t_max
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic",
+        "config": {"workload": f"ring N={n} theta={a.theta} leaf={a.leaf} dt={a.dt} mixed",
+                   "n_bodies": n, "leaf_size": a.leaf, "theta": a.theta, "dt": a.dt,
+                   "precision": "mixed", "parallelism": f"replicas x{ws}",
+                   "l2": "inputs (640 MB of bodies, 1.1 GB with the tree) exceed the 129 MB "
+                         "L2; no flush"},
+        "gpu_launches": launches, "clocks": clk, "host_wall_s": host_s,
+    }
+    if a.no_extras or rank != 0:
+        if rank == 0:
+            print(json.dumps(line))
+        return
+
+    # ---- per-phase device times (events around every phase) and interaction counts
+    sim.set_bodies(bodies)
+    sim.set_timing(True)
+    sim.simple_sim(a.dt, 2)
+    ph = sim.stats()
+    sim.set_timing(False)
+    sim.set_bodies(bodies)
+    sim.build_tree()
+    sim.set_counting(True)
+    sim.calc_accel()
+    cnt = sim.counts()
+    sim.set_counting(False)
+    flops = 18 * cnt["p2p"] + 10 * cnt["opened"] + 9 * cnt["m2p"]
+    walk_s = ph["walk_ms"] / 2 / 1e3
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s at the sampled clock
+    achieved = flops / walk_s / 1e12
+    line["phases_ms_per_step"] = {k: ph[k] / 2 for k in ("build_ms", "moments_ms", "walk_ms",
+                                                         "kick_ms")}
+    line["interactions_per_body"] = {k: v / n for k, v in cnt.items()}
+    line["roofline"] = {
+        "kernel": "k_walk_mixed", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+        "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+        "note": "walk flops = 18 P2P + 10 opening tests + 9 M2P per body (counted on the "
+                "device); peak = 152 SMs x 128 FP32 lanes x 2 x sampled SM clock (nominal "
+                "rate; no measured FP32 figure exists)"}
+    # build: algorithmic bytes ~ N*(40 L + 32) with L = multi-block levels, see the design doc
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    levels = max(1, int(np.ceil(np.log2(n / 1024.0))))
+    build_bytes = n * (40 * levels + 32)
+    build_s = ph["build_ms"] / 2 / 1e3
+    line["roofline_build"] = {
+        "bound": "hbm", "achieved": build_bytes / build_s / 1e9, "peak": hbm, "unit": "GB/s",
+        "frac": build_bytes / build_s / 1e9 / hbm, "traffic": None,
+        "peak_source": "MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
+
+    # ---- accuracy of the mixed walk against the FP64 direct sum
+    rng = np.random.default_rng(12345)
+    sinks = np.sort(rng.choice(np.arange(1, n), a.err_samples, replace=False))
+    sim.set_bodies(bodies)
+    sim.build_tree()
+    macc = sim.calc_accel()
+    direct = sim.direct_accel(np.concatenate([[0], sinks]))
+    sim.set_precision("fp64")
+    facc = sim.calc_accel()
+    sim.set_precision("mixed")
+
+    def rel(x, y):
+        return np.linalg.norm(x - y, axis=1) / np.linalg.norm(y, axis=1)
+
+    e_mixed = rel(macc[sinks], direct[1:])
+    e_fp64 = rel(facc[sinks], direct[1:])
+    e_mix_vs_fp64 = rel(macc[sinks], facc[sinks])
+    line["accuracy"] = {
+        "samples": int(a.err_samples), "reference": "FP64 direct sum (GPU kernel, all N)",
+        "mixed_max_rel": float(e_mixed.max()), "mixed_rms_rel": float(np.sqrt(np.mean(e_mixed ** 2))),
+        "fp64_tree_max_rel": float(e_fp64.max()),
+        "mixed_vs_fp64_tree_max_rel": float(e_mix_vs_fp64.max()),
+        "body0_mixed_rel": float(rel(macc[:1], direct[:1])[0]),
+        "body0_fp64_tree_rel": float(rel(facc[:1], direct[:1])[0]),
+    }
+    sim.close()
+
+    # ---- FP64 plain path, same bodies
+    f64 = kd.KDTreeSim(n, leaf_size=a.leaf, layout="dfs", precision="fp64", theta=a.theta,
+                       dt=a.dt, device=dev)
+    f64.set_bodies(bodies)
+    f64.simple_sim(a.dt, 1)
+    torch.cuda.synchronize()
+    f64.simple_sim(a.dt, a.fp64_steps)
+    fst = f64.stats()
+    fp64_rate = n * a.fp64_steps / (fst["total_ms"] / 1e3)
+    line["fp64"] = {"value": fp64_rate, "unit": UNIT, "steps": a.fp64_steps,
+                    "ms_per_step": fst["total_ms"] / a.fp64_steps}
+    line["mixed_over_fp64"] = value / ws / fp64_rate
+    f64.close()
+
+    # ---- end to end through the C ABI with host buffers
+    keep, host = pinned_bodies(n)
+    host[:] = bodies
+    e2e = kd.KDTreeSim(n, leaf_size=a.leaf, layout="dfs", precision="mixed", theta=a.theta,
+                       dt=a.dt, device=dev)
+    e2e.set_bodies(host)
+    e2e.simple_sim(a.dt, 1)
+    e2e.get_bodies(out=host)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        e2e.set_bodies(host)
+        e2e.simple_sim(a.dt, 1)
+        e2e.get_bodies(out=host)
+    e2e_s = time.perf_counter() - t0
+    e2e.close()
+    line["e2e"] = {"value": n * a.e2e_steps / e2e_s, "unit": UNIT,
+                   "h2d_bytes_per_step": 64 * n, "d2h_bytes_per_step": 64 * n,
+                   "steps": a.e2e_steps,
+                   "call": "kd_set_bodies(pinned host) + kd_simple_sim(1) + kd_get_bodies"}
+    del keep
+
+    # ---- CPU baseline (oracle port of the reference algorithm)
+    if not a.no_cpu_baseline:
+        rate, threads, t = cpu_step_rate(bodies, a.cpu_steps, a.leaf, a.theta, a.dt)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{a.cpu_steps} full FP64 step(s) of the {n}-body "
+                                          f"ring ({t:.1f} s)"}
+    print(json.dumps(line))
+
+
+def main():
+    a = parse()
+    ws, rank, local = dist_setup()
+    if a.impl == "reference":
+        run_reference(a, ws, rank)
+    else:
+        run_ours(a, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

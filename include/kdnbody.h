@@ -1,0 +1,172 @@
+/*
+ * kdnbody.h -- C ABI of libkdnbody.so, the GB300 kD-tree Barnes-Hut step.
+ *
+ * The reference (MarkCLewis/MultiLanguageKDTree) exposes this path as the Rust module
+ * surface of Parallel/RustVersion (src/lib.rs:1-3: array_kd_tree, array_particle,
+ * quickstat).  Each entry point below names the reference function it stands in for.
+ * Conventions:
+ *   - every call returns 0 (KD_OK) or a negative KD_E* code; nothing aborts or throws
+ *     across this boundary, and kd_last_error() holds a one-line message;
+ *   - the caller owns every host buffer; the library owns all device memory of a context;
+ *   - one context = one CUDA stream on one device; a context is not thread-safe, a
+ *     process may hold several;
+ *   - body indices are 0..n-1 in the order of the array given to kd_set_bodies.
+ */
+#ifndef KDNBODY_H
+#define KDNBODY_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KD_OK 0
+#define KD_EINVAL (-1)    /* bad argument: size, leaf size, layout, NULL pointer */
+#define KD_ENOMEM (-2)    /* device or host allocation failed */
+#define KD_ECUDA (-3)     /* a CUDA runtime call failed */
+#define KD_ESTATE (-4)    /* call out of order (no bodies yet, no tree yet, no tape) */
+#define KD_ENUMERIC (-5)  /* non-finite position/velocity/mass, or a negative mass */
+#define KD_EOVERFLOW (-6) /* node slots exhausted: the reference would panic here */
+#define KD_EDEVICE (-7)   /* a device-side check failed (stack depth, iteration cap) */
+
+#define KD_MAX_LEAF 8
+
+/* Body record: Particle of Parallel/RustVersion/src/array_particle.rs:3-8 (and
+ * Parallel/CVersion/src/particle.h:13-18): position, velocity, radius (unused by the
+ * dynamics, carried through), mass.  64 bytes, #[repr(C)]-compatible. */
+typedef struct {
+    double p[3];
+    double v[3];
+    double r;
+    double m;
+} kd_particle_c;
+
+/* Node record: the flat KDTree struct of Parallel/CVersion/src/kdtree.h:9-22, with 8 leaf
+ * slots so that both reference leaf sizes (7: sequential Rust and C; 8: parallel Rust) fit.
+ * A leaf has num_parts > 0 (or is an unused PAR4 slot with num_parts == 0 and left ==
+ * right == 0); an internal node has num_parts == 0 and the fields of the Rust
+ * KDTree::Internal variant (array_kd_tree.rs:25-33).  particles[] holds body indices. */
+typedef struct {
+    uint64_t num_parts;
+    uint64_t particles[KD_MAX_LEAF];
+    uint64_t split_dim;
+    double split_val;
+    double m;
+    double cm[3];
+    double size;
+    uint64_t left;
+    uint64_t right;
+} kd_node_c;
+
+/* Node numbering.  DFS: left = cur+1, right = last node of left + 1 -- build_tree of
+ * array_kd_tree.rs:63-130.  PAR4: left = cur+1, right = cur+1+nodes_needed(len/2) --
+ * build_tree_par4 of array_kd_tree.rs:515-583 (the one simple_sim uses, :643). */
+enum { KD_LAYOUT_DFS = 0, KD_LAYOUT_PAR4 = 1 };
+
+/* FP64: the reference's arithmetic, every interaction of every body as the Rust walk makes
+ * it.  MIXED: FP32 pairwise and multipole terms on split (hi+lo) coordinates with
+ * compensated sums; FP64 for storage, tree splits, kick-drift and the heavy-body term. */
+enum { KD_PREC_FP64 = 0, KD_PREC_MIXED = 1 };
+
+typedef struct {
+    int32_t leaf_size;  /* MAX_PARTS: 7 (Sequential Rust, C) or 8 (Parallel Rust); 2..8 */
+    int32_t layout;     /* KD_LAYOUT_* numbering reported by kd_get_nodes */
+    int32_t precision;  /* KD_PREC_* */
+    int32_t device;     /* CUDA device ordinal */
+    double theta;       /* THETA, array_kd_tree.rs:15 (0.3) */
+    double dt;          /* time step used by kd_simple_sim when its dt argument is 0 */
+    double heavy_frac;  /* MIXED: bodies with m >= heavy_frac * total mass are summed
+                           directly in FP64 (the central-mass term); <= 0 disables */
+    uint64_t seed;      /* reserved for generators; the build itself is deterministic */
+} kd_params;
+
+typedef struct kd_ctx kd_ctx;
+typedef struct kd_tape kd_tape;
+
+/* Per-phase device times of the last kd_simple_sim / kd_calc_accel call, milliseconds,
+ * and the walk's interaction counts when counting was requested. */
+typedef struct {
+    double build_ms;    /* per-phase sums; filled only while kd_set_timing(ctx, 1) */
+    double moments_ms;
+    double walk_ms;
+    double kick_ms;
+    double total_ms;    /* whole call, always */
+    uint64_t steps;
+    uint64_t launches;  /* kernels launched by the call */
+} kd_stats;
+
+/* Fill defaults: leaf 7, DFS, FP64, device 0, theta 0.3, dt 1e-3, heavy_frac 1e-3. */
+void kd_default_params(kd_params *params);
+
+/* allocate_node_vec / nodes_needed_for_particles: number of node slots the reference
+ * allocates for n bodies.  PAR4: Parallel/RustVersion/src/array_kd_tree.rs:45-60;
+ * DFS: Sequential/RustVersion/src/array_kd_tree.rs:37-46 (that Vec grows on demand;
+ * kd_build_tree reports the nodes actually used). */
+size_t kd_nodes_needed(size_t n, int32_t leaf_size, int32_t layout);
+
+/* Create a context for n bodies (1 <= n < 2^31).  Replaces the set-up half of
+ * simple_sim (array_kd_tree.rs:624-630): node storage, index vector, accelerations.
+ * Returns NULL on failure; kd_last_error(NULL) then says why. */
+kd_ctx *kd_create(size_t n, const kd_params *params);
+void kd_destroy(kd_ctx *ctx);
+
+/* Last error message of ctx (or of the calling thread's last failed kd_create when ctx is
+ * NULL).  Never NULL. */
+const char *kd_last_error(const kd_ctx *ctx);
+
+/* Copy n bodies host -> device (Vec<Particle> handed to simple_sim/build_tree).  Checks
+ * that every p, v, m is finite and m >= 0. */
+int kd_set_bodies(kd_ctx *ctx, const kd_particle_c *bodies, size_t n);
+/* Copy the bodies device -> host (the &mut Vec<Particle> after simple_sim returns). */
+int kd_get_bodies(kd_ctx *ctx, kd_particle_c *bodies, size_t n);
+
+/* build_tree (array_kd_tree.rs:63-130) / build_tree_par4 (:515-583) over the current
+ * bodies, on the device.  *last_node (may be NULL) receives the index of the last node
+ * used in the context's layout: build_tree's return value for DFS, the highest occupied
+ * slot for PAR4. */
+int kd_build_tree(kd_ctx *ctx, size_t *last_node);
+
+/* Copy the tree built by the last kd_build_tree to the host in the context's layout.
+ * cap must be >= the node count (kd_nodes_needed for PAR4, last_node+1 for DFS);
+ * *count receives the number of records written. */
+int kd_get_nodes(kd_ctx *ctx, kd_node_c *out, size_t cap, size_t *count);
+
+/* calc_accel (array_kd_tree.rs:619-621) for every body at once, over the tree of the last
+ * kd_build_tree: acc[3*i+d] = d-th component of the acceleration of body i. */
+int kd_calc_accel(kd_ctx *ctx, double *acc);
+
+/* simple_sim (array_kd_tree.rs:623-664): `steps` steps of build -> accel -> kick-drift
+ * (v += dt*a; p += dt*v), bodies resident on the device between calls.  dt == 0 uses
+ * params.dt. */
+int kd_simple_sim(kd_ctx *ctx, double dt, int64_t steps);
+
+/* Switch the arithmetic of later walks (KD_PREC_*). */
+int kd_set_precision(kd_ctx *ctx, int32_t precision);
+
+/* Device timings of the last call. */
+int kd_get_stats(const kd_ctx *ctx, kd_stats *out);
+
+/* Record CUDA events around every phase of every step (build, moments, walk, kick) so
+ * kd_get_stats reports per-phase device time.  Off by default. */
+int kd_set_timing(kd_ctx *ctx, int32_t on);
+
+/* FP64 direct sum (no tree) for a list of sink bodies over all n bodies, pair kernel of
+ * array_particle.rs:67-76 -- the all-pairs form of Sequential/RustVersion/src/
+ * simd_particle.rs:95-103, one-sided.  acc[3*k+d] for sinks[k].  An error yardstick for the
+ * tree walks; O(ns * n). */
+int kd_direct_accel(kd_ctx *ctx, const uint64_t *sinks, size_t ns, double *acc);
+
+/* Interaction counts of the last walk, summed over bodies: out[0] = pair (P2P)
+ * interactions, out[1] = opening tests at internal nodes, out[2] = accepted multipole
+ * (M2P) interactions, out[3] = nodes visited by the warps.  Counting is enabled by
+ * kd_set_counting(ctx, 1) (it costs a few percent). */
+int kd_set_counting(kd_ctx *ctx, int32_t on);
+int kd_get_counts(const kd_ctx *ctx, uint64_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KDNBODY_H */

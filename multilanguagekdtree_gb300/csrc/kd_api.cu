@@ -1,0 +1,749 @@
+// kd_api.cu -- host runtime behind include/kdnbody.h: the per-n tree plan, device memory of
+// a context, the step sequence and the C entry points.
+//
+// The reference's step (MarkCLewis/MultiLanguageKDTree Parallel/RustVersion/src/
+// array_kd_tree.rs:623-664 simple_sim) is: reset the index vector, build the tree, compute
+// every body's acceleration, kick-drift.  Here the same step is a fixed sequence of kernel
+// launches on the context's stream; the bodies stay on the device between calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/kdnbody.h"
+#include "kd_internal.cuh"
+
+using namespace kd;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+constexpr uint32_t kNone = 0xffffffffu;
+
+// nodes_needed_for_particles of Parallel/RustVersion/src/array_kd_tree.rs:45-53; the
+// power of two 2^ceil(log2 x) is the smallest one >= x (equal for every x < 2^52).
+uint64_t needed_par(uint64_t n, uint32_t leaf) {
+    if (n <= leaf) return 1;
+    const uint64_t min_leaves = n / (leaf / 2);
+    uint64_t leaves = 1;
+    while (leaves < min_leaves) leaves <<= 1;
+    return 2 * leaves - 1;
+}
+
+// Sequential/RustVersion/src/array_kd_tree.rs:37-39
+uint64_t needed_seq(uint64_t n, uint32_t leaf) { return 2 * (n / (leaf / 2) + 1); }
+
+// The tree of n bodies: shape, segment of every node, DFS and PAR4 numbering, level lists.
+struct Plan {
+    uint32_t n = 0, leaf = 0, n_nodes = 0;
+    std::vector<uint32_t> start, count, right, parent, leaves;
+    std::vector<uint64_t> par4;           // PAR4 slot of every DFS node
+    std::vector<std::vector<uint32_t>> glevels;  // internal nodes of the multi-block levels
+    std::vector<uint32_t> gmax;           // largest segment per multi-block level
+    std::vector<uint32_t> local_roots;
+    std::vector<uint32_t> ttab;
+    uint64_t par4_slots = 0, par4_last = 0;
+    bool par4_ok = true;
+};
+
+struct Memo {
+    uint32_t leaf;
+    std::unordered_map<uint64_t, uint64_t> t;
+    uint64_t T(uint64_t nb) {
+        if (nb <= leaf) return 1;
+        auto it = t.find(nb);
+        if (it != t.end()) return it->second;
+        uint64_t v = 1 + T(nb / 2) + T(nb - nb / 2);
+        t.emplace(nb, v);
+        return v;
+    }
+};
+
+bool make_plan(uint32_t n, uint32_t leaf, Plan &p, std::string &err) {
+    p.n = n;
+    p.leaf = leaf;
+    Memo memo{leaf, {}};
+    const uint64_t total = memo.T(n);
+    if (total >= 0xffffffffull) {
+        err = "too many nodes";
+        return false;
+    }
+    p.n_nodes = (uint32_t)total;
+    p.start.assign(p.n_nodes, 0);
+    p.count.assign(p.n_nodes, 0);
+    p.right.assign(p.n_nodes, 0);
+    p.parent.assign(p.n_nodes, kNone);
+    p.par4.assign(p.n_nodes, 0);
+    p.par4_slots = needed_par(n, leaf);
+    p.ttab.resize(kLocalMax + 1);
+    for (uint32_t i = 0; i <= (uint32_t)kLocalMax; ++i) p.ttab[i] = (uint32_t)memo.T(i);
+
+    struct E {
+        uint32_t id, st, cn, parent;
+        uint64_t par4, cap4;
+    };
+    std::vector<E> cur{{0u, 0u, n, kNone, 0ull, p.par4_slots}}, nxt;
+    bool local_found = false;
+    while (!cur.empty()) {
+        uint32_t mx = 0;
+        for (const E &e : cur) mx = std::max(mx, e.cn);
+        if (!local_found && mx <= (uint32_t)kLocalMax) {
+            local_found = true;
+            for (const E &e : cur) p.local_roots.push_back(e.id);
+        }
+        std::vector<uint32_t> internal;
+        nxt.clear();
+        for (const E &e : cur) {
+            p.start[e.id] = e.st;
+            p.count[e.id] = e.cn;
+            p.parent[e.id] = e.parent;
+            p.par4[e.id] = e.par4;
+            p.par4_last = std::max(p.par4_last, e.par4);
+            if (e.cap4 < 1) p.par4_ok = false;
+            if (e.cn > leaf) {
+                internal.push_back(e.id);
+                const uint32_t lc = e.cn / 2, rc = e.cn - lc;
+                const uint32_t lid = e.id + 1;
+                const uint32_t rid = e.id + 1 + (uint32_t)memo.T(lc);
+                p.right[e.id] = rid;
+                const uint64_t lcap = needed_par(lc, leaf);
+                // build_tree_par4 splits its slice as [this | left: lcap | right: rest]
+                if (1 + lcap > e.cap4) p.par4_ok = false;
+                const uint64_t rcap = e.cap4 > 1 + lcap ? e.cap4 - 1 - lcap : 0;
+                nxt.push_back({lid, e.st, lc, e.id, e.par4 + 1, lcap});
+                nxt.push_back({rid, e.st + lc, rc, e.id, e.par4 + 1 + lcap, rcap});
+            } else {
+                p.leaves.push_back(e.id);
+            }
+        }
+        if (!local_found) {
+            p.glevels.push_back(internal);
+            p.gmax.push_back(mx);
+        }
+        cur.swap(nxt);
+    }
+    return true;
+}
+
+template <typename T>
+cudaError_t dalloc(T **ptr, size_t count) {
+    *ptr = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)ptr, sizeof(T) * count);
+}
+
+}  // namespace
+
+struct kd_ctx {
+    size_t n = 0;
+    kd_params prm{};
+    cudaStream_t st = nullptr;
+    std::string err;
+    Plan plan;
+
+    // static topology on the device
+    uint32_t *d_start = nullptr, *d_count = nullptr, *d_right = nullptr, *d_parent = nullptr,
+             *d_leaves = nullptr, *d_ttab = nullptr, *d_local_roots = nullptr;
+    std::vector<uint32_t *> d_glevels;
+    Topology topo{};
+
+    Bodies bodies{};
+    double *acc = nullptr;
+    void *aos = nullptr;  // staging for host transfers
+    Work work{};
+    Scratch scr{};
+    NodeOut nout{};
+    Moments mom{}, momf{};  // FP64 and light (mixed) moments
+    NodeD *recd = nullptr;
+    NodeF *recf = nullptr;
+    dbl4 *tpos = nullptr;
+    uint32_t *tid = nullptr;
+    float4 *thi = nullptr, *tlo = nullptr;
+    uint32_t *dev_err = nullptr;
+    unsigned long long *d_counts = nullptr;
+    uint32_t *d_heavy = nullptr, *d_nheavy = nullptr;
+    double *d_total = nullptr;
+    int n_heavy = 0;
+    std::vector<uint32_t> heavy;
+    int final_buf = 0;
+
+    bool has_bodies = false, has_tree = false, tree_fp64 = false, tree_mixed = false;
+    bool counting = false, timing = false;
+    uint64_t counts[4] = {0, 0, 0, 0};
+    uint64_t launches = 0;              // kernels enqueued since the last reset
+    std::vector<cudaEvent_t> tev;       // per-step phase events (timing mode)
+    kd_stats stats{};
+    cudaEvent_t ev[6] = {};
+
+    std::vector<void *> owned;
+
+    int fail(int code, const char *fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *what) {
+        return fail(e == cudaErrorMemoryAllocation ? KD_ENOMEM : KD_ECUDA, "%s: %s", what,
+                    cudaGetErrorString(e));
+    }
+    template <typename T>
+    cudaError_t alloc(T **p, size_t count) {
+        cudaError_t e = dalloc(p, count);
+        if (e == cudaSuccess) owned.push_back((void *)*p);
+        return e;
+    }
+};
+
+namespace {
+
+#define KD_CHECK(ctx, expr)                                      \
+    do {                                                         \
+        cudaError_t e_ = (expr);                                 \
+        if (e_ != cudaSuccess) return (ctx)->cuda_fail(e_, #expr); \
+    } while (0)
+
+int upload(kd_ctx *c, uint32_t **dst, const std::vector<uint32_t> &src) {
+    KD_CHECK(c, c->alloc(dst, src.size()));
+    if (!src.empty())
+        KD_CHECK(c, cudaMemcpy(*dst, src.data(), src.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice));
+    return KD_OK;
+}
+
+int setup(kd_ctx *c) {
+    const size_t n = c->n;
+    Plan &p = c->plan;
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    KD_CHECK(c, cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    for (auto &e : c->ev) KD_CHECK(c, cudaEventCreate(&e));
+    int rc;
+    if ((rc = upload(c, &c->d_start, p.start))) return rc;
+    if ((rc = upload(c, &c->d_count, p.count))) return rc;
+    if ((rc = upload(c, &c->d_right, p.right))) return rc;
+    if ((rc = upload(c, &c->d_parent, p.parent))) return rc;
+    if ((rc = upload(c, &c->d_leaves, p.leaves))) return rc;
+    if ((rc = upload(c, &c->d_ttab, p.ttab))) return rc;
+    if ((rc = upload(c, &c->d_local_roots, p.local_roots))) return rc;
+    c->d_glevels.resize(p.glevels.size());
+    size_t maxG = 1, maxGT = 1, maxGmulti = 1;
+    for (size_t l = 0; l < p.glevels.size(); ++l) {
+        if ((rc = upload(c, &c->d_glevels[l], p.glevels[l]))) return rc;
+        const size_t G = p.glevels[l].size();
+        const size_t tiles = (p.gmax[l] + kTile - 1) / kTile;
+        maxG = std::max(maxG, G);
+        maxGT = std::max(maxGT, G * tiles);
+        if (p.gmax[l] > kMultiMin) maxGmulti = std::max(maxGmulti, G);
+    }
+    Topology &t = c->topo;
+    t.n = (uint32_t)n;
+    t.leaf = p.leaf;
+    t.n_nodes = p.n_nodes;
+    t.n_leaves = (uint32_t)p.leaves.size();
+    t.start = c->d_start;
+    t.count = c->d_count;
+    t.right = c->d_right;
+    t.parent = c->d_parent;
+    t.leaves = c->d_leaves;
+    t.ttab = c->d_ttab;
+
+    Bodies &b = c->bodies;
+    KD_CHECK(c, c->alloc(&b.x, n));
+    KD_CHECK(c, c->alloc(&b.y, n));
+    KD_CHECK(c, c->alloc(&b.z, n));
+    KD_CHECK(c, c->alloc(&b.vx, n));
+    KD_CHECK(c, c->alloc(&b.vy, n));
+    KD_CHECK(c, c->alloc(&b.vz, n));
+    KD_CHECK(c, c->alloc(&b.m, n));
+    KD_CHECK(c, c->alloc(&b.r, n));
+    KD_CHECK(c, c->alloc(&c->acc, 3 * n));
+    KD_CHECK(c, c->alloc((double **)&c->aos, 8 * n));
+    for (int k = 0; k < 2; ++k) {
+        KD_CHECK(c, c->alloc(&c->work.x[k], n));
+        KD_CHECK(c, c->alloc(&c->work.y[k], n));
+        KD_CHECK(c, c->alloc(&c->work.z[k], n));
+        KD_CHECK(c, c->alloc(&c->work.id[k], n));
+        KD_CHECK(c, c->alloc(&c->scr.ckey[k], n));
+        KD_CHECK(c, c->alloc(&c->scr.cpos[k], n));
+    }
+    KD_CHECK(c, c->alloc(&c->scr.bmin, 3 * maxG));
+    KD_CHECK(c, c->alloc(&c->scr.bmax, 3 * maxG));
+    KD_CHECK(c, c->alloc(&c->scr.sel, maxG));
+    KD_CHECK(c, c->alloc(&c->scr.hist, (size_t)kHistBins * maxGmulti));
+    KD_CHECK(c, c->alloc(&c->scr.cand_cnt, maxG));
+    KD_CHECK(c, c->alloc(&c->scr.tile_cnt, maxGT));
+    KD_CHECK(c, c->alloc(&c->scr.tile_off, maxGT));
+    KD_CHECK(c, c->alloc(&c->dev_err, 1));
+    c->scr.err = c->dev_err;
+    const size_t nn = p.n_nodes;
+    KD_CHECK(c, c->alloc(&c->nout.split_dim, nn));
+    KD_CHECK(c, c->alloc(&c->nout.split_val, nn));
+    KD_CHECK(c, c->alloc(&c->nout.size, nn));
+    KD_CHECK(c, c->alloc(&c->mom.M, nn));
+    KD_CHECK(c, c->alloc(&c->mom.S, 3 * nn));
+    KD_CHECK(c, c->alloc(&c->mom.counter, nn));
+    KD_CHECK(c, c->alloc(&c->momf.M, nn));
+    KD_CHECK(c, c->alloc(&c->momf.S, 3 * nn));
+    c->momf.counter = c->mom.counter;
+    KD_CHECK(c, c->alloc(&c->recd, nn));
+    KD_CHECK(c, c->alloc(&c->recf, nn));
+    KD_CHECK(c, c->alloc(&c->tpos, n));
+    KD_CHECK(c, c->alloc(&c->tid, n));
+    KD_CHECK(c, c->alloc(&c->thi, n));
+    KD_CHECK(c, c->alloc(&c->tlo, n));
+    KD_CHECK(c, c->alloc(&c->d_counts, 4));
+    KD_CHECK(c, c->alloc(&c->d_heavy, kMaxHeavy));
+    KD_CHECK(c, c->alloc(&c->d_nheavy, 1));
+    KD_CHECK(c, c->alloc(&c->d_total, 1));
+    KD_CHECK(c, cudaMemset(c->dev_err, 0, sizeof(uint32_t)));
+    KD_CHECK(c, cudaMemset(c->nout.split_dim, 0, nn));
+    KD_CHECK(c, cudaMemset(c->nout.split_val, 0, nn * sizeof(double)));
+    KD_CHECK(c, cudaMemset(c->nout.size, 0, nn * sizeof(double)));
+    return KD_OK;
+}
+
+// Read and clear the device error word; translate it.
+int check_device(kd_ctx *c) {
+    uint32_t e = 0;
+    KD_CHECK(c, cudaMemcpyAsync(&e, c->dev_err, sizeof e, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaStreamSynchronize(c->st));
+    if (e) {
+        KD_CHECK(c, cudaMemsetAsync(c->dev_err, 0, sizeof(uint32_t), c->st));
+        if (e & kErrNumeric)
+            return c->fail(KD_ENUMERIC, "non-finite position/velocity/mass or negative mass");
+        if (e & kErrStack) return c->fail(KD_EDEVICE, "traversal stack overflow");
+        if (e & kErrSelect) return c->fail(KD_EDEVICE, "median select failed to converge");
+        return c->fail(KD_EDEVICE, "device check failed (0x%x)", e);
+    }
+    return KD_OK;
+}
+
+// Build: multi-block levels, then the shared-memory subtree finish.  Leaves the bodies in
+// tree order in tpos/tid.
+void enqueue_build(kd_ctx *c) {
+    Plan &p = c->plan;
+    launch_init_work(c->bodies, c->work, (uint32_t)c->n, c->st);
+    c->launches += 2;  // init + local finish
+    int cur = 0;
+    for (size_t l = 0; l < p.glevels.size(); ++l) {
+        LevelArgs lv;
+        lv.ids = c->d_glevels[l];
+        lv.G = (uint32_t)p.glevels[l].size();
+        lv.tiles = (p.gmax[l] + kTile - 1) / kTile;
+        lv.multi = p.gmax[l] > kMultiMin;
+        c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, c->st);
+        cur ^= 1;
+    }
+    launch_local(c->topo, c->d_local_roots, (uint32_t)p.local_roots.size(), c->nout, c->work,
+                 cur, c->bodies.m, c->tpos, c->tid, c->st);
+    c->final_buf = cur;
+}
+
+void enqueue_moments(kd_ctx *c, bool fp64, bool mixed) {
+    c->launches += (fp64 ? 1 : 0) + (mixed ? 2 : 0);
+    if (fp64) launch_moments_fp64(c->topo, c->nout, c->tpos, c->mom, c->recd, c->st);
+    if (mixed) {
+        launch_split_mixed(c->tpos, c->tid, c->d_heavy, c->n_heavy, (uint32_t)c->n, c->thi,
+                           c->tlo, c->st);
+        launch_moments_mixed(c->topo, c->nout, c->tpos, c->thi, c->momf, c->recf, c->st);
+    }
+}
+
+void enqueue_walk(kd_ctx *c) {
+    c->launches += 1;
+    unsigned long long *cnt = c->counting ? c->d_counts : nullptr;
+    if (c->prm.precision == KD_PREC_MIXED)
+        launch_walk_mixed(c->recf, c->thi, c->tlo, c->tid, (uint32_t)c->n, c->prm.theta,
+                          c->bodies, c->d_heavy, c->n_heavy, c->acc, c->dev_err, cnt, c->st);
+    else
+        launch_walk_fp64(c->recd, c->tpos, c->tid, (uint32_t)c->n, c->prm.theta, c->acc,
+                         c->dev_err, cnt, c->st);
+}
+
+int fetch_counts(kd_ctx *c) {
+    if (!c->counting) return KD_OK;
+    unsigned long long h[4];
+    KD_CHECK(c, cudaMemcpyAsync(h, c->d_counts, sizeof h, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaStreamSynchronize(c->st));
+    for (int i = 0; i < 4; ++i) c->counts[i] = h[i];
+    return KD_OK;
+}
+
+int reset_counts(kd_ctx *c) {
+    if (c->counting) KD_CHECK(c, cudaMemsetAsync(c->d_counts, 0, 4 * sizeof(unsigned long long), c->st));
+    return KD_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+
+extern "C" {
+
+void kd_default_params(kd_params *p) {
+    if (!p) return;
+    p->leaf_size = 7;
+    p->layout = KD_LAYOUT_DFS;
+    p->precision = KD_PREC_FP64;
+    p->device = 0;
+    p->theta = 0.3;
+    p->dt = 1e-3;
+    p->heavy_frac = 1e-3;
+    p->seed = 0;
+}
+
+size_t kd_nodes_needed(size_t n, int32_t leaf_size, int32_t layout) {
+    if (leaf_size < 2 || leaf_size > KD_MAX_LEAF) return 0;
+    return layout == KD_LAYOUT_PAR4 ? (size_t)needed_par(n, (uint32_t)leaf_size)
+                                    : (size_t)needed_seq(n, (uint32_t)leaf_size);
+}
+
+const char *kd_last_error(const kd_ctx *ctx) {
+    return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+kd_ctx *kd_create(size_t n, const kd_params *params) {
+    kd_params prm;
+    if (params)
+        prm = *params;
+    else
+        kd_default_params(&prm);
+    if (n < 1 || n >= (1ull << 31)) {
+        g_create_error = "n must be in [1, 2^31)";
+        return nullptr;
+    }
+    if (prm.leaf_size < 2 || prm.leaf_size > KD_MAX_LEAF) {
+        g_create_error = "leaf_size must be in [2, 8]";
+        return nullptr;
+    }
+    if (prm.layout != KD_LAYOUT_DFS && prm.layout != KD_LAYOUT_PAR4) {
+        g_create_error = "unknown layout";
+        return nullptr;
+    }
+    if (prm.precision != KD_PREC_FP64 && prm.precision != KD_PREC_MIXED) {
+        g_create_error = "unknown precision";
+        return nullptr;
+    }
+    if (!(prm.theta >= 0.0) || !std::isfinite(prm.theta)) {
+        g_create_error = "theta must be finite and >= 0";
+        return nullptr;
+    }
+    kd_ctx *c = new (std::nothrow) kd_ctx();
+    if (!c) {
+        g_create_error = "out of host memory";
+        return nullptr;
+    }
+    c->n = n;
+    c->prm = prm;
+    std::string perr;
+    if (!make_plan((uint32_t)n, (uint32_t)prm.leaf_size, c->plan, perr)) {
+        g_create_error = perr;
+        delete c;
+        return nullptr;
+    }
+    if (prm.layout == KD_LAYOUT_PAR4 && !c->plan.par4_ok) {
+        g_create_error = "PAR4 node slots exhausted for this n (build_tree_par4 would panic)";
+        delete c;
+        return nullptr;
+    }
+    if (setup(c) != KD_OK) {
+        g_create_error = c->err;
+        kd_destroy(c);
+        return nullptr;
+    }
+    return c;
+}
+
+void kd_destroy(kd_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->prm.device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    for (void *p : c->owned) cudaFree(p);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : c->tev)
+        if (e) cudaEventDestroy(e);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+}
+
+int kd_set_bodies(kd_ctx *c, const kd_particle_c *bodies, size_t n) {
+    if (!c) return KD_EINVAL;
+    if (!bodies || n != c->n) return c->fail(KD_EINVAL, "expected %zu bodies", c->n);
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    KD_CHECK(c, cudaMemcpyAsync(c->aos, bodies, n * sizeof(kd_particle_c),
+                                cudaMemcpyHostToDevice, c->st));
+    launch_aos_to_soa(c->aos, c->bodies, (uint32_t)n, c->dev_err, c->st);
+    launch_find_heavy(c->bodies, (uint32_t)n, c->prm.heavy_frac > 0 ? c->prm.heavy_frac : 2.0,
+                      c->d_total, c->d_heavy, c->d_nheavy, c->dev_err, c->st);
+    uint32_t nh = 0;
+    uint32_t ids[kMaxHeavy];
+    KD_CHECK(c, cudaMemcpyAsync(&nh, c->d_nheavy, sizeof nh, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaMemcpyAsync(ids, c->d_heavy, sizeof ids, cudaMemcpyDeviceToHost, c->st));
+    int rc = check_device(c);
+    c->has_tree = false;
+    if (rc) {
+        c->has_bodies = false;
+        return rc;
+    }
+    c->heavy.assign(ids, ids + std::min<uint32_t>(nh, kMaxHeavy));
+    std::sort(c->heavy.begin(), c->heavy.end());
+    c->n_heavy = (int)c->heavy.size();
+    if (nh > (uint32_t)kMaxHeavy) {
+        c->n_heavy = 0;
+        c->heavy.clear();
+        if (c->prm.precision == KD_PREC_MIXED) {
+            c->has_bodies = false;
+            return c->fail(KD_EINVAL, "%u bodies exceed heavy_frac of the total mass; at most %d",
+                           nh, kMaxHeavy);
+        }
+    }
+    if (c->n_heavy)
+        KD_CHECK(c, cudaMemcpyAsync(c->d_heavy, c->heavy.data(), c->n_heavy * sizeof(uint32_t),
+                                    cudaMemcpyHostToDevice, c->st));
+    c->has_bodies = true;
+    return KD_OK;
+}
+
+int kd_get_bodies(kd_ctx *c, kd_particle_c *bodies, size_t n) {
+    if (!c) return KD_EINVAL;
+    if (!bodies || n != c->n) return c->fail(KD_EINVAL, "expected %zu bodies", c->n);
+    if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    launch_soa_to_aos(c->bodies, c->aos, (uint32_t)n, c->st);
+    KD_CHECK(c, cudaMemcpyAsync(bodies, c->aos, n * sizeof(kd_particle_c),
+                                cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaStreamSynchronize(c->st));
+    return KD_OK;
+}
+
+int kd_build_tree(kd_ctx *c, size_t *last_node) {
+    if (!c) return KD_EINVAL;
+    if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
+    enqueue_build(c);
+    KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
+    enqueue_moments(c, true, c->prm.precision == KD_PREC_MIXED);
+    KD_CHECK(c, cudaEventRecord(c->ev[2], c->st));
+    KD_CHECK(c, cudaGetLastError());
+    int rc = check_device(c);
+    if (rc) return rc;
+    c->stats = kd_stats{};
+    c->stats.build_ms = elapsed(c->ev[0], c->ev[1]);
+    c->stats.moments_ms = elapsed(c->ev[1], c->ev[2]);
+    c->stats.total_ms = elapsed(c->ev[0], c->ev[2]);
+    c->has_tree = true;
+    c->tree_fp64 = true;
+    c->tree_mixed = c->prm.precision == KD_PREC_MIXED;
+    if (last_node)
+        *last_node = c->prm.layout == KD_LAYOUT_PAR4 ? (size_t)c->plan.par4_last
+                                                     : (size_t)c->plan.n_nodes - 1;
+    return KD_OK;
+}
+
+int kd_get_nodes(kd_ctx *c, kd_node_c *out, size_t cap, size_t *count) {
+    if (!c) return KD_EINVAL;
+    if (!c->has_tree || !c->tree_fp64) return c->fail(KD_ESTATE, "no tree built");
+    const Plan &p = c->plan;
+    const size_t need = c->prm.layout == KD_LAYOUT_PAR4 ? p.par4_slots : p.n_nodes;
+    if (!out || cap < need) return c->fail(KD_EINVAL, "need %zu node slots", need);
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    const size_t nn = p.n_nodes;
+    std::vector<uint8_t> sd(nn);
+    std::vector<double> sv(nn), sz(nn), M(nn), S(3 * nn);
+    std::vector<uint32_t> tid(c->n);
+    KD_CHECK(c, cudaMemcpyAsync(sd.data(), c->nout.split_dim, nn, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaMemcpyAsync(sv.data(), c->nout.split_val, nn * 8, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaMemcpyAsync(sz.data(), c->nout.size, nn * 8, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaMemcpyAsync(M.data(), c->mom.M, nn * 8, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaMemcpyAsync(S.data(), c->mom.S, 3 * nn * 8, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaMemcpyAsync(tid.data(), c->tid, c->n * 4, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaStreamSynchronize(c->st));
+    const bool par4 = c->prm.layout == KD_LAYOUT_PAR4;
+    if (par4) {
+        // unused slots stay as allocate_node_vec leaves them: Leaf{0, [usize::MAX; MAX]}
+        for (size_t i = 0; i < need; ++i) {
+            memset(&out[i], 0, sizeof(kd_node_c));
+            for (int k = 0; k < KD_MAX_LEAF; ++k) out[i].particles[k] = ~0ull;
+        }
+    }
+    auto slot = [&](uint32_t id) -> size_t { return par4 ? (size_t)p.par4[id] : (size_t)id; };
+    for (uint32_t id = 0; id < nn; ++id) {
+        kd_node_c &o = out[slot(id)];
+        memset(&o, 0, sizeof o);
+        if (p.count[id] > p.leaf) {
+            o.num_parts = 0;
+            o.split_dim = sd[id];
+            o.split_val = sv[id];
+            o.m = M[id];
+            o.cm[0] = S[3 * id] / M[id];
+            o.cm[1] = S[3 * id + 1] / M[id];
+            o.cm[2] = S[3 * id + 2] / M[id];
+            o.size = sz[id];
+            o.left = slot(id + 1);
+            o.right = slot(p.right[id]);
+        } else {
+            o.num_parts = p.count[id];
+            for (uint32_t k = 0; k < p.count[id]; ++k) o.particles[k] = tid[p.start[id] + k];
+        }
+    }
+    if (count) *count = need;
+    return KD_OK;
+}
+
+int kd_calc_accel(kd_ctx *c, double *acc) {
+    if (!c) return KD_EINVAL;
+    if (!acc) return c->fail(KD_EINVAL, "acc is NULL");
+    if (!c->has_tree) return c->fail(KD_ESTATE, "no tree built");
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    const bool mixed = c->prm.precision == KD_PREC_MIXED;
+    if (mixed && !c->tree_mixed) {
+        enqueue_moments(c, false, true);
+        c->tree_mixed = true;
+    }
+    int rc = reset_counts(c);
+    if (rc) return rc;
+    KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
+    enqueue_walk(c);
+    KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
+    KD_CHECK(c, cudaGetLastError());
+    KD_CHECK(c, cudaMemcpyAsync(acc, c->acc, 3 * c->n * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->st));
+    rc = check_device(c);
+    if (rc) return rc;
+    c->stats = kd_stats{};
+    c->stats.walk_ms = elapsed(c->ev[0], c->ev[1]);
+    c->stats.total_ms = c->stats.walk_ms;
+    return fetch_counts(c);
+}
+
+int kd_simple_sim(kd_ctx *c, double dt, int64_t steps) {
+    if (!c) return KD_EINVAL;
+    if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
+    if (steps < 0) return c->fail(KD_EINVAL, "steps must be >= 0");
+    if (dt == 0.0) dt = c->prm.dt;
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    const bool mixed = c->prm.precision == KD_PREC_MIXED;
+    int rc = reset_counts(c);
+    if (rc) return rc;
+    const size_t nev = c->timing ? 5 * (size_t)steps : 0;
+    while (c->tev.size() < nev) {
+        cudaEvent_t e;
+        KD_CHECK(c, cudaEventCreate(&e));
+        c->tev.push_back(e);
+    }
+    c->launches = 0;
+    KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
+    for (int64_t s = 0; s < steps; ++s) {
+        cudaEvent_t *e = c->timing ? &c->tev[5 * (size_t)s] : nullptr;
+        if (e) KD_CHECK(c, cudaEventRecord(e[0], c->st));
+        enqueue_build(c);
+        if (e) KD_CHECK(c, cudaEventRecord(e[1], c->st));
+        enqueue_moments(c, !mixed, mixed);
+        if (e) KD_CHECK(c, cudaEventRecord(e[2], c->st));
+        enqueue_walk(c);
+        if (e) KD_CHECK(c, cudaEventRecord(e[3], c->st));
+        launch_kick_drift(c->bodies, c->acc, (uint32_t)c->n, dt, c->st);
+        c->launches += 1;
+        if (e) KD_CHECK(c, cudaEventRecord(e[4], c->st));
+    }
+    KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
+    KD_CHECK(c, cudaGetLastError());
+    rc = check_device(c);
+    c->has_tree = false;  // the tree no longer matches the moved bodies
+    if (rc) return rc;
+    c->stats = kd_stats{};
+    c->stats.total_ms = elapsed(c->ev[0], c->ev[1]);
+    c->stats.steps = (uint64_t)steps;
+    c->stats.launches = c->launches;
+    for (int64_t s = 0; s < (c->timing ? steps : 0); ++s) {
+        cudaEvent_t *e = &c->tev[5 * (size_t)s];
+        c->stats.build_ms += elapsed(e[0], e[1]);
+        c->stats.moments_ms += elapsed(e[1], e[2]);
+        c->stats.walk_ms += elapsed(e[2], e[3]);
+        c->stats.kick_ms += elapsed(e[3], e[4]);
+    }
+    return fetch_counts(c);
+}
+
+int kd_set_precision(kd_ctx *c, int32_t precision) {
+    if (!c) return KD_EINVAL;
+    if (precision != KD_PREC_FP64 && precision != KD_PREC_MIXED)
+        return c->fail(KD_EINVAL, "unknown precision");
+    c->prm.precision = precision;
+    return KD_OK;
+}
+
+int kd_get_stats(const kd_ctx *c, kd_stats *out) {
+    if (!c || !out) return KD_EINVAL;
+    *out = c->stats;
+    return KD_OK;
+}
+
+int kd_set_timing(kd_ctx *c, int32_t on) {
+    if (!c) return KD_EINVAL;
+    c->timing = on != 0;
+    return KD_OK;
+}
+
+int kd_direct_accel(kd_ctx *c, const uint64_t *sinks, size_t ns, double *acc) {
+    if (!c) return KD_EINVAL;
+    if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
+    if (!sinks || !acc || ns == 0 || ns > (1u << 24))
+        return c->fail(KD_EINVAL, "need 1 <= ns <= 2^24 sinks and output storage");
+    for (size_t k = 0; k < ns; ++k)
+        if (sinks[k] >= c->n) return c->fail(KD_EINVAL, "sink %zu out of range", k);
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    const size_t chunks = (c->n + kDirectChunk - 1) / kDirectChunk;
+    uint64_t *d_sinks = nullptr;
+    double *d_part = nullptr, *d_acc = nullptr;
+    cudaError_t e = cudaMalloc((void **)&d_sinks, ns * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_part, 3 * ns * chunks * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d_acc, 3 * ns * sizeof(double));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_sinks, sinks, ns * sizeof(uint64_t), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) {
+        launch_direct(c->bodies, (uint32_t)c->n, d_sinks, (uint32_t)ns, d_part, d_acc, c->st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(acc, d_acc, 3 * ns * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    cudaFree(d_sinks);
+    cudaFree(d_part);
+    cudaFree(d_acc);
+    if (e != cudaSuccess) return c->cuda_fail(e, "kd_direct_accel");
+    return KD_OK;
+}
+
+int kd_set_counting(kd_ctx *c, int32_t on) {
+    if (!c) return KD_EINVAL;
+    c->counting = on != 0;
+    return KD_OK;
+}
+
+int kd_get_counts(const kd_ctx *c, uint64_t out[4]) {
+    if (!c || !out) return KD_EINVAL;
+    for (int i = 0; i < 4; ++i) out[i] = c->counts[i];
+    return KD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,156 @@
+// kd_internal.cuh -- device data layout and launch wrappers shared by the build, walk and
+// API translation units of libkdnbody.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace kd {
+
+// 32-byte aligned (x, y, z, mass) body record in tree order
+using dbl4 = double4_32a;
+
+__device__ __forceinline__ dbl4 ldg_dbl4(const dbl4 *p) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    return make_double4_32a(a.x, a.y, b.x, b.y);
+}
+
+// ---------------------------------------------------------------- tuning constants
+constexpr int kLocalMax = 1024;     // segments this small finish their whole subtree in
+                                    // one thread block, in shared memory
+constexpr int kLocalThreads = 256;
+constexpr int kTile = 2048;         // elements per block in the multi-block level passes
+constexpr int kTileThreads = 256;
+constexpr int kHistBits = 12;       // radix digit of the median select
+constexpr int kHistBins = 1 << kHistBits;
+constexpr int kSelCap = 2048;       // candidates sorted in shared memory by one block
+constexpr int kSelThreads = 512;
+constexpr uint32_t kMultiMin = 32768;  // segments above this use multi-block histograms
+constexpr int kSelMaxIters = 16;    // radix refinement passes before giving up (error)
+constexpr int kWalkWarps = 4;       // warps per walk block
+constexpr int kStackMax = 64;       // per-warp traversal stack entries
+constexpr int kMaxHeavy = 8;        // bodies summed directly in FP64 on the mixed path
+
+// device error flags (bit set in ctx->dev_err)
+constexpr uint32_t kErrSelect = 1u;   // median select did not converge
+constexpr uint32_t kErrStack = 2u;    // traversal stack overflow
+constexpr uint32_t kErrNumeric = 4u;  // non-finite or negative input
+constexpr uint32_t kErrHeavy = 8u;    // more heavy bodies than kMaxHeavy
+
+// ---------------------------------------------------------------- node records
+// Walk record of the FP64 path.  Internal: a = right child (DFS id), b = 0; the left child
+// is always id+1.  Leaf: a = first body in tree order, b = body count (>= 1).
+struct __align__(16) NodeD {
+    double cmx, cmy, cmz, m;
+    double size2;
+    uint32_t a, b;
+    double pad;
+};
+static_assert(sizeof(NodeD) == 56 || sizeof(NodeD) == 64, "NodeD layout");
+
+// Walk record of the mixed path: centre of mass as hi+lo floats, light mass, size^2.
+struct __align__(16) NodeF {
+    float4 hi;  // cm hi x,y,z ; light mass
+    float4 lo;  // cm lo x,y,z ; size^2
+    uint32_t a, b, pad0, pad1;
+};
+
+// Per-segment state of the median select at one level of the multi-block build.
+struct SegSel {
+    uint32_t sd;      // split dimension
+    uint32_t shift;   // first-pass digit shift
+    uint32_t digit;   // selected first-pass digit
+    uint32_t c;       // candidates left
+    uint32_t r;       // rank wanted among the candidates
+    uint32_t pad;
+    uint64_t kmed;    // median key (order-preserving transform of the coordinate)
+    uint32_t idmed;   // median body id (tie break)
+    uint32_t posmed;  // position of the median inside the segment
+};
+
+// ---------------------------------------------------------------- argument blocks
+struct Topology {          // static per (n, leaf), DFS ids
+    uint32_t n, leaf, n_nodes, n_leaves;
+    const uint32_t *start;   // first body (tree order) of every node
+    const uint32_t *count;   // bodies of every node
+    const uint32_t *right;   // right child of internal nodes
+    const uint32_t *parent;  // parent, 0xffffffff at the root
+    const uint32_t *leaves;  // DFS ids of the leaves
+    const uint32_t *ttab;    // DFS subtree size for 0..kLocalMax bodies
+};
+
+struct NodeOut {           // per-node results of the build
+    uint8_t *split_dim;
+    double *split_val;
+    double *size;
+};
+
+struct LevelArgs {
+    const uint32_t *ids;     // internal nodes of this level
+    uint32_t G;              // number of segments
+    uint32_t tiles;          // tiles per segment
+    bool multi;              // multi-block select
+};
+
+struct Work {              // ping-pong buffers of the level passes (segment order)
+    double *x[2], *y[2], *z[2];
+    uint32_t *id[2];
+};
+
+struct Scratch {
+    unsigned long long *bmin, *bmax;  // [G*3] ordered keys
+    SegSel *sel;
+    uint32_t *hist;                   // [G*kHistBins]
+    uint32_t *cand_cnt;               // [G]
+    unsigned long long *ckey[2];      // [n] candidate keys
+    uint32_t *cpos[2];                // [n] candidate positions
+    uint32_t *tile_cnt, *tile_off;    // [G*tiles]
+    uint32_t *err;
+};
+
+struct Bodies {             // master state, original order
+    double *x, *y, *z, *vx, *vy, *vz, *m, *r;
+};
+
+// ---------------------------------------------------------------- launchers (kd_build.cu)
+void launch_init_work(const Bodies &b, Work &w, uint32_t n, cudaStream_t st);
+// returns the number of kernels it launched
+int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
+                 Scratch &s, cudaStream_t st);
+void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
+                  const NodeOut &no, const Work &w, int cur, const double *mass,
+                  dbl4 *tpos, uint32_t *tid, cudaStream_t st);
+
+// ---------------------------------------------------------------- launchers (kd_walk.cu)
+struct Moments {
+    double *M;                // [n_nodes]
+    double *S;                // [3*n_nodes] sum m*p
+    uint32_t *counter;        // [n_nodes] arrival counters
+};
+
+void launch_moments_fp64(const Topology &t, const NodeOut &no, const dbl4 *tpos,
+                         Moments &mo, NodeD *rec, cudaStream_t st);
+void launch_split_mixed(const dbl4 *tpos, const uint32_t *tid, const uint32_t *heavy_ids,
+                        int n_heavy, uint32_t n, float4 *thi, float4 *tlo, cudaStream_t st);
+void launch_moments_mixed(const Topology &t, const NodeOut &no, const dbl4 *tpos,
+                          const float4 *thi, Moments &mo, NodeF *rec, cudaStream_t st);
+void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
+                      double theta, double *acc, uint32_t *err,
+                      unsigned long long *counts, cudaStream_t st);
+void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
+                       const uint32_t *tid, uint32_t n, double theta, const Bodies &b,
+                       const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
+                       unsigned long long *counts, cudaStream_t st);
+void launch_kick_drift(Bodies &b, double *acc, uint32_t n, double dt, cudaStream_t st);
+void launch_aos_to_soa(const void *aos, Bodies &b, uint32_t n, uint32_t *err, cudaStream_t st);
+void launch_soa_to_aos(const Bodies &b, void *aos, uint32_t n, cudaStream_t st);
+// FP64 direct sum for ns sinks; `partial` holds ns * ceil(n / kDirectChunk) * 3 doubles
+constexpr uint32_t kDirectChunk = 1u << 18;
+constexpr int kDirectThreads = 128;
+void launch_direct(const Bodies &b, uint32_t n, const uint64_t *sinks, uint32_t ns,
+                   double *partial, double *acc, cudaStream_t st);
+void launch_find_heavy(const Bodies &b, uint32_t n, double frac, double *scratch_total,
+                       uint32_t *heavy_ids, uint32_t *n_heavy, uint32_t *err, cudaStream_t st);
+
+}  // namespace kd

@@ -1,0 +1,647 @@
+// kd_walk.cu -- multipole upward pass, theta-opening traversal and kick-drift.
+//
+// FP64 path: every body gets exactly the interaction set of the reference's recursive walk
+// (MarkCLewis/MultiLanguageKDTree Parallel/RustVersion/src/array_kd_tree.rs:585-621): a
+// warp walks the union of its 32 bodies' walks with a shared stack, and a per-lane mask
+// records which bodies still descend.  The opening test and both force kernels use the
+// reference's IEEE operation order (array_kd_tree.rs:601-609, array_particle.rs:67-76),
+// written with explicit round-to-nearest intrinsics so no multiply-add is fused.
+//
+// Mixed path: the same traversal in FP32 on split (hi + lo) coordinates, compensated
+// (Kahan) per-body sums, and the heavy bodies (the central mass of a ring) summed directly
+// in FP64 and left out of the FP32 node masses.
+#include "kd_internal.cuh"
+
+namespace kd {
+
+static constexpr uint32_t kFull = 0xffffffffu;
+static constexpr uint32_t kNone = 0xffffffffu;
+
+// ------------------------------------------------------------------ upward pass
+
+// One thread per leaf sums its bodies, then climbs: the second child to arrive at a parent
+// combines both children (left + right, a fixed order) and continues upward.
+__global__ void k_moments_fp64(Topology t, NodeOut no, const dbl4 *tpos, Moments mo,
+                               NodeD *rec) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= t.n_leaves) return;
+    const uint32_t id = t.leaves[i];
+    const uint32_t st = t.start[id], cn = t.count[id];
+    double M = 0.0, Sx = 0.0, Sy = 0.0, Sz = 0.0;
+    for (uint32_t k = st; k < st + cn; ++k) {
+        const dbl4 q = tpos[k];
+        M += q.w;
+        Sx = fma(q.w, q.x, Sx);
+        Sy = fma(q.w, q.y, Sy);
+        Sz = fma(q.w, q.z, Sz);
+    }
+    mo.M[id] = M;
+    mo.S[3 * id] = Sx;
+    mo.S[3 * id + 1] = Sy;
+    mo.S[3 * id + 2] = Sz;
+    NodeD r;
+    r.cmx = Sx; r.cmy = Sy; r.cmz = Sz; r.m = M;
+    r.size2 = 0.0;
+    r.a = st;
+    r.b = cn;
+    r.pad = 0.0;
+    rec[id] = r;
+    uint32_t node = t.parent[id];
+    while (node != kNone) {
+        __threadfence();
+        if (atomicAdd(&mo.counter[node], 1u) == 0u) return;
+        __threadfence();
+        const uint32_t L = node + 1, R = t.right[node];
+        const double m = __dadd_rn(__ldcg(&mo.M[L]), __ldcg(&mo.M[R]));
+        const double sx = __dadd_rn(__ldcg(&mo.S[3 * L]), __ldcg(&mo.S[3 * R]));
+        const double sy = __dadd_rn(__ldcg(&mo.S[3 * L + 1]), __ldcg(&mo.S[3 * R + 1]));
+        const double sz = __dadd_rn(__ldcg(&mo.S[3 * L + 2]), __ldcg(&mo.S[3 * R + 2]));
+        mo.M[node] = m;
+        mo.S[3 * node] = sx;
+        mo.S[3 * node + 1] = sy;
+        mo.S[3 * node + 2] = sz;
+        const double size = no.size[node];
+        NodeD q;
+        // cm /= m as array_kd_tree.rs:548-550; size*size as :606
+        q.cmx = __ddiv_rn(sx, m);
+        q.cmy = __ddiv_rn(sy, m);
+        q.cmz = __ddiv_rn(sz, m);
+        q.m = m;
+        q.size2 = __dmul_rn(size, size);
+        q.a = R;
+        q.b = 0u;
+        q.pad = 0.0;
+        rec[node] = q;
+        node = t.parent[node];
+    }
+}
+
+void launch_moments_fp64(const Topology &t, const NodeOut &no, const dbl4 *tpos,
+                         Moments &mo, NodeD *rec, cudaStream_t st) {
+    cudaMemsetAsync(mo.counter, 0, sizeof(uint32_t) * t.n_nodes, st);
+    k_moments_fp64<<<(t.n_leaves + 255) / 256, 256, 0, st>>>(t, no, tpos, mo, rec);
+}
+
+__device__ __forceinline__ bool is_heavy(uint32_t id, const uint32_t *heavy_ids, int n_heavy) {
+    bool h = false;
+    for (int i = 0; i < n_heavy; ++i) h |= heavy_ids[i] == id;
+    return h;
+}
+
+// Tree-ordered split coordinates: hi = fl32(x), lo = fl32(x - hi); heavy bodies get a zero
+// FP32 mass (their pull is added in FP64).
+__global__ void k_split_mixed(const dbl4 *tpos, const uint32_t *tid,
+                              const uint32_t *heavy_ids, int n_heavy, uint32_t n, float4 *thi,
+                              float4 *tlo) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += gridDim.x * blockDim.x) {
+        const dbl4 q = tpos[k];
+        const float hx = (float)q.x, hy = (float)q.y, hz = (float)q.z;
+        const float lx = (float)(q.x - (double)hx), ly = (float)(q.y - (double)hy),
+                    lz = (float)(q.z - (double)hz);
+        const float m = is_heavy(tid[k], heavy_ids, n_heavy) ? 0.0f : (float)q.w;
+        thi[k] = make_float4(hx, hy, hz, m);
+        tlo[k] = make_float4(lx, ly, lz, 0.0f);
+    }
+}
+
+void launch_split_mixed(const dbl4 *tpos, const uint32_t *tid, const uint32_t *heavy_ids,
+                        int n_heavy, uint32_t n, float4 *thi, float4 *tlo, cudaStream_t st) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 8192) blocks = 8192;
+    k_split_mixed<<<blocks, 256, 0, st>>>(tpos, tid, heavy_ids, n_heavy, n, thi, tlo);
+}
+
+__device__ __forceinline__ NodeF make_nodef(double sx, double sy, double sz, double m,
+                                            double size2, uint32_t a, uint32_t b) {
+    NodeF r;
+    const double cx = sx / m, cy = sy / m, cz = sz / m;  // NaN for massless nodes: never accepted
+    const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
+    r.hi = make_float4(hx, hy, hz, (float)m);
+    r.lo = make_float4((float)(cx - (double)hx), (float)(cy - (double)hy),
+                       (float)(cz - (double)hz), (float)size2);
+    r.a = a;
+    r.b = b;
+    r.pad0 = r.pad1 = 0u;
+    return r;
+}
+
+// Upward pass of the light (FP32-summed) masses.  Moments are accumulated in FP64.
+__global__ void k_moments_mixed(Topology t, NodeOut no, const dbl4 *tpos, const float4 *thi,
+                                Moments mo, NodeF *rec) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= t.n_leaves) return;
+    const uint32_t id = t.leaves[i];
+    const uint32_t st = t.start[id], cn = t.count[id];
+    double M = 0.0, Sx = 0.0, Sy = 0.0, Sz = 0.0;
+    for (uint32_t k = st; k < st + cn; ++k) {
+        const dbl4 q = tpos[k];
+        const double m = thi[k].w == 0.0f ? 0.0 : q.w;
+        M += m;
+        Sx = fma(m, q.x, Sx);
+        Sy = fma(m, q.y, Sy);
+        Sz = fma(m, q.z, Sz);
+    }
+    mo.M[id] = M;
+    mo.S[3 * id] = Sx;
+    mo.S[3 * id + 1] = Sy;
+    mo.S[3 * id + 2] = Sz;
+    rec[id] = make_nodef(Sx, Sy, Sz, M, 0.0, st, cn);
+    uint32_t node = t.parent[id];
+    while (node != kNone) {
+        __threadfence();
+        if (atomicAdd(&mo.counter[node], 1u) == 0u) return;
+        __threadfence();
+        const uint32_t L = node + 1, R = t.right[node];
+        const double m = __ldcg(&mo.M[L]) + __ldcg(&mo.M[R]);
+        const double sx = __ldcg(&mo.S[3 * L]) + __ldcg(&mo.S[3 * R]);
+        const double sy = __ldcg(&mo.S[3 * L + 1]) + __ldcg(&mo.S[3 * R + 1]);
+        const double sz = __ldcg(&mo.S[3 * L + 2]) + __ldcg(&mo.S[3 * R + 2]);
+        mo.M[node] = m;
+        mo.S[3 * node] = sx;
+        mo.S[3 * node + 1] = sy;
+        mo.S[3 * node + 2] = sz;
+        const double size = no.size[node];
+        rec[node] = make_nodef(sx, sy, sz, m, size * size, R, 0u);
+        node = t.parent[node];
+    }
+}
+
+void launch_moments_mixed(const Topology &t, const NodeOut &no, const dbl4 *tpos,
+                          const float4 *thi, Moments &mo, NodeF *rec, cudaStream_t st) {
+    cudaMemsetAsync(mo.counter, 0, sizeof(uint32_t) * t.n_nodes, st);
+    k_moments_mixed<<<(t.n_leaves + 255) / 256, 256, 0, st>>>(t, no, tpos, thi, mo, rec);
+}
+
+// ------------------------------------------------------------------ FP64 walk
+
+__device__ __forceinline__ void load_noded(const NodeD *rec, uint32_t node, double &cx,
+                                           double &cy, double &cz, double &m, double &s2,
+                                           uint32_t &a, uint32_t &b) {
+    const double2 *p = reinterpret_cast<const double2 *>(rec + node);
+    const double2 v0 = __ldg(p), v1 = __ldg(p + 1), v2 = __ldg(p + 2);
+    cx = v0.x; cy = v0.y; cz = v1.x; m = v1.y; s2 = v2.x;
+    const uint2 ab = __ldg(reinterpret_cast<const uint2 *>(p + 2) + 1);
+    a = ab.x;
+    b = ab.y;
+}
+
+template <bool kCount>
+__global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
+    const NodeD *__restrict__ rec, const dbl4 *__restrict__ tpos,
+    const uint32_t *__restrict__ tid, uint32_t n, double theta2, double *__restrict__ acc,
+    uint32_t *err, unsigned long long *counts) {
+    __shared__ uint2 stack[kWalkWarps][kStackMax];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t s = (blockIdx.x * kWalkWarps + warp) * 32 + lane;
+    const bool valid = s < n;
+    uint32_t mask = __ballot_sync(kFull, valid);
+    if (mask == 0) return;
+    const uint32_t bit = 1u << lane;
+    dbl4 me = valid ? tpos[s] : make_double4_32a(0.0, 0.0, 0.0, 0.0);
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
+    uint32_t node = 0;
+    int sp = 0;
+    while (true) {
+        double cx, cy, cz, m, s2;
+        uint32_t a, b;
+        load_noded(rec, node, cx, cy, cz, m, s2, a, b);
+        if (kCount) c_vis += (mask & bit) ? 1 : 0;
+        bool descend = false;
+        if (b != 0u) {
+            // leaf: sequential pair sum, self excluded by identity (array_kd_tree.rs:588-598)
+            if (mask & bit) {
+                for (uint32_t k = 0; k < b; ++k) {
+                    const uint32_t j = a + k;
+                    if (j == s) continue;
+                    const dbl4 q = ldg_dbl4(&tpos[j]);
+                    const double dx = __dsub_rn(me.x, q.x);
+                    const double dy = __dsub_rn(me.y, q.y);
+                    const double dz = __dsub_rn(me.z, q.z);
+                    const double dp2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                 __dmul_rn(dz, dz));
+                    const double dist = __dsqrt_rn(dp2);
+                    const double magi = __ddiv_rn(-q.w, __dmul_rn(__dmul_rn(dist, dist), dist));
+                    ax = __dadd_rn(ax, __dmul_rn(magi, dx));
+                    ay = __dadd_rn(ay, __dmul_rn(magi, dy));
+                    az = __dadd_rn(az, __dmul_rn(magi, dz));
+                    if (kCount) ++c_p2p;
+                }
+            }
+        } else {
+            bool take = false;
+            if (mask & bit) {
+                const double dx = __dsub_rn(me.x, cx);
+                const double dy = __dsub_rn(me.y, cy);
+                const double dz = __dsub_rn(me.z, cz);
+                const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                            __dmul_rn(dz, dz));
+                if (kCount) ++c_open;
+                if (s2 < __dmul_rn(theta2, d2)) {
+                    take = true;
+                    const double dist = __dsqrt_rn(d2);
+                    const double magi = __ddiv_rn(-m, __dmul_rn(d2, dist));
+                    ax = __dadd_rn(ax, __dmul_rn(dx, magi));
+                    ay = __dadd_rn(ay, __dmul_rn(dy, magi));
+                    az = __dadd_rn(az, __dmul_rn(dz, magi));
+                    if (kCount) ++c_m2p;
+                }
+            }
+            const uint32_t open = mask & ~__ballot_sync(kFull, take);
+            if (open) {
+                if (sp >= kStackMax) {
+                    if (lane == 0) atomicOr(err, kErrStack);
+                    break;
+                }
+                if (lane == 0) stack[warp][sp] = make_uint2(a, open);
+                ++sp;
+                node = node + 1;
+                mask = open;
+                descend = true;
+            }
+        }
+        if (descend) continue;
+        if (sp == 0) break;
+        __syncwarp();
+        --sp;
+        const uint2 e = stack[warp][sp];
+        node = e.x;
+        mask = e.y;
+        __syncwarp();
+    }
+    if (valid) {
+        const uint32_t o = tid[s];
+        acc[3 * (size_t)o] = ax;
+        acc[3 * (size_t)o + 1] = ay;
+        acc[3 * (size_t)o + 2] = az;
+    }
+    if (kCount) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            c_p2p += __shfl_xor_sync(kFull, c_p2p, o);
+            c_open += __shfl_xor_sync(kFull, c_open, o);
+            c_m2p += __shfl_xor_sync(kFull, c_m2p, o);
+            c_vis += __shfl_xor_sync(kFull, c_vis, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&counts[0], c_p2p);
+            atomicAdd(&counts[1], c_open);
+            atomicAdd(&counts[2], c_m2p);
+            atomicAdd(&counts[3], c_vis);
+        }
+    }
+}
+
+void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
+                      double theta, double *acc, uint32_t *err, unsigned long long *counts,
+                      cudaStream_t st) {
+    const uint32_t threads = kWalkWarps * 32;
+    const uint32_t blocks = (n + threads - 1) / threads;
+    const double theta2 = theta * theta;  // THETA * THETA is formed first (array_kd_tree.rs:606)
+    if (counts)
+        k_walk_fp64<true><<<blocks, threads, 0, st>>>(rec, tpos, tid, n, theta2, acc, err, counts);
+    else
+        k_walk_fp64<false><<<blocks, threads, 0, st>>>(rec, tpos, tid, n, theta2, acc, err,
+                                                       nullptr);
+}
+
+// ------------------------------------------------------------------ mixed walk
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
+    const float y = x - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+struct HeavyBody {
+    double x, y, z, m;
+};
+
+template <bool kCount>
+__global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
+    const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
+    const float4 *__restrict__ tlo, const uint32_t *__restrict__ tid, uint32_t n, float theta2,
+    Bodies b, const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
+    uint32_t *err, unsigned long long *counts) {
+    __shared__ uint2 stack[kWalkWarps][kStackMax];
+    __shared__ HeavyBody heavy[kMaxHeavy];
+    if (threadIdx.x < n_heavy) {
+        const uint32_t h = heavy_ids[threadIdx.x];
+        heavy[threadIdx.x] = HeavyBody{b.x[h], b.y[h], b.z[h], b.m[h]};
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t s = (blockIdx.x * kWalkWarps + warp) * 32 + lane;
+    const bool valid = s < n;
+    uint32_t mask = __ballot_sync(kFull, valid);
+    if (mask == 0) return;
+    const uint32_t bit = 1u << lane;
+    const float4 mh = valid ? thi[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 ml = valid ? tlo[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
+    uint32_t node = 0;
+    int sp = 0;
+    while (true) {
+        const NodeF r = rec[node];
+        if (kCount) c_vis += (mask & bit) ? 1 : 0;
+        bool descend = false;
+        if (r.b != 0u) {
+            if (mask & bit) {
+                float px = 0.f, py = 0.f, pz = 0.f;
+                for (uint32_t k = 0; k < r.b; ++k) {
+                    const uint32_t j = r.a + k;
+                    if (j == s) continue;
+                    const float4 qh = __ldg(&thi[j]);
+                    const float4 ql = __ldg(&tlo[j]);
+                    const float dx = (mh.x - qh.x) + (ml.x - ql.x);
+                    const float dy = (mh.y - qh.y) + (ml.y - ql.y);
+                    const float dz = (mh.z - qh.z) + (ml.z - ql.z);
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float inv = rsqrtf(d2);
+                    const float f = -qh.w * (inv * inv * inv);
+                    px = fmaf(f, dx, px);
+                    py = fmaf(f, dy, py);
+                    pz = fmaf(f, dz, pz);
+                    if (kCount) ++c_p2p;
+                }
+                kahan_add(sx, cx, px);
+                kahan_add(sy, cy, py);
+                kahan_add(sz, cz, pz);
+            }
+        } else {
+            bool take = false;
+            if (mask & bit) {
+                const float dx = (mh.x - r.hi.x) + (ml.x - r.lo.x);
+                const float dy = (mh.y - r.hi.y) + (ml.y - r.lo.y);
+                const float dz = (mh.z - r.hi.z) + (ml.z - r.lo.z);
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (kCount) ++c_open;
+                if (r.lo.w < theta2 * d2) {
+                    take = true;
+                    const float inv = rsqrtf(d2);
+                    const float f = -r.hi.w * (inv * inv * inv);
+                    kahan_add(sx, cx, f * dx);
+                    kahan_add(sy, cy, f * dy);
+                    kahan_add(sz, cz, f * dz);
+                    if (kCount) ++c_m2p;
+                }
+            }
+            const uint32_t open = mask & ~__ballot_sync(kFull, take);
+            if (open) {
+                if (sp >= kStackMax) {
+                    if (lane == 0) atomicOr(err, kErrStack);
+                    break;
+                }
+                if (lane == 0) stack[warp][sp] = make_uint2(r.a, open);
+                ++sp;
+                node = node + 1;
+                mask = open;
+                descend = true;
+            }
+        }
+        if (descend) continue;
+        if (sp == 0) break;
+        __syncwarp();
+        --sp;
+        const uint2 e = stack[warp][sp];
+        node = e.x;
+        mask = e.y;
+        __syncwarp();
+    }
+    if (valid) {
+        const uint32_t o = tid[s];
+        double ax = (double)sx - (double)cx;
+        double ay = (double)sy - (double)cy;
+        double az = (double)sz - (double)cz;
+        // heavy bodies in FP64, pair kernel of array_particle.rs:67-76
+        const double px = b.x[o], py = b.y[o], pz = b.z[o];
+        for (int h = 0; h < n_heavy; ++h) {
+            if (heavy_ids[h] == o) continue;
+            const HeavyBody q = heavy[h];
+            const double dx = px - q.x, dy = py - q.y, dz = pz - q.z;
+            const double dp2 = dx * dx + dy * dy + dz * dz;
+            const double dist = sqrt(dp2);
+            const double magi = -q.m / (dist * dist * dist);
+            ax += magi * dx;
+            ay += magi * dy;
+            az += magi * dz;
+        }
+        acc[3 * (size_t)o] = ax;
+        acc[3 * (size_t)o + 1] = ay;
+        acc[3 * (size_t)o + 2] = az;
+    }
+    if (kCount) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            c_p2p += __shfl_xor_sync(kFull, c_p2p, o);
+            c_open += __shfl_xor_sync(kFull, c_open, o);
+            c_m2p += __shfl_xor_sync(kFull, c_m2p, o);
+            c_vis += __shfl_xor_sync(kFull, c_vis, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&counts[0], c_p2p);
+            atomicAdd(&counts[1], c_open);
+            atomicAdd(&counts[2], c_m2p);
+            atomicAdd(&counts[3], c_vis);
+        }
+    }
+}
+
+void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
+                       const uint32_t *tid, uint32_t n, double theta, const Bodies &b,
+                       const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
+                       unsigned long long *counts, cudaStream_t st) {
+    const uint32_t threads = kWalkWarps * 32;
+    const uint32_t blocks = (n + threads - 1) / threads;
+    const float theta2 = (float)(theta * theta);
+    if (counts)
+        k_walk_mixed<true><<<blocks, threads, 0, st>>>(rec, thi, tlo, tid, n, theta2, b,
+                                                       heavy_ids, n_heavy, acc, err, counts);
+    else
+        k_walk_mixed<false><<<blocks, threads, 0, st>>>(rec, thi, tlo, tid, n, theta2, b,
+                                                        heavy_ids, n_heavy, acc, err, nullptr);
+}
+
+// ------------------------------------------------------------------ kick-drift
+
+// v += dt*a; p += dt*v (array_kd_tree.rs:649-658), IEEE order without fused multiply-add.
+__global__ void k_kick_drift(Bodies b, const double *__restrict__ acc, uint32_t n, double dt) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const double vx = __dadd_rn(b.vx[i], __dmul_rn(dt, acc[3 * (size_t)i]));
+        const double vy = __dadd_rn(b.vy[i], __dmul_rn(dt, acc[3 * (size_t)i + 1]));
+        const double vz = __dadd_rn(b.vz[i], __dmul_rn(dt, acc[3 * (size_t)i + 2]));
+        b.vx[i] = vx;
+        b.vy[i] = vy;
+        b.vz[i] = vz;
+        b.x[i] = __dadd_rn(b.x[i], __dmul_rn(dt, vx));
+        b.y[i] = __dadd_rn(b.y[i], __dmul_rn(dt, vy));
+        b.z[i] = __dadd_rn(b.z[i], __dmul_rn(dt, vz));
+    }
+}
+
+void launch_kick_drift(Bodies &b, double *acc, uint32_t n, double dt, cudaStream_t st) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_kick_drift<<<blocks, 256, 0, st>>>(b, acc, n, dt);
+}
+
+// ------------------------------------------------------------------ body transfer
+
+__global__ void k_aos_to_soa(const double *__restrict__ aos, Bodies b, uint32_t n,
+                             uint32_t *err) {
+    bool bad = false;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const double2 *p = reinterpret_cast<const double2 *>(aos + 8 * (size_t)i);
+        const double2 a0 = p[0], a1 = p[1], a2 = p[2], a3 = p[3];
+        b.x[i] = a0.x; b.y[i] = a0.y; b.z[i] = a1.x;
+        b.vx[i] = a1.y; b.vy[i] = a2.x; b.vz[i] = a2.y;
+        b.r[i] = a3.x; b.m[i] = a3.y;
+        bad |= !(isfinite(a0.x) && isfinite(a0.y) && isfinite(a1.x) && isfinite(a1.y) &&
+                 isfinite(a2.x) && isfinite(a2.y) && isfinite(a3.y) && a3.y >= 0.0);
+    }
+    if (__any_sync(__activemask(), bad) && bad) atomicOr(err, kErrNumeric);
+}
+
+void launch_aos_to_soa(const void *aos, Bodies &b, uint32_t n, uint32_t *err, cudaStream_t st) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_aos_to_soa<<<blocks, 256, 0, st>>>(static_cast<const double *>(aos), b, n, err);
+}
+
+__global__ void k_soa_to_aos(Bodies b, double *__restrict__ aos, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        double2 *p = reinterpret_cast<double2 *>(aos + 8 * (size_t)i);
+        p[0] = make_double2(b.x[i], b.y[i]);
+        p[1] = make_double2(b.z[i], b.vx[i]);
+        p[2] = make_double2(b.vy[i], b.vz[i]);
+        p[3] = make_double2(b.r[i], b.m[i]);
+    }
+}
+
+void launch_soa_to_aos(const Bodies &b, void *aos, uint32_t n, cudaStream_t st) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_soa_to_aos<<<blocks, 256, 0, st>>>(b, static_cast<double *>(aos), n);
+}
+
+// ------------------------------------------------------------------ direct sum
+
+// Sinks are spread one per thread; sources are swept in chunks of kDirectChunk bodies, one
+// chunk per grid column, staged through shared memory.  Each (sink, chunk) partial is
+// summed in source order; the chunks are then added in chunk order (deterministic).
+__global__ __launch_bounds__(kDirectThreads) void k_direct(Bodies b, uint32_t n,
+                                                          const uint64_t *__restrict__ sinks,
+                                                          uint32_t ns, double *partial) {
+    __shared__ double sx[kDirectThreads], sy[kDirectThreads], sz[kDirectThreads],
+        sm[kDirectThreads];
+    const uint32_t k = blockIdx.x * kDirectThreads + threadIdx.x;
+    const uint32_t chunk = blockIdx.y;
+    const uint32_t j0 = chunk * kDirectChunk, j1 = min(n, j0 + kDirectChunk);
+    const bool valid = k < ns;
+    const uint32_t i = valid ? (uint32_t)sinks[k] : 0u;
+    const double px = valid ? b.x[i] : 0.0, py = valid ? b.y[i] : 0.0, pz = valid ? b.z[i] : 0.0;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (uint32_t base = j0; base < j1; base += kDirectThreads) {
+        const uint32_t j = base + threadIdx.x;
+        __syncthreads();
+        if (j < j1) {
+            sx[threadIdx.x] = b.x[j];
+            sy[threadIdx.x] = b.y[j];
+            sz[threadIdx.x] = b.z[j];
+            sm[threadIdx.x] = b.m[j];
+        }
+        __syncthreads();
+        const uint32_t cnt = min((uint32_t)kDirectThreads, j1 - base);
+        for (uint32_t q = 0; q < cnt; ++q) {
+            if (base + q == i) continue;
+            const double dx = __dsub_rn(px, sx[q]);
+            const double dy = __dsub_rn(py, sy[q]);
+            const double dz = __dsub_rn(pz, sz[q]);
+            const double dp2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                         __dmul_rn(dz, dz));
+            const double dist = __dsqrt_rn(dp2);
+            const double magi = __ddiv_rn(-sm[q], __dmul_rn(__dmul_rn(dist, dist), dist));
+            ax = __dadd_rn(ax, __dmul_rn(magi, dx));
+            ay = __dadd_rn(ay, __dmul_rn(magi, dy));
+            az = __dadd_rn(az, __dmul_rn(magi, dz));
+        }
+    }
+    if (valid) {
+        double *o = partial + 3 * ((size_t)chunk * ns + k);
+        o[0] = ax;
+        o[1] = ay;
+        o[2] = az;
+    }
+}
+
+__global__ void k_direct_sum(const double *partial, uint32_t ns, uint32_t chunks, double *acc) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns) return;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (uint32_t c = 0; c < chunks; ++c) {
+        const double *o = partial + 3 * ((size_t)c * ns + k);
+        ax += o[0];
+        ay += o[1];
+        az += o[2];
+    }
+    acc[3 * (size_t)k] = ax;
+    acc[3 * (size_t)k + 1] = ay;
+    acc[3 * (size_t)k + 2] = az;
+}
+
+void launch_direct(const Bodies &b, uint32_t n, const uint64_t *sinks, uint32_t ns,
+                   double *partial, double *acc, cudaStream_t st) {
+    const uint32_t chunks = (n + kDirectChunk - 1) / kDirectChunk;
+    dim3 grid((ns + kDirectThreads - 1) / kDirectThreads, chunks);
+    k_direct<<<grid, kDirectThreads, 0, st>>>(b, n, sinks, ns, partial);
+    k_direct_sum<<<(ns + 255) / 256, 256, 0, st>>>(partial, ns, chunks, acc);
+}
+
+// ------------------------------------------------------------------ heavy bodies
+
+// Total mass in a fixed reduction order (one block), then every body at or above
+// frac * total is listed (unordered; the host sorts the short list).
+__global__ __launch_bounds__(1024) void k_total_mass(const double *m, uint32_t n, double *out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += m[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        *out = t;
+    }
+}
+
+__global__ void k_heavy(const double *m, uint32_t n, double frac, const double *total,
+                        uint32_t *heavy_ids, uint32_t *n_heavy) {
+    const double thr = frac * (*total);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        if (m[i] > 0.0 && m[i] >= thr) {
+            const uint32_t k = atomicAdd(n_heavy, 1u);
+            if (k < (uint32_t)kMaxHeavy) heavy_ids[k] = i;
+        }
+    }
+}
+
+void launch_find_heavy(const Bodies &b, uint32_t n, double frac, double *scratch_total,
+                       uint32_t *heavy_ids, uint32_t *n_heavy, uint32_t *err, cudaStream_t st) {
+    (void)err;
+    cudaMemsetAsync(n_heavy, 0, sizeof(uint32_t), st);
+    k_total_mass<<<1, 1024, 0, st>>>(b.m, n, scratch_total);
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_heavy<<<blocks, 256, 0, st>>>(b.m, n, frac, scratch_total, heavy_ids, n_heavy);
+}
+
+}  // namespace kd

@@ -1,0 +1,453 @@
+/*
+ * kdoracle.c -- CPU ORACLE for the kD-tree Barnes-Hut step.  TEST INFRASTRUCTURE ONLY.
+ *
+ * This file restates, in plain C, the reference's Rust implementation of the hot path
+ * (MarkCLewis/MultiLanguageKDTree, Parallel/RustVersion/src/array_kd_tree.rs,
+ * quickstat.rs, array_particle.rs and the leaf-7 constants of
+ * Sequential/RustVersion/src/array_kd_tree.rs).  It is the checker that the CUDA library
+ * is compared against: only tests, the smoke check and the CPU-baseline leg of the bench
+ * may load it.  Nothing in the product links or calls it.
+ *
+ * Parity pin: the restatement is validated against the reference's own C port
+ * (Parallel/CVersion/src/kdtree.c), compiled from the reference sources into oracle/_ref
+ * by oracle/build.py, on identical particle arrays (tests/test_oracle.py), and against
+ * the quickstat known answer of quickstat.rs:191-197.
+ *
+ * Arithmetic: every floating-point expression keeps the reference's operation order and is
+ * compiled with -ffp-contract=off, so no multiply-add is fused (Rust never fuses).
+ * The pivot RNG (fastrand in the reference) is a seeded splitmix64 here: pivots only decide
+ * the order of indices inside a node, never which bodies a node holds when keys differ.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_MAX_LEAF 8
+
+/* Particle record: array_particle.rs:3-8 (p[3], v[3], r, m; 64 bytes). */
+typedef struct {
+    double p[3];
+    double v[3];
+    double r;
+    double m;
+} orc_particle;
+
+/* Flat node record, field for field the C port's KDTree (Parallel/CVersion/src/kdtree.h:9-22)
+ * widened to 8 leaf slots so both leaf sizes of the reference (7 and 8) fit. */
+typedef struct {
+    uint64_t num_parts;
+    uint64_t particles[ORC_MAX_LEAF];
+    uint64_t split_dim;
+    double split_val;
+    double m;
+    double cm[3];
+    double size;
+    uint64_t left;
+    uint64_t right;
+} orc_node;
+
+typedef struct {
+    uint64_t s;
+} orc_rng;
+
+static uint64_t rng_next(orc_rng *r) {
+    uint64_t z = (r->s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+/* uniform integer in [lo, hi) -- stands in for fastrand::usize(s..e) */
+static size_t rng_range(orc_rng *r, size_t lo, size_t hi) {
+    return lo + (size_t)(rng_next(r) % (uint64_t)(hi - lo));
+}
+
+/* ---------------------------------------------------------------- node counts */
+
+/* nodes_needed_for_particles, Parallel/RustVersion/src/array_kd_tree.rs:45-53.
+ * 2^ceil(log2(x)) is taken as the smallest power of two >= x, which equals the Rust
+ * f64 expression for every x below 2^52. */
+uint64_t orc_nodes_needed_par(uint64_t n, int leaf) {
+    if (n <= (uint64_t)leaf) return 1;
+    uint64_t min_leaves = n / (uint64_t)(leaf / 2);
+    uint64_t leaves = 1;
+    while (leaves < min_leaves) leaves <<= 1;
+    return 2 * leaves - 1;
+}
+
+/* nodes_needed_for_particles, Sequential/RustVersion/src/array_kd_tree.rs:37-39 */
+uint64_t orc_nodes_needed_seq(uint64_t n, int leaf) {
+    return 2 * (n / (uint64_t)(leaf / 2) + 1);
+}
+
+/* ---------------------------------------------------------------- quickselect */
+
+/* quickstat_index, Parallel/RustVersion/src/quickstat.rs:9-34, with the comparator
+ * `lt(a, b) = keys[a] < keys[b]` (array_kd_tree.rs:561-562 passes p[split_dim]). */
+static void quickstat_keys(uint64_t *idx, size_t len, size_t goal, const double *keys,
+                           size_t stride, orc_rng *rng) {
+    size_t s = 0, e = len;
+    while (s + 1 < e) {
+        size_t pivot = rng_range(rng, s, e);
+        uint64_t t = idx[s]; idx[s] = idx[pivot]; idx[pivot] = t;
+        size_t low = s + 1, high = e - 1;
+        while (low <= high) {
+            if (keys[idx[low] * stride] < keys[idx[s] * stride]) {
+                low += 1;
+            } else {
+                t = idx[low]; idx[low] = idx[high]; idx[high] = t;
+                high -= 1;
+            }
+        }
+        t = idx[s]; idx[s] = idx[high]; idx[high] = t;
+        if (high < goal) s = high + 1;
+        else if (high > goal) e = high;
+        else s = e;
+    }
+}
+
+/* Public form used by the known-answer test: values are a plain array. */
+void orc_quickstat_index(uint64_t *idx, size_t len, size_t goal, const double *vals,
+                         uint64_t seed) {
+    orc_rng rng = {seed};
+    quickstat_keys(idx, len, goal, vals, 1, &rng);
+}
+
+/* ---------------------------------------------------------------- build */
+
+/* Segment scan of array_kd_tree.rs:532-557 (par4) / :86-111 (DFS): mass, unnormalised
+ * then normalised centre of mass, bounding box from +-1e100, split dimension by strict >
+ * from dim 0, size = extent along the split dimension. */
+static void scan_segment(const uint64_t *idx, size_t len, const orc_particle *P,
+                         double *m_out, double cm[3], uint64_t *split_dim, double *size) {
+    double mn[3] = {1e100, 1e100, 1e100};
+    double mx[3] = {-1e100, -1e100, -1e100};
+    double m = 0.0;
+    cm[0] = cm[1] = cm[2] = 0.0;
+    for (size_t i = 0; i < len; ++i) {
+        const orc_particle *q = &P[idx[i]];
+        m += q->m;
+        cm[0] += q->m * q->p[0];
+        cm[1] += q->m * q->p[1];
+        cm[2] += q->m * q->p[2];
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = fmin(mn[d], q->p[d]);
+            mx[d] = fmax(mx[d], q->p[d]);
+        }
+    }
+    cm[0] /= m;
+    cm[1] /= m;
+    cm[2] /= m;
+    uint64_t sd = 0;
+    for (int d = 1; d < 3; ++d)
+        if (mx[d] - mn[d] > mx[sd] - mn[sd]) sd = (uint64_t)d;
+    *m_out = m;
+    *split_dim = sd;
+    *size = mx[sd] - mn[sd];
+}
+
+typedef struct {
+    orc_node *nodes;
+    size_t cap;
+    int leaf;
+    int overflow;
+    orc_rng rng;
+} dfs_state;
+
+static int ensure_cap(dfs_state *st, size_t node) {
+    if (node < st->cap) return 1;
+    st->overflow = 1; /* the reference grows its Vec here (array_kd_tree.rs:75-77) */
+    return 0;
+}
+
+/* build_tree (DFS-packed numbering), Parallel/RustVersion/src/array_kd_tree.rs:63-130 and
+ * Sequential/RustVersion/src/array_kd_tree.rs:49-138.  Returns the last node used. */
+static size_t build_dfs(uint64_t *idx, size_t start, size_t end, const orc_particle *P,
+                        size_t cur, dfs_state *st) {
+    size_t np = end - start;
+    if (np <= (size_t)st->leaf) {
+        if (!ensure_cap(st, cur)) return cur;
+        orc_node *n = &st->nodes[cur];
+        memset(n, 0, sizeof(*n));
+        n->num_parts = np;
+        for (size_t i = 0; i < np; ++i) n->particles[i] = idx[start + i];
+        return cur;
+    }
+    double m, cm[3], size;
+    uint64_t sd;
+    scan_segment(idx + start, np, P, &m, cm, &sd, &size);
+    size_t mid = (start + end) / 2;
+    quickstat_keys(idx + start, np, mid - start, &P[0].p[sd], sizeof(orc_particle) / 8,
+                   &st->rng);
+    double split_val = P[idx[mid]].p[sd];
+    size_t left = build_dfs(idx, start, mid, P, cur + 1, st);
+    size_t right = build_dfs(idx, mid, end, P, left + 1, st);
+    if (!ensure_cap(st, cur)) return right;
+    orc_node *n = &st->nodes[cur];
+    memset(n, 0, sizeof(*n));
+    n->split_dim = sd;
+    n->split_val = split_val;
+    n->m = m;
+    n->cm[0] = cm[0]; n->cm[1] = cm[1]; n->cm[2] = cm[2];
+    n->size = size;
+    n->left = cur + 1;
+    n->right = left + 1;
+    return right;
+}
+
+/* Returns the last node index, or (uint64_t)-1 when `cap` slots were not enough. */
+uint64_t orc_build_tree_dfs(uint64_t *idx, size_t n, const orc_particle *P, orc_node *nodes,
+                            size_t cap, int leaf, uint64_t seed) {
+    dfs_state st = {nodes, cap, leaf, 0, {seed}};
+    size_t last = build_dfs(idx, 0, n, P, 0, &st);
+    return st.overflow ? (uint64_t)-1 : (uint64_t)last;
+}
+
+typedef struct {
+    int leaf;
+    int max_threads;
+    volatile int overflow;
+} par4_cfg;
+
+/* build_tree_par4, Parallel/RustVersion/src/array_kd_tree.rs:515-583.  `nodes`/`cap` is
+ * the slice handed to this subtree; the left subtree gets nodes_needed(len/2) slots and the
+ * right subtree whatever remains (:566-569).  rayon::join becomes an OpenMP task pair while
+ * thread_cnt < the thread count (:571-578). */
+static void build_par4(uint64_t *idx, size_t np, size_t cur, const orc_particle *P,
+                       orc_node *nodes, size_t cap, size_t thread_cnt, par4_cfg *cfg,
+                       uint64_t seed) {
+    if (cap < 1) { cfg->overflow = 1; return; }
+    if (np <= (size_t)cfg->leaf) {
+        orc_node *n = &nodes[0];
+        memset(n, 0, sizeof(*n));
+        n->num_parts = np;
+        for (size_t i = 0; i < np; ++i) n->particles[i] = idx[i];
+        return;
+    }
+    double m, cm[3], size;
+    uint64_t sd;
+    scan_segment(idx, np, P, &m, cm, &sd, &size);
+    size_t mid = np / 2;
+    orc_rng rng = {seed};
+    quickstat_keys(idx, np, mid, &P[0].p[sd], sizeof(orc_particle) / 8, &rng);
+    double split_val = P[idx[mid]].p[sd];
+    size_t num_nodes = (size_t)orc_nodes_needed_par(mid, cfg->leaf);
+    if (1 + num_nodes > cap) { cfg->overflow = 1; return; }
+    uint64_t sl = rng_next(&rng), sr = rng_next(&rng);
+    if ((int)thread_cnt < cfg->max_threads) {
+#pragma omp task shared(cfg)
+        build_par4(idx, mid, cur + 1, P, nodes + 1, num_nodes, thread_cnt * 2, cfg, sl);
+#pragma omp task shared(cfg)
+        build_par4(idx + mid, np - mid, cur + 1 + num_nodes, P, nodes + 1 + num_nodes,
+                   cap - 1 - num_nodes, thread_cnt * 2, cfg, sr);
+#pragma omp taskwait
+    } else {
+        build_par4(idx, mid, cur + 1, P, nodes + 1, num_nodes, thread_cnt * 2, cfg, sl);
+        build_par4(idx + mid, np - mid, cur + 1 + num_nodes, P, nodes + 1 + num_nodes,
+                   cap - 1 - num_nodes, thread_cnt * 2, cfg, sr);
+    }
+    orc_node *n = &nodes[0];
+    memset(n, 0, sizeof(*n));
+    n->split_dim = sd;
+    n->split_val = split_val;
+    n->m = m;
+    n->cm[0] = cm[0]; n->cm[1] = cm[1]; n->cm[2] = cm[2];
+    n->size = size;
+    n->left = cur + 1;
+    n->right = cur + 1 + num_nodes;
+}
+
+static int max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* Returns 0, or -1 when the node slice overflowed (the Rust code would panic). Unused slots
+ * are left as empty leaves, as allocate_node_vec leaves them (array_kd_tree.rs:55-60). */
+int orc_build_tree_par4(uint64_t *idx, size_t n, const orc_particle *P, orc_node *nodes,
+                        size_t cap, int leaf, uint64_t seed) {
+    par4_cfg cfg = {leaf, max_threads(), 0};
+    memset(nodes, 0, cap * sizeof(orc_node));
+#pragma omp parallel
+#pragma omp single
+    build_par4(idx, n, 0, P, nodes, cap, 1, &cfg, seed);
+    return cfg.overflow ? -1 : 0;
+}
+
+/* ---------------------------------------------------------------- walk */
+
+/* calc_pp_accel, array_particle.rs:67-76 */
+static inline void pp_accel(const orc_particle *pi, const orc_particle *pj, double a[3]) {
+    double dx = pi->p[0] - pj->p[0];
+    double dy = pi->p[1] - pj->p[1];
+    double dz = pi->p[2] - pj->p[2];
+    double dp2 = dx * dx + dy * dy + dz * dz;
+    double dist = sqrt(dp2);
+    double magi = -pj->m / (dist * dist * dist);
+    a[0] = magi * dx;
+    a[1] = magi * dy;
+    a[2] = magi * dz;
+}
+
+typedef struct {
+    uint64_t p2p, opened, m2p, visits;
+} orc_counts;
+
+/* accel_recur, Parallel/RustVersion/src/array_kd_tree.rs:585-617: sequential sum inside a
+ * leaf with self-exclusion by index, opening test size^2 < theta^2 |d|^2 (strict), and the
+ * binary-tree sum left + right. */
+static void accel_recur(size_t cur, size_t p, const orc_particle *P, const orc_node *nodes,
+                        double theta2, double out[3], orc_counts *c) {
+    const orc_node *n = &nodes[cur];
+    if (c) c->visits++;
+    if (n->num_parts > 0) {
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (uint64_t i = 0; i < n->num_parts; ++i) {
+            if (n->particles[i] != p) {
+                double pa[3];
+                pp_accel(&P[p], &P[n->particles[i]], pa);
+                acc[0] += pa[0];
+                acc[1] += pa[1];
+                acc[2] += pa[2];
+                if (c) c->p2p++;
+            }
+        }
+        out[0] = acc[0]; out[1] = acc[1]; out[2] = acc[2];
+        return;
+    }
+    double dx = P[p].p[0] - n->cm[0];
+    double dy = P[p].p[1] - n->cm[1];
+    double dz = P[p].p[2] - n->cm[2];
+    double dist_sqr = dx * dx + dy * dy + dz * dz;
+    if (c) c->opened++;
+    if (n->size * n->size < theta2 * dist_sqr) {
+        double dist = sqrt(dist_sqr);
+        double magi = -n->m / (dist_sqr * dist);
+        out[0] = dx * magi; out[1] = dy * magi; out[2] = dz * magi;
+        if (c) c->m2p++;
+    } else {
+        double l[3], r[3];
+        accel_recur(n->left, p, P, nodes, theta2, l, c);
+        accel_recur(n->right, p, P, nodes, theta2, r, c);
+        out[0] = l[0] + r[0]; out[1] = l[1] + r[1]; out[2] = l[2] + r[2];
+    }
+}
+
+/* calc_accel (array_kd_tree.rs:619-621) for every body, parallel over sinks like the
+ * par_iter_mut of :647.  `theta` is THETA (:15); THETA*THETA is formed first (:606). */
+void orc_calc_accel_all(const orc_particle *P, size_t n, const orc_node *nodes, double theta,
+                        double *acc) {
+    double theta2 = theta * theta;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (size_t i = 0; i < n; ++i) accel_recur(0, i, P, nodes, theta2, &acc[3 * i], NULL);
+}
+
+/* Instrumented walk over a list of sinks: interaction counts per the reference's walk. */
+void orc_walk_counts(const orc_particle *P, const orc_node *nodes, double theta,
+                     const uint64_t *sinks, size_t ns, uint64_t out[4]) {
+    double theta2 = theta * theta;
+    orc_counts tot = {0, 0, 0, 0};
+    for (size_t k = 0; k < ns; ++k) {
+        double a[3];
+        accel_recur(0, (size_t)sinks[k], P, nodes, theta2, a, &tot);
+    }
+    out[0] = tot.p2p; out[1] = tot.opened; out[2] = tot.m2p; out[3] = tot.visits;
+}
+
+/* ---------------------------------------------------------------- step loop */
+
+/* simple_sim, Parallel/RustVersion/src/array_kd_tree.rs:623-664 (layout 1 = build_tree_par4)
+ * and Sequential/RustVersion/src/array_kd_tree.rs:178-218 (layout 0 = DFS build_tree):
+ * reset indices, build, accel for every body, then v += dt*a; p += dt*v.
+ * `acc_trace`, when not NULL, receives every step's accelerations (steps*n*3). */
+int orc_simple_sim(orc_particle *P, size_t n, double dt, int64_t steps, int leaf, int layout,
+                   double theta, uint64_t seed, double *acc_trace) {
+    size_t cap = layout == 1 ? (size_t)orc_nodes_needed_par(n, leaf) : 2 * n + 2;
+    orc_node *nodes = (orc_node *)calloc(cap, sizeof(orc_node));
+    uint64_t *idx = (uint64_t *)malloc(n * sizeof(uint64_t));
+    double *acc = (double *)calloc(3 * n, sizeof(double));
+    if (!nodes || !idx || !acc) { free(nodes); free(idx); free(acc); return -2; }
+    int rc = 0;
+    for (int64_t step = 0; step < steps; ++step) {
+        for (size_t i = 0; i < n; ++i) idx[i] = i;
+        uint64_t s = seed + 0x51ED27ULL * (uint64_t)step;
+        if (layout == 1) {
+            if (orc_build_tree_par4(idx, n, P, nodes, cap, leaf, s) != 0) { rc = -1; break; }
+        } else {
+            if (orc_build_tree_dfs(idx, n, P, nodes, cap, leaf, s) == (uint64_t)-1) { rc = -1; break; }
+        }
+        orc_calc_accel_all(P, n, nodes, theta, acc);
+        if (acc_trace) memcpy(acc_trace + (size_t)step * 3 * n, acc, 3 * n * sizeof(double));
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < n; ++i) {
+            orc_particle *b = &P[i];
+            double *a = &acc[3 * i];
+            b->v[0] += dt * a[0];
+            b->v[1] += dt * a[1];
+            b->v[2] += dt * a[2];
+            double dx = dt * b->v[0];
+            double dy = dt * b->v[1];
+            double dz = dt * b->v[2];
+            b->p[0] += dx;
+            b->p[1] += dy;
+            b->p[2] += dz;
+            a[0] = 0.0; a[1] = 0.0; a[2] = 0.0;
+        }
+    }
+    free(nodes); free(idx); free(acc);
+    return rc;
+}
+
+/* ---------------------------------------------------------------- direct sum */
+
+/* FP64 direct sum for a set of sinks: one-sided form of the all-pairs kernel of
+ * Sequential/RustVersion/src/simd_particle.rs:95-103, each pair evaluated like
+ * calc_pp_accel (array_particle.rs:67-76).  Summed in source order. */
+void orc_direct_accel(const orc_particle *P, size_t n, const uint64_t *sinks, size_t ns,
+                      double *acc) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (size_t k = 0; k < ns; ++k) {
+        size_t i = (size_t)sinks[k];
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (size_t j = 0; j < n; ++j) {
+            if (j == i) continue;
+            double pa[3];
+            pp_accel(&P[i], &P[j], pa);
+            a0 += pa[0]; a1 += pa[1]; a2 += pa[2];
+        }
+        acc[3 * k] = a0; acc[3 * k + 1] = a1; acc[3 * k + 2] = a2;
+    }
+}
+
+/* Direct-sum potential energy sum_{i<j} -m_i m_j / r_ij and kinetic energy (small N). */
+void orc_energy(const orc_particle *P, size_t n, double out[2]) {
+    double pe = 0.0, ke = 0.0;
+#pragma omp parallel for reduction(+ : pe, ke) schedule(dynamic, 16)
+    for (size_t i = 0; i < n; ++i) {
+        const orc_particle *a = &P[i];
+        ke += 0.5 * a->m * (a->v[0] * a->v[0] + a->v[1] * a->v[1] + a->v[2] * a->v[2]);
+        for (size_t j = i + 1; j < n; ++j) {
+            double dx = a->p[0] - P[j].p[0], dy = a->p[1] - P[j].p[1], dz = a->p[2] - P[j].p[2];
+            pe -= a->m * P[j].m / sqrt(dx * dx + dy * dy + dz * dz);
+        }
+    }
+    out[0] = ke;
+    out[1] = pe;
+}
+
+int orc_omp_threads(void) { return max_threads(); }
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}

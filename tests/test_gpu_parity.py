@@ -1,0 +1,245 @@
+"""GPU parity: libkdnbody.so (through its C ABI) against the golden fixtures made by the
+reference's own C port and against the oracle.
+
+Bars: node membership, split_dim, split_val and size bit-exact; node mass and centre of
+mass within 1e-12 relative; FP64 accelerations within 1e-12 relative per body (the
+reference's own summation order differs between its Rust and C ports at that level);
+mixed-precision accelerations within 1e-4 relative of an FP64 direct sum."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import check_split_invariant, leaf_map, leaf_sets, rel_err, replay_positions
+
+pytestmark = pytest.mark.gpu
+
+ACC_RTOL = 1e-12
+MIXED_RTOL = 1e-4
+
+
+def gpu_tree(kd, bodies, leaf=7, layout="dfs", theta=0.3, precision="fp64"):
+    s = kd.KDTreeSim(len(bodies), leaf_size=leaf, layout=layout, theta=theta,
+                     precision=precision)
+    s.set_bodies(bodies)
+    last = s.build_tree()
+    return s, s.nodes(), last
+
+
+# ------------------------------------------------------------------ reference test cases
+
+def test_single_node(kd):
+    b = kd.two_bodies()
+    for layout in ("dfs", "par4"):
+        s, nodes, last = gpu_tree(kd, b, leaf=8, layout=layout)
+        assert last == 0
+        assert nodes[0]["num_parts"] == 2
+        assert sorted(nodes[0]["particles"][:2]) == [0, 1]
+        acc = s.calc_accel()
+        # 1/r^2 pull of each body on the other
+        assert np.allclose(acc[0], [1e-20, 0, 0], rtol=1e-15)
+        assert np.allclose(acc[1], [-1.0, 0, 0], rtol=1e-15)
+        s.close()
+
+
+def test_two_leaves(kd):
+    b = kd.circular_orbits(11, seed=3)
+    for layout, leaf in [("dfs", 7), ("par4", 8)]:
+        s, nodes, _ = gpu_tree(kd, b, leaf=leaf, layout=layout)
+        check_split_invariant(nodes, b)
+        assert nodes[0]["num_parts"] == 0
+        assert nodes[1]["num_parts"] + nodes[2]["num_parts"] == 12
+        s.close()
+
+
+# ------------------------------------------------------------------ golden (reference C port)
+
+def test_membership_and_accel_vs_golden_every_step(kd, golden):
+    n = int(golden["n"])
+    s = kd.KDTreeSim(n, leaf_size=7, layout="dfs", theta=0.3)
+    for k, b in enumerate(replay_positions(golden)):
+        s.set_bodies(b)
+        last = s.build_tree()
+        nodes = s.nodes()
+        assert last == int(golden["last_node"][k])
+        assert np.array_equal(leaf_map(nodes, n), golden["leaf_of"][k]), f"step {k}"
+        internal = golden["split_dim"][k] >= 0
+        assert np.array_equal(nodes["split_dim"][internal].astype(np.int64),
+                              golden["split_dim"][k][internal])
+        assert np.array_equal(nodes["split_val"][internal], golden["split_val"][k][internal])
+        assert np.allclose(nodes["m"][internal], golden["m"][k][internal], rtol=1e-12, atol=0)
+        assert np.allclose(nodes["cm"][internal], golden["cm"][k][internal], rtol=1e-12,
+                           atol=1e-15)
+        acc = s.calc_accel()
+        assert rel_err(acc, golden["acc"][k]).max() <= ACC_RTOL, f"step {k}"
+    s.close()
+
+
+def test_simple_sim_vs_golden(kd, golden):
+    b = golden["init"].copy().view(kd.PARTICLE_DTYPE)
+    kd.simple_sim(b, float(golden["dt"]), int(golden["steps"]), leaf_size=7)
+    assert np.abs(b["p"] - golden["final"]["p"]).max() < 1e-13
+    assert np.abs(b["v"] - golden["final"]["v"]).max() < 1e-11
+    assert np.array_equal(b["m"], golden["final"]["m"])
+    assert np.array_equal(b["r"], golden["final"]["r"])
+
+
+# ------------------------------------------------------------------ oracle, larger sizes
+
+@pytest.mark.parametrize("n,leaf,layout,gen", [
+    (5001, 7, "dfs", "circ"), (20_000, 8, "par4", "ring"), (100_000, 7, "dfs", "ring"),
+    (100_000, 8, "par4", "plummer"), (65_537, 7, "par4", "ring"), (1023, 7, "dfs", "plummer"),
+    (1025, 8, "dfs", "ring"), (33_000, 7, "dfs", "plummer"),
+])
+def test_tree_and_accel_vs_oracle(kd, oracle, n, leaf, layout, gen):
+    b = {"circ": lambda: kd.circular_orbits(n - 1, seed=n),
+         "ring": lambda: kd.ring(n, seed=n),
+         "plummer": lambda: kd.plummer(n, seed=n)}[gen]()
+    s, nodes, _ = gpu_tree(kd, b, leaf=leaf, layout=layout)
+    onodes = (oracle.build_tree_dfs(b, leaf=leaf)[0] if layout == "dfs"
+              else oracle.build_tree_par4(b, leaf=leaf))
+    assert len(nodes) == len(onodes)
+    assert leaf_sets(nodes) == leaf_sets(onodes)
+    internal = onodes["num_parts"] == 0
+    for f in ("split_dim", "split_val", "size", "left", "right"):
+        assert np.array_equal(nodes[f][internal], onodes[f][internal]), f
+    assert np.allclose(nodes["m"][internal], onodes["m"][internal], rtol=1e-12, atol=0)
+    assert np.allclose(nodes["cm"][internal], onodes["cm"][internal], rtol=1e-12, atol=1e-14)
+    acc = s.calc_accel()
+    oacc = oracle.calc_accel(b, onodes, 0.3)
+    assert rel_err(acc, oacc).max() <= ACC_RTOL
+    s.close()
+
+
+def test_c2_size_one_million(kd, oracle):
+    """1,000,000-body ring, leaf 7, theta 0.3: membership bit-exact against the oracle and
+    accelerations of 4,096 sampled bodies within 1e-12."""
+    n = 1_000_000
+    b = kd.ring(n, seed=2024)
+    s, nodes, _ = gpu_tree(kd, b, leaf=7, layout="dfs")
+    onodes, _ = oracle.build_tree_dfs(b, leaf=7)
+    assert np.array_equal(leaf_map(nodes, n), leaf_map(onodes, n))
+    internal = onodes["num_parts"] == 0
+    assert np.array_equal(nodes["split_val"][internal], onodes["split_val"][internal])
+    acc = s.calc_accel()
+    oacc = oracle.calc_accel(b, onodes, 0.3)
+    assert rel_err(acc, oacc).max() <= ACC_RTOL
+    s.close()
+
+
+def test_steps_keep_matching_the_oracle(kd, oracle):
+    """Five steps of the step loop on both sides from the same bodies (leaf 8, PAR4)."""
+    n = 30_000
+    b0 = kd.ring(n, seed=77)
+    g = b0.copy()
+    kd.simple_sim(g, 1e-3, 5, leaf_size=8)
+    o = b0.copy()
+    oracle.simple_sim(o, 1e-3, 5, leaf=8, layout="par4")
+    assert np.abs(g["p"] - o["p"]).max() < 1e-13
+    assert np.abs(g["v"] - o["v"]).max() < 1e-11
+
+
+# ------------------------------------------------------------------ edge cases
+
+@pytest.mark.parametrize("n", [1, 2, 6, 7, 8, 9, 15, 16, 17])
+def test_tiny_sizes(kd, oracle, n):
+    b = kd.plummer(max(n, 2), seed=n)[:n].copy()
+    for leaf, layout in [(7, "dfs"), (8, "par4")]:
+        s, nodes, last = gpu_tree(kd, b, leaf=leaf, layout=layout)
+        onodes = (oracle.build_tree_dfs(b, leaf=leaf)[0] if layout == "dfs"
+                  else oracle.build_tree_par4(b, leaf=leaf))
+        assert leaf_sets(nodes) == leaf_sets(onodes)
+        acc = s.calc_accel()
+        oacc = oracle.calc_accel(b, onodes, 0.3)
+        assert np.allclose(acc, oacc, rtol=1e-12, atol=0)
+        s.close()
+
+
+def test_ties_give_a_valid_median_split(kd):
+    """Many equal coordinates (a lattice): the reference's own choice among tied bodies
+    depends on its random pivots, so the check is the split post-condition with ties:
+    left <= split_val <= right, len/2 bodies left, every body exactly once."""
+    g = np.arange(40, dtype=np.float64)
+    x, y, z = np.meshgrid(g, g, g[:10], indexing="ij")
+    n = x.size
+    b = np.zeros(n, dtype=kd.PARTICLE_DTYPE)
+    b["p"] = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    b["m"] = 1.0
+    s, nodes, _ = gpu_tree(kd, b, leaf=7)
+    members = np.concatenate([nd["particles"][: nd["num_parts"]] for nd in nodes
+                              if nd["num_parts"] > 0])
+    assert np.array_equal(np.sort(members), np.arange(n))
+    p = b["p"]
+
+    def collect(i):
+        nd = nodes[i]
+        if nd["num_parts"] > 0:
+            return list(nd["particles"][: nd["num_parts"]])
+        return collect(int(nd["left"])) + collect(int(nd["right"]))
+
+    for i, nd in enumerate(nodes[:200]):
+        if nd["num_parts"] == 0:
+            d, sv = int(nd["split_dim"]), nd["split_val"]
+            L = np.array(collect(int(nd["left"])), dtype=np.int64)
+            R = np.array(collect(int(nd["right"])), dtype=np.int64)
+            assert len(L) == (len(L) + len(R)) // 2
+            assert (p[L, d] <= sv).all() and (p[R, d] >= sv).all()
+    s.close()
+
+
+def test_invalid_bodies_are_rejected(kd):
+    b = kd.ring(1000, seed=1)
+    s = kd.KDTreeSim(1000)
+    bad = b.copy()
+    bad["p"][10, 1] = np.nan
+    with pytest.raises(kd.KDError) as e:
+        s.set_bodies(bad)
+    assert "KD_ENUMERIC" in str(e.value)
+    bad = b.copy()
+    bad["m"][3] = -1.0
+    with pytest.raises(kd.KDError):
+        s.set_bodies(bad)
+    with pytest.raises(kd.KDError):
+        s.set_bodies(b[:999])
+    with pytest.raises(kd.KDError):
+        s.build_tree()  # no valid bodies yet
+    s.set_bodies(b)
+    s.build_tree()
+    s.close()
+
+
+# ------------------------------------------------------------------ mixed precision
+
+def test_mixed_precision_vs_direct_sum(kd, oracle):
+    n = 200_000
+    b = kd.ring(n, seed=31)
+    s = kd.KDTreeSim(n, leaf_size=7, precision="mixed")
+    s.set_bodies(b)
+    s.build_tree()
+    acc = s.calc_accel()
+    rng = np.random.default_rng(4)
+    sinks = rng.choice(np.arange(1, n), 4096, replace=False)
+    ref = oracle.direct_accel(b, sinks)
+    err = rel_err(acc[sinks], ref)
+    assert err.max() <= MIXED_RTOL, err.max()
+    s.set_precision("fp64")
+    acc64 = s.calc_accel()
+    assert rel_err(acc[sinks], acc64[sinks]).max() <= MIXED_RTOL
+    s.close()
+
+
+def test_mixed_precision_plummer(kd, oracle):
+    """Equal-mass sphere (no heavy body): the FP32 terms carry everything.  Compared with
+    the FP64 tree walk, so the check isolates the precision error from the theta error."""
+    n = 100_000
+    b = kd.plummer(n, seed=41)
+    s = kd.KDTreeSim(n, leaf_size=7, precision="mixed", theta=0.5)
+    s.set_bodies(b)
+    s.build_tree()
+    acc = s.calc_accel()
+    s.set_precision("fp64")
+    acc64 = s.calc_accel()
+    err = rel_err(acc, acc64)
+    assert np.sqrt(np.mean(err ** 2)) <= 1e-5
+    assert err.max() <= 1e-3
+    s.close()
