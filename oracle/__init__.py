@@ -56,6 +56,7 @@ class Oracle:
             "orc_build_tree_par4": (C.c_int, [_vp, C.c_size_t, _vp, _vp, C.c_size_t, C.c_int,
                                               C.c_uint64]),
             "orc_calc_accel_all": (None, [_vp, C.c_size_t, _vp, C.c_double, _vp]),
+            "orc_calc_accel_abs": (None, [_vp, C.c_size_t, _vp, C.c_double, _vp, _vp]),
             "orc_walk_counts": (None, [_vp, _vp, C.c_double, _vp, C.c_size_t, _vp]),
             "orc_simple_sim": (C.c_int, [_vp, C.c_size_t, C.c_double, C.c_int64, C.c_int, C.c_int,
                                          C.c_double, C.c_uint64, _vp]),
@@ -122,6 +123,15 @@ class Oracle:
         acc = np.zeros((len(b), 3))
         self.lib.orc_calc_accel_all(_p(b), len(b), _p(nodes), theta, _p(acc))
         return acc
+
+    def calc_accel_abs(self, bodies, nodes, theta: float = 0.3):
+        """(acc, sum over terms of |term|) per body."""
+        b = self._bodies(bodies)
+        nodes = np.ascontiguousarray(nodes, dtype=NODE)
+        acc = np.zeros((len(b), 3))
+        ab = np.zeros(len(b))
+        self.lib.orc_calc_accel_abs(_p(b), len(b), _p(nodes), theta, _p(acc), _p(ab))
+        return acc, ab
 
     def walk_counts(self, bodies, nodes, sinks, theta: float = 0.3) -> dict:
         b = self._bodies(bodies)

@@ -304,7 +304,7 @@ typedef struct {
  * leaf with self-exclusion by index, opening test size^2 < theta^2 |d|^2 (strict), and the
  * binary-tree sum left + right. */
 static void accel_recur(size_t cur, size_t p, const orc_particle *P, const orc_node *nodes,
-                        double theta2, double out[3], orc_counts *c) {
+                        double theta2, double out[3], orc_counts *c, double *absum) {
     const orc_node *n = &nodes[cur];
     if (c) c->visits++;
     if (n->num_parts > 0) {
@@ -313,6 +313,7 @@ static void accel_recur(size_t cur, size_t p, const orc_particle *P, const orc_n
             if (n->particles[i] != p) {
                 double pa[3];
                 pp_accel(&P[p], &P[n->particles[i]], pa);
+                if (absum) *absum += sqrt(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]);
                 acc[0] += pa[0];
                 acc[1] += pa[1];
                 acc[2] += pa[2];
@@ -331,11 +332,12 @@ static void accel_recur(size_t cur, size_t p, const orc_particle *P, const orc_n
         double dist = sqrt(dist_sqr);
         double magi = -n->m / (dist_sqr * dist);
         out[0] = dx * magi; out[1] = dy * magi; out[2] = dz * magi;
+        if (absum) *absum += sqrt(out[0] * out[0] + out[1] * out[1] + out[2] * out[2]);
         if (c) c->m2p++;
     } else {
         double l[3], r[3];
-        accel_recur(n->left, p, P, nodes, theta2, l, c);
-        accel_recur(n->right, p, P, nodes, theta2, r, c);
+        accel_recur(n->left, p, P, nodes, theta2, l, c, absum);
+        accel_recur(n->right, p, P, nodes, theta2, r, c, absum);
         out[0] = l[0] + r[0]; out[1] = l[1] + r[1]; out[2] = l[2] + r[2];
     }
 }
@@ -346,7 +348,19 @@ void orc_calc_accel_all(const orc_particle *P, size_t n, const orc_node *nodes, 
                         double *acc) {
     double theta2 = theta * theta;
 #pragma omp parallel for schedule(dynamic, 256)
-    for (size_t i = 0; i < n; ++i) accel_recur(0, i, P, nodes, theta2, &acc[3 * i], NULL);
+    for (size_t i = 0; i < n; ++i) accel_recur(0, i, P, nodes, theta2, &acc[3 * i], NULL, NULL);
+}
+
+/* Same walk, also returning per body the sum of the magnitudes of its interaction terms:
+ * the scale that bounds the rounding error of any summation order of those terms. */
+void orc_calc_accel_abs(const orc_particle *P, size_t n, const orc_node *nodes, double theta,
+                        double *acc, double *absum) {
+    double theta2 = theta * theta;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (size_t i = 0; i < n; ++i) {
+        absum[i] = 0.0;
+        accel_recur(0, i, P, nodes, theta2, &acc[3 * i], NULL, &absum[i]);
+    }
 }
 
 /* Instrumented walk over a list of sinks: interaction counts per the reference's walk. */
@@ -356,7 +370,7 @@ void orc_walk_counts(const orc_particle *P, const orc_node *nodes, double theta,
     orc_counts tot = {0, 0, 0, 0};
     for (size_t k = 0; k < ns; ++k) {
         double a[3];
-        accel_recur(0, (size_t)sinks[k], P, nodes, theta2, a, &tot);
+        accel_recur(0, (size_t)sinks[k], P, nodes, theta2, a, &tot, NULL);
     }
     out[0] = tot.p2p; out[1] = tot.opened; out[2] = tot.m2p; out[3] = tot.visits;
 }

@@ -95,6 +95,22 @@ def rel_err(a, b):
     return num / np.where(den > 0, den, 1.0)
 
 
+def assert_accel_close(acc, ref, absum, rtol=1e-12, kappa=100.0):
+    """FP64 acceleration parity.  Different summation orders of the same terms differ by
+    rounding proportional to the sum of the terms' magnitudes (absum), so:
+    |da| <= rtol * |a| for every body whose sum is well conditioned (absum <= kappa |a|), and
+    |da| <= rtol * absum for every body (e.g. a central mass whose pulls nearly cancel)."""
+    d = np.linalg.norm(acc - ref, axis=-1)
+    a = np.linalg.norm(ref, axis=-1)
+    well = absum <= kappa * a
+    assert well.mean() > 0.5, "too few well-conditioned bodies for a relative check"
+    rel = d[well] / a[well]
+    assert rel.max() <= rtol, f"max relative error {rel.max():.3e} > {rtol}"
+    scaled = d / np.where(absum > 0, absum, 1.0)
+    assert scaled.max() <= rtol, f"max error / sum|terms| {scaled.max():.3e} > {rtol}"
+    return rel.max(), scaled.max()
+
+
 def check_split_invariant(nodes, bodies, root=0):
     """The reference's recur_test_tree_struct (array_kd_tree.rs:834-877), on all three
     dimensions: every body under the left child is < split_val, every body under the right

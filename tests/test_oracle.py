@@ -6,7 +6,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import check_split_invariant, leaf_map, leaf_sets, rel_err, replay_positions
+from conftest import (assert_accel_close, check_split_invariant, leaf_map, leaf_sets, rel_err,
+                      replay_positions)
 from multilanguagekdtree_gb300.array_particle import circular_orbits, plummer, ring, two_bodies
 
 
@@ -106,9 +107,9 @@ def test_oracle_matches_reference_c(oracle, refc, case):
     assert np.array_equal(nodes["size"][internal], ref_nodes["size"][internal])
     assert np.allclose(nodes["m"][internal], ref_nodes["m"][internal], rtol=1e-13, atol=0)
     assert np.allclose(nodes["cm"][internal], ref_nodes["cm"][internal], rtol=1e-13, atol=1e-15)
-    acc = oracle.calc_accel(b, nodes, 0.3)
+    acc, absum = oracle.calc_accel_abs(b, nodes, 0.3)
     acc_ref = refc.calc_accel(b, ref_nodes)
-    assert rel_err(acc, acc_ref).max() <= 1e-12
+    assert_accel_close(acc, acc_ref, absum, 1e-12)
 
 
 def test_oracle_vs_golden_every_step(oracle, golden):
@@ -122,8 +123,8 @@ def test_oracle_vs_golden_every_step(oracle, golden):
                               golden["split_dim"][k][internal])
         assert np.array_equal(nodes["split_val"][internal], golden["split_val"][k][internal])
         assert np.allclose(nodes["m"][internal], golden["m"][k][internal], rtol=1e-13, atol=0)
-        acc = oracle.calc_accel(b, nodes, 0.3)
-        assert rel_err(acc, golden["acc"][k]).max() <= 1e-12
+        acc, absum = oracle.calc_accel_abs(b, nodes, 0.3)
+        assert_accel_close(acc, golden["acc"][k], absum, 1e-12)
 
 
 def test_oracle_simple_sim_vs_golden(oracle, golden):
