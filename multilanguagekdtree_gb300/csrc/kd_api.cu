@@ -277,8 +277,10 @@ int setup(kd_ctx *c) {
         KD_CHECK(c, c->alloc(&c->scr.ckey[k], n));
         KD_CHECK(c, c->alloc(&c->scr.cpos[k], n));
     }
-    KD_CHECK(c, c->alloc(&c->scr.bmin, 3 * maxG));
-    KD_CHECK(c, c->alloc(&c->scr.bmax, 3 * maxG));
+    for (int k = 0; k < 2; ++k) {
+        KD_CHECK(c, c->alloc(&c->scr.bmin[k], 3 * maxG));
+        KD_CHECK(c, c->alloc(&c->scr.bmax[k], 3 * maxG));
+    }
     KD_CHECK(c, c->alloc(&c->scr.sel, maxG));
     KD_CHECK(c, c->alloc(&c->scr.hist, (size_t)kHistBins * maxGmulti));
     KD_CHECK(c, c->alloc(&c->scr.cand_cnt, maxG));
@@ -329,12 +331,13 @@ int check_device(kd_ctx *c) {
     return KD_OK;
 }
 
-// Build: multi-block levels, then the shared-memory subtree finish.  Leaves the bodies in
-// tree order in tpos/tid.
-void enqueue_build(kd_ctx *c) {
+// Build: multi-block levels, then the shared-memory subtree finish, which also produces the
+// moments and walk records below the local roots; then the nodes above them.  Leaves the
+// bodies in tree order in tpos/tid (and thi/tlo when mixed records are wanted).
+void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     Plan &p = c->plan;
     launch_init_work(c->bodies, c->work, (uint32_t)c->n, c->st);
-    c->launches += 2;  // init + local finish
+    c->launches += 3;  // init + local finish + upward pass
     int cur = 0;
     for (size_t l = 0; l < p.glevels.size(); ++l) {
         LevelArgs lv;
@@ -342,22 +345,27 @@ void enqueue_build(kd_ctx *c) {
         lv.G = (uint32_t)p.glevels[l].size();
         lv.tiles = (p.gmax[l] + kTile - 1) / kTile;
         lv.multi = p.gmax[l] > kMultiMin;
-        c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, c->st);
+        const uint32_t G_next = l + 1 < p.glevels.size() ? (uint32_t)p.glevels[l + 1].size() : 0u;
+        c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, (int)l, G_next,
+                                    c->st);
         cur ^= 1;
     }
-    launch_local(c->topo, c->d_local_roots, (uint32_t)p.local_roots.size(), c->nout, c->work,
-                 cur, c->bodies.m, c->tpos, c->tid, c->st);
+    LocalOut o;
+    o.mass = c->bodies.m;
+    o.tpos = c->tpos;
+    o.tid = c->tid;
+    o.thi = c->thi;
+    o.tlo = c->tlo;
+    o.mo = c->mom;
+    o.mof = c->momf;
+    o.recd = want_d ? c->recd : nullptr;
+    o.recf = want_f ? c->recf : nullptr;
+    o.heavy = c->d_heavy;
+    o.n_heavy = c->n_heavy;
+    const uint32_t nr = (uint32_t)p.local_roots.size();
+    launch_local(c->topo, c->d_local_roots, nr, c->nout, c->work, cur, o, c->dev_err, c->st);
+    launch_moments_top(c->topo, c->d_local_roots, nr, c->nout, o, c->st);
     c->final_buf = cur;
-}
-
-void enqueue_moments(kd_ctx *c, bool fp64, bool mixed) {
-    c->launches += (fp64 ? 1 : 0) + (mixed ? 2 : 0);
-    if (fp64) launch_moments_fp64(c->topo, c->nout, c->tpos, c->mom, c->recd, c->st);
-    if (mixed) {
-        launch_split_mixed(c->tpos, c->tid, c->d_heavy, c->n_heavy, (uint32_t)c->n, c->thi,
-                           c->tlo, c->st);
-        launch_moments_mixed(c->topo, c->nout, c->tpos, c->thi, c->momf, c->recf, c->st);
-    }
 }
 
 void enqueue_walk(kd_ctx *c) {
@@ -539,9 +547,8 @@ int kd_build_tree(kd_ctx *c, size_t *last_node) {
     if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
     KD_CHECK(c, cudaSetDevice(c->prm.device));
     KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
-    enqueue_build(c);
+    enqueue_build(c, true, true);
     KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
-    enqueue_moments(c, true, c->prm.precision == KD_PREC_MIXED);
     KD_CHECK(c, cudaEventRecord(c->ev[2], c->st));
     KD_CHECK(c, cudaGetLastError());
     int rc = check_device(c);
@@ -552,7 +559,7 @@ int kd_build_tree(kd_ctx *c, size_t *last_node) {
     c->stats.total_ms = elapsed(c->ev[0], c->ev[2]);
     c->has_tree = true;
     c->tree_fp64 = true;
-    c->tree_mixed = c->prm.precision == KD_PREC_MIXED;
+    c->tree_mixed = true;
     if (last_node)
         *last_node = c->prm.layout == KD_LAYOUT_PAR4 ? (size_t)c->plan.par4_last
                                                      : (size_t)c->plan.n_nodes - 1;
@@ -614,11 +621,6 @@ int kd_calc_accel(kd_ctx *c, double *acc) {
     if (!acc) return c->fail(KD_EINVAL, "acc is NULL");
     if (!c->has_tree) return c->fail(KD_ESTATE, "no tree built");
     KD_CHECK(c, cudaSetDevice(c->prm.device));
-    const bool mixed = c->prm.precision == KD_PREC_MIXED;
-    if (mixed && !c->tree_mixed) {
-        enqueue_moments(c, false, true);
-        c->tree_mixed = true;
-    }
     int rc = reset_counts(c);
     if (rc) return rc;
     KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
@@ -655,9 +657,8 @@ int kd_simple_sim(kd_ctx *c, double dt, int64_t steps) {
     for (int64_t s = 0; s < steps; ++s) {
         cudaEvent_t *e = c->timing ? &c->tev[5 * (size_t)s] : nullptr;
         if (e) KD_CHECK(c, cudaEventRecord(e[0], c->st));
-        enqueue_build(c);
+        enqueue_build(c, !mixed, mixed);
         if (e) KD_CHECK(c, cudaEventRecord(e[1], c->st));
-        enqueue_moments(c, !mixed, mixed);
         if (e) KD_CHECK(c, cudaEventRecord(e[2], c->st));
         enqueue_walk(c);
         if (e) KD_CHECK(c, cudaEventRecord(e[3], c->st));

@@ -25,11 +25,29 @@ namespace kd {
 static constexpr uint32_t kFull = 0xffffffffu;
 
 // Order-preserving map double -> uint64 (no NaN reaches the build).  -0.0 and +0.0 compare
-// equal under the reference's `<`, so both get the key of +0.0.
+// equal under the reference's `<`, so both get the key of +0.0.  Integer operations only:
+// on this GPU every FP64 instruction, compares and min/max included, runs on the narrow
+// FP64 pipe, so the build orders, bounds and bins bodies through these keys.
 __device__ __forceinline__ unsigned long long ord_key(double v) {
     unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    if (v == 0.0) b = 0ull;
+    if ((b << 1) == 0ull) b = 0ull;
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// Monotone (non-decreasing) double -> float by truncating the mantissa, flushing magnitudes
+// below the float range to zero and saturating above it; integer operations only.
+__device__ __forceinline__ float trunc_float(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const uint32_t sign = (uint32_t)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7ff) - 1023 + 127;
+    uint32_t fb;
+    if (e >= 255)
+        fb = 0x7f800000u;
+    else if (e <= 0)
+        fb = 0u;
+    else
+        fb = ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu);
+    return __uint_as_float(fb | sign);
 }
 __device__ __forceinline__ double ord_val(unsigned long long k) {
     unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
@@ -155,19 +173,20 @@ __global__ __launch_bounds__(kTileThreads) void k_bbox(Topology t, LevelArgs lv,
                                                        unsigned long long *bmax) {
     TileRef r;
     if (!tile_of(t, lv, r)) return;
-    double mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
     for (uint32_t k = r.lo + threadIdx.x; k < r.hi; k += blockDim.x) {
-        double v0 = wx[r.start + k], v1 = wy[r.start + k], v2 = wz[r.start + k];
-        mn[0] = fmin(mn[0], v0); mx[0] = fmax(mx[0], v0);
-        mn[1] = fmin(mn[1], v1); mx[1] = fmax(mx[1], v1);
-        mn[2] = fmin(mn[2], v2); mx[2] = fmax(mx[2], v2);
+        const unsigned long long k0 = ord_key(wx[r.start + k]), k1 = ord_key(wy[r.start + k]),
+                                 k2 = ord_key(wz[r.start + k]);
+        mn[0] = min(mn[0], k0); mx[0] = max(mx[0], k0);
+        mn[1] = min(mn[1], k1); mx[1] = max(mx[1], k1);
+        mn[2] = min(mn[2], k2); mx[2] = max(mx[2], k2);
     }
-    __shared__ double red[kTileThreads / 32][6];
+    __shared__ unsigned long long red[kTileThreads / 32][6];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        mn[d] = warp_fmin(mn[d]);
-        mx[d] = warp_fmax(mx[d]);
+        mn[d] = warp_min(mn[d]);
+        mx[d] = warp_max(mx[d]);
     }
     if (lane == 0) {
         for (int d = 0; d < 3; ++d) { red[warp][d] = mn[d]; red[warp][3 + d] = mx[d]; }
@@ -175,17 +194,27 @@ __global__ __launch_bounds__(kTileThreads) void k_bbox(Topology t, LevelArgs lv,
     __syncthreads();
     if (threadIdx.x < 3) {
         int d = threadIdx.x;
-        double a = INFINITY, b = -INFINITY;
+        unsigned long long a = ~0ull, b = 0ull;
         for (int w = 0; w < kTileThreads / 32; ++w) {
-            a = fmin(a, red[w][d]);
-            b = fmax(b, red[w][3 + d]);
+            a = min(a, red[w][d]);
+            b = max(b, red[w][3 + d]);
         }
-        atomicMin(&bmin[r.seg * 3 + d], ord_key(a));
-        atomicMax(&bmax[r.seg * 3 + d], ord_key(b));
+        atomicMin(&bmin[r.seg * 3 + d], a);
+        atomicMax(&bmax[r.seg * 3 + d], b);
     }
 }
 
-// Split dimension, size and the first radix window of every segment.
+// First-pass bin of a coordinate: linear in [lo, hi] along the split dimension.  The
+// truncating conversion, the float difference to lo, the product by a positive scale and the
+// truncation to an integer are each monotone in v, so bin(v1) < bin(v2) implies v1 < v2:
+// the bins order the bodies consistently with (coordinate, id), and equal coordinates share
+// a bin.
+__device__ __forceinline__ uint32_t lin_bin(double v, float lo, float scale) {
+    const float f = (trunc_float(v) - lo) * scale;
+    return f >= (float)(kHistBins - 1) ? (uint32_t)(kHistBins - 1) : (uint32_t)f;
+}
+
+// Split dimension, size and the first-pass binning of every segment.
 __global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin,
                         const unsigned long long *bmax, SegSel *sel, NodeOut no) {
     uint32_t seg = blockIdx.x * blockDim.x + threadIdx.x;
@@ -202,11 +231,12 @@ __global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin
     choose_split(mn, mx, sd, size);
     no.split_dim[id] = (uint8_t)sd;
     no.size[id] = size;
-    unsigned long long kmin = bmin[seg * 3 + sd], kmax = bmax[seg * 3 + sd];
-    int b = 64 - __clzll((long long)(kmin ^ kmax));
     SegSel s;
     s.sd = sd;
-    s.shift = b > kHistBits ? (uint32_t)(b - kHistBits) : 0u;
+    s.lo = trunc_float(mn[sd]);
+    const float range = trunc_float(mx[sd]) - s.lo;
+    const float scale = (float)kHistBins / range;
+    s.scale = (range > 0.0f && isfinite(scale)) ? scale : 0.0f;
     s.digit = 0;
     s.c = cnt;
     s.r = cnt / 2;
@@ -217,8 +247,7 @@ __global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin
     sel[seg] = s;
 }
 
-// First radix pass over big segments: histogram of the 12 bits just below the common
-// prefix of the segment's keys.
+// First pass over big segments: histogram of linear bins of the split coordinate.
 __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
                                                        const double *wx, const double *wy,
                                                        const double *wz, const SegSel *sel,
@@ -231,8 +260,7 @@ __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
     const SegSel s = sel[r.seg];
     const double *w = pick(wx, wy, wz, s.sd) + r.start;
     for (uint32_t k = r.lo + threadIdx.x; k < r.hi; k += blockDim.x) {
-        uint32_t dig = (uint32_t)(ord_key(w[k]) >> s.shift) & (kHistBins - 1);
-        atomicAdd(&h[dig], 1u);
+        atomicAdd(&h[lin_bin(w[k], s.lo, s.scale)], 1u);
     }
     __syncthreads();
     uint32_t *gh = hist + (size_t)r.seg * kHistBins;
@@ -313,8 +341,9 @@ __global__ __launch_bounds__(kTileThreads) void k_collect(Topology t, LevelArgs 
     for (uint32_t base = r.lo; base < r.hi; base += blockDim.x) {
         uint32_t k = base + threadIdx.x;
         bool in = k < r.hi;
-        unsigned long long key = in ? ord_key(w[k]) : 0ull;
-        bool hit = in && (((uint32_t)(key >> s.shift) & (kHistBins - 1)) == s.digit);
+        const double v = in ? w[k] : 0.0;
+        const unsigned long long key = ord_key(v);
+        bool hit = in && lin_bin(v, s.lo, s.scale) == s.digit;
         uint32_t m = __ballot_sync(kFull, hit);
         if (m) {
             uint32_t leader = __ffs(m) - 1, slot = 0;
@@ -374,10 +403,13 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
             if (r >= c) r = c - 1;
             break;
         }
+        // the first pass over a whole segment uses the linear bins of its bounding box;
+        // later passes use the key bits below the candidates' common prefix (then the id)
+        const bool lin = src < 0 && iter == 0 && st.scale > 0.0f;
         // key and id range of the candidates
         unsigned long long kmn = ~0ull, kmx = 0ull;
         uint32_t imn = kFull, imx = 0u;
-        for (uint32_t j = threadIdx.x; j < c; j += blockDim.x) {
+        for (uint32_t j = threadIdx.x; j < (lin ? 0u : c); j += blockDim.x) {
             unsigned long long key;
             uint32_t pos;
             get(j, key, pos);
@@ -402,7 +434,8 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
         const bool bykey = kmn != kmx;
         int bits = bykey ? 64 - __clzll((long long)(kmn ^ kmx)) : 32 - __clz((int)(imn ^ imx));
         const uint32_t shift = bits > kHistBits ? (uint32_t)(bits - kHistBits) : 0u;
-        auto digit = [&](unsigned long long key, uint32_t id) -> uint32_t {
+        auto digit = [&](unsigned long long key, uint32_t id, uint32_t pos) -> uint32_t {
+            if (lin) return lin_bin(w[pos], st.lo, st.scale);
             return bykey ? ((uint32_t)(key >> shift) & (kHistBins - 1))
                          : ((id >> shift) & (kHistBins - 1));
         };
@@ -410,7 +443,7 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
             unsigned long long key;
             uint32_t pos;
             get(j, key, pos);
-            atomicAdd(&h[digit(key, ids[pos])], 1u);
+            atomicAdd(&h[digit(key, ids[pos], pos)], 1u);
         }
         __syncthreads();
         find_bin(h, r, out3);
@@ -422,7 +455,7 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
             unsigned long long key = 0;
             uint32_t pos = 0;
             if (in) get(j, key, pos);
-            bool hit = in && digit(key, ids[pos]) == dig;
+            bool hit = in && digit(key, ids[pos], pos) == dig;
             uint32_t m = __ballot_sync(kFull, hit);
             if (m) {
                 uint32_t leader = __ffs(m) - 1, slot = 0;
@@ -534,13 +567,18 @@ __global__ __launch_bounds__(256) void k_tile_scan(Topology t, LevelArgs lv,
     if (threadIdx.x == 0 && carry != cnt / 2) atomicOr(err, kErrSelect);
 }
 
-// Stable partition: bodies keep their relative order inside each child.
+// Stable partition: bodies keep their relative order inside each child.  With `nbmin`
+// set, the bounding boxes of the two children (segments 2*seg and 2*seg+1 of the next
+// level) are reduced on the way.
 __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
     Topology t, LevelArgs lv, const double *sx, const double *sy, const double *sz,
     const uint32_t *sid, double *dx, double *dy, double *dz, uint32_t *did, const SegSel *sel,
-    const uint32_t *tile_off) {
+    const uint32_t *tile_off, unsigned long long *nbmin, unsigned long long *nbmax) {
     TileRef r;
     if (!tile_of(t, lv, r)) return;
+    // [child][dim] running bounds of this thread, as ordered keys
+    unsigned long long cmn[2][3] = {{~0ull, ~0ull, ~0ull}, {~0ull, ~0ull, ~0ull}};
+    unsigned long long cmx[2][3] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
     const SegSel s = sel[r.seg];
     const uint32_t mid = r.cnt / 2;
     const uint32_t lbase = tile_off[(size_t)r.seg * lv.tiles + r.tile];
@@ -560,8 +598,9 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
             vz = sz[r.start + k];
             id = sid[r.start + k];
         }
-        double key = s.sd == 0 ? vx : (s.sd == 1 ? vy : vz);
-        bool isL = in && goes_left(ord_key(key), id, s.kmed, s.idmed);
+        const unsigned long long kx = ord_key(vx), ky = ord_key(vy), kz = ord_key(vz);
+        const unsigned long long key = s.sd == 0 ? kx : (s.sd == 1 ? ky : kz);
+        bool isL = in && goes_left(key, id, s.kmed, s.idmed);
         bool isR = in && !isL;
         uint32_t bl = __ballot_sync(kFull, isL), br = __ballot_sync(kFull, isR);
         if (lane == 0) { wl[warp] = __popc(bl); wr[warp] = __popc(br); }
@@ -581,21 +620,73 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
             dz[dst] = vz;
             did[dst] = id;
         }
+        if (nbmin && in) {
+            if (isL) {
+                cmn[0][0] = min(cmn[0][0], kx); cmx[0][0] = max(cmx[0][0], kx);
+                cmn[0][1] = min(cmn[0][1], ky); cmx[0][1] = max(cmx[0][1], ky);
+                cmn[0][2] = min(cmn[0][2], kz); cmx[0][2] = max(cmx[0][2], kz);
+            } else {
+                cmn[1][0] = min(cmn[1][0], kx); cmx[1][0] = max(cmx[1][0], kx);
+                cmn[1][1] = min(cmn[1][1], ky); cmx[1][1] = max(cmx[1][1], ky);
+                cmn[1][2] = min(cmn[1][2], kz); cmx[1][2] = max(cmx[1][2], kz);
+            }
+        }
         runL += totL;
         runR += totR;
         __syncthreads();
     }
+    if (nbmin) {
+        __shared__ unsigned long long red[kTileThreads / 32][12];
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                cmn[c][d] = warp_min(cmn[c][d]);
+                cmx[c][d] = warp_max(cmx[c][d]);
+            }
+        if (lane == 0) {
+            for (int c = 0; c < 2; ++c)
+                for (int d = 0; d < 3; ++d) {
+                    red[warp][6 * c + d] = cmn[c][d];
+                    red[warp][6 * c + 3 + d] = cmx[c][d];
+                }
+        }
+        __syncthreads();
+        if (threadIdx.x < 12) {
+            const int c = threadIdx.x / 6, q = threadIdx.x % 6, d = q % 3;
+            const bool is_max = q >= 3;
+            unsigned long long v = is_max ? 0ull : ~0ull;
+            for (int wq = 0; wq < kTileThreads / 32; ++wq)
+                v = is_max ? max(v, red[wq][threadIdx.x]) : min(v, red[wq][threadIdx.x]);
+            const size_t child = 2 * (size_t)r.seg + c;
+            if (is_max)
+                atomicMax(&nbmax[child * 3 + d], v);
+            else
+                atomicMin(&nbmin[child * 3 + d], v);
+        }
+    }
 }
 
 int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
-                 Scratch &s, cudaStream_t st) {
+                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st) {
     const int nxt = cur ^ 1;
     const uint32_t G = lv.G;
     const uint32_t grid = G * lv.tiles;
-    cudaMemsetAsync(s.bmin, 0xff, sizeof(unsigned long long) * 3 * G, st);
-    cudaMemsetAsync(s.bmax, 0x00, sizeof(unsigned long long) * 3 * G, st);
-    k_bbox<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], s.bmin, s.bmax);
-    k_split<<<(G + 127) / 128, 128, 0, st>>>(t, lv, s.bmin, s.bmax, s.sel, no);
+    unsigned long long *bmin = s.bmin[lvl & 1], *bmax = s.bmax[lvl & 1];
+    unsigned long long *nbmin = G_next ? s.bmin[(lvl + 1) & 1] : nullptr;
+    unsigned long long *nbmax = G_next ? s.bmax[(lvl + 1) & 1] : nullptr;
+    int launched = 5;
+    if (lvl == 0) {
+        cudaMemsetAsync(bmin, 0xff, sizeof(unsigned long long) * 3 * G, st);
+        cudaMemsetAsync(bmax, 0x00, sizeof(unsigned long long) * 3 * G, st);
+        k_bbox<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], bmin, bmax);
+        ++launched;
+    }
+    if (G_next) {
+        cudaMemsetAsync(nbmin, 0xff, sizeof(unsigned long long) * 3 * G_next, st);
+        cudaMemsetAsync(nbmax, 0x00, sizeof(unsigned long long) * 3 * G_next, st);
+    }
+    k_split<<<(G + 127) / 128, 128, 0, st>>>(t, lv, bmin, bmax, s.sel, no);
     if (lv.multi) {
         cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * kHistBins * (size_t)G, st);
         cudaMemsetAsync(s.cand_cnt, 0, sizeof(uint32_t) * G, st);
@@ -604,6 +695,7 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
         k_find<<<G, kTileThreads, 0, st>>>(s.hist, s.sel);
         k_collect<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], s.sel,
                                                  s.cand_cnt, s.ckey[0], s.cpos[0]);
+        launched += 3;
     }
     k_select<<<G, kSelThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur], s.sel,
                                         s, no);
@@ -612,130 +704,311 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
     k_tile_scan<<<G, 256, 0, st>>>(t, lv, s.tile_cnt, s.tile_off, s.err);
     k_part_scatter<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur],
                                                   w.id[cur], w.x[nxt], w.y[nxt], w.z[nxt],
-                                                  w.id[nxt], s.sel, s.tile_off);
-    return lv.multi ? 9 : 6;
+                                                  w.id[nxt], s.sel, s.tile_off, nbmin, nbmax);
+    return launched;
 }
 
 // ------------------------------------------------------------------ local subtree finish
+//
+// One thread block owns a segment of at most kLocalMax bodies and builds its whole subtree
+// in shared memory.  Per level, every internal sub-segment is handled by one warp, with no
+// block barrier inside the level:
+//   1. bounding box -> split_dim, size (choose_split);
+//   2. exact rank-len/2 select on (key, body id): 8-bit radix passes over a warp-private
+//      histogram, narrowing the candidate set until at most 32 remain, then a 32-lane
+//      rank by comparison;
+//   3. stable partition of the sub-segment's index list around the median.
+// A block barrier separates levels (the next level's sub-segment table).
+
+constexpr int kLocalWarps = kLocalThreads / 32;
+constexpr int kLocalLevels = 16;
 
 struct LocalSmem {
-    double x[kLocalMax], y[kLocalMax], z[kLocalMax];
-    unsigned long long key[2 * kLocalMax];
-    unsigned long long val[2 * kLocalMax];
+    double x[kLocalMax], y[kLocalMax], z[kLocalMax], m[kLocalMax];
     uint32_t id[kLocalMax];
-    uint32_t tab_st[2][kLocalMax / 2], tab_cn[2][kLocalMax / 2], tab_id[2][kLocalMax / 2];
-    uint16_t perm[kLocalMax];
-    uint8_t sd[kLocalMax / 2];
-    uint32_t G[2], qmax[2];
-    uint32_t wcnt[kLocalThreads / 32];
+    uint32_t hist[kLocalWarps][256];
+    unsigned long long ckey[kLocalWarps][32];
+    uint32_t cid[kLocalWarps][32];
+    // internal sub-segments of every level, appended level after level
+    uint32_t tab_id[kLocalMax];
+    uint16_t tab_st[kLocalMax], tab_cn[kLocalMax];
+    uint16_t perm[kLocalMax], perm2[kLocalMax];
+    uint16_t clid[kLocalWarps][32];
+    uint32_t lvl_off[kLocalLevels + 1];
+    uint32_t nlvl;
+    uint32_t wcnt[kLocalWarps];
 };
+
+// Candidate filter of the radix select: the top `kb` bits of the key and the top `ib` bits of
+// the id are fixed to kp / ip.
+struct RadixState {
+    int kb, ib;
+    unsigned long long kp;
+    uint32_t ip;
+    __device__ __forceinline__ bool match(unsigned long long key, uint32_t id) const {
+        const bool km = kb == 0 || (key >> (64 - kb)) == kp;
+        const bool im = ib == 0 || (id >> (32 - ib)) == ip;
+        return km && im;
+    }
+    // digit of width w just below the fixed bits (key first, then id)
+    __device__ __forceinline__ uint32_t digit(unsigned long long key, uint32_t id, int w) const {
+        if (kb < 64) return (uint32_t)(key >> (64 - kb - w)) & ((1u << w) - 1u);
+        return (id >> (32 - ib - w)) & ((1u << w) - 1u);
+    }
+    __device__ __forceinline__ int width() const {
+        return kb < 64 ? min(8, 64 - kb) : min(8, 32 - ib);
+    }
+    __device__ __forceinline__ void fix(uint32_t d, int w) {
+        if (kb < 64) {
+            kp = (kp << w) | d;
+            kb += w;
+        } else {
+            ip = (ip << w) | d;
+            ib += w;
+        }
+    }
+};
+
+__device__ __forceinline__ double coord(const LocalSmem &S, uint32_t sd, uint32_t l) {
+    return sd == 0 ? S.x[l] : (sd == 1 ? S.y[l] : S.z[l]);
+}
+
+// Sums of a leaf's bodies (tree positions [st, st+cn) of this block), full and light mass.
+__device__ __forceinline__ void leaf_sums(const LocalSmem &S, uint32_t st, uint32_t cn,
+                                          const LocalOut &o, double f[4], double g[4]) {
+    f[0] = f[1] = f[2] = f[3] = 0.0;
+    g[0] = g[1] = g[2] = g[3] = 0.0;
+    for (uint32_t k = st; k < st + cn; ++k) {
+        const uint32_t l = S.perm[k];
+        const double mm = S.m[l];
+        f[0] += mm;
+        f[1] = fma(mm, S.x[l], f[1]);
+        f[2] = fma(mm, S.y[l], f[2]);
+        f[3] = fma(mm, S.z[l], f[3]);
+        if (o.recf && !is_heavy(S.id[l], o.heavy, o.n_heavy)) {
+            g[0] += mm;
+            g[1] = fma(mm, S.x[l], g[1]);
+            g[2] = fma(mm, S.y[l], g[2]);
+            g[3] = fma(mm, S.z[l], g[3]);
+        }
+    }
+}
+
+__device__ __forceinline__ void store_moments(const Moments &mo, uint32_t id, const double v[4]) {
+    mo.M[id] = v[0];
+    mo.S[3 * (size_t)id] = v[1];
+    mo.S[3 * (size_t)id + 1] = v[2];
+    mo.S[3 * (size_t)id + 2] = v[3];
+}
+
+__device__ __forceinline__ void load_moments(const Moments &mo, uint32_t id, double v[4]) {
+    v[0] = mo.M[id];
+    v[1] = mo.S[3 * (size_t)id];
+    v[2] = mo.S[3 * (size_t)id + 1];
+    v[3] = mo.S[3 * (size_t)id + 2];
+}
 
 __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint32_t *roots,
                                                          NodeOut no, const double *wx,
                                                          const double *wy, const double *wz,
-                                                         const uint32_t *wid,
-                                                         const double *mass, dbl4 *tpos,
-                                                         uint32_t *tid) {
+                                                         const uint32_t *wid, LocalOut o,
+                                                         uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LocalSmem &S = *reinterpret_cast<LocalSmem *>(smem_raw);
     const uint32_t root = roots[blockIdx.x];
     const uint32_t s0 = t.start[root], c0 = t.count[root];
     const uint32_t leaf = t.leaf;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nwarps = kLocalThreads / 32;
+    const uint32_t lt = (1u << lane) - 1u;
 
     for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
         S.x[k] = wx[s0 + k];
         S.y[k] = wy[s0 + k];
         S.z[k] = wz[s0 + k];
-        S.id[k] = wid[s0 + k];
+        const uint32_t id = wid[s0 + k];
+        S.id[k] = id;
+        S.m[k] = o.mass[id];
         S.perm[k] = (uint16_t)k;
     }
-    int cur = 0;
     if (threadIdx.x == 0) {
-        if (c0 > leaf) {
-            S.tab_st[0][0] = 0;
-            S.tab_cn[0][0] = c0;
-            S.tab_id[0][0] = root;
-            S.G[0] = 1;
-            S.qmax[0] = c0;
-        } else {
-            S.G[0] = 0;
-        }
+        const uint32_t g0 = c0 > leaf ? 1u : 0u;
+        S.tab_st[0] = 0;
+        S.tab_cn[0] = (uint16_t)c0;
+        S.tab_id[0] = root;
+        S.lvl_off[0] = 0;
+        S.lvl_off[1] = g0;
+        S.nlvl = g0;
     }
     __syncthreads();
 
-    while (S.G[cur] > 0) {
-        const uint32_t G = S.G[cur];
-        // bounding box and split of every internal sub-segment: one warp each
-        for (uint32_t i = warp; i < G; i += nwarps) {
-            const uint32_t st = S.tab_st[cur][i], cn = S.tab_cn[cur][i];
-            double mn[3] = {INFINITY, INFINITY, INFINITY};
-            double mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    // ================================================================ top-down split
+    for (uint32_t L = 0;; ++L) {
+        const uint32_t lo = S.lvl_off[L], hi = S.lvl_off[L + 1];
+        if (hi == lo) break;
+        for (uint32_t i = lo + warp; i < hi; i += kLocalWarps) {
+            const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
+            // ---- 1. bounding box and split
+            unsigned long long kmn[3] = {~0ull, ~0ull, ~0ull}, kmx[3] = {0ull, 0ull, 0ull};
             for (uint32_t k = lane; k < cn; k += 32) {
-                uint32_t l = S.perm[st + k];
-                double v0 = S.x[l], v1 = S.y[l], v2 = S.z[l];
-                mn[0] = fmin(mn[0], v0); mx[0] = fmax(mx[0], v0);
-                mn[1] = fmin(mn[1], v1); mx[1] = fmax(mx[1], v1);
-                mn[2] = fmin(mn[2], v2); mx[2] = fmax(mx[2], v2);
+                const uint32_t l = S.perm[st + k];
+                const unsigned long long k0 = ord_key(S.x[l]), k1 = ord_key(S.y[l]),
+                                         k2 = ord_key(S.z[l]);
+                kmn[0] = min(kmn[0], k0); kmx[0] = max(kmx[0], k0);
+                kmn[1] = min(kmn[1], k1); kmx[1] = max(kmx[1], k1);
+                kmn[2] = min(kmn[2], k2); kmx[2] = max(kmx[2], k2);
             }
+            double mn[3], mx[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                mn[d] = warp_fmin(mn[d]);
-                mx[d] = warp_fmax(mx[d]);
+                kmn[d] = warp_min(kmn[d]);
+                kmx[d] = warp_max(kmx[d]);
+                mn[d] = ord_val(kmn[d]);
+                mx[d] = ord_val(kmx[d]);
             }
+            uint32_t sd;
+            double size;
+            choose_split(mn, mx, sd, size);
             if (lane == 0) {
-                uint32_t sd;
-                double size;
-                choose_split(mn, mx, sd, size);
-                S.sd[i] = (uint8_t)sd;
-                const uint32_t id = S.tab_id[cur][i];
-                no.split_dim[id] = (uint8_t)sd;
-                no.size[id] = size;
+                no.split_dim[nid] = (uint8_t)sd;
+                no.size[nid] = size;
             }
-        }
-        __syncthreads();
-        const uint32_t P = next_pow2(S.qmax[cur]);
-        const uint32_t lgP = 31 - __clz(P);
-        const uint32_t total = G * P;
-        for (uint32_t q = threadIdx.x; q < total; q += blockDim.x) {
-            const uint32_t i = q >> lgP, k = q & (P - 1);
-            if (k < S.tab_cn[cur][i]) {
-                const uint32_t l = S.perm[S.tab_st[cur][i] + k];
-                const uint32_t sd = S.sd[i];
-                const double v = sd == 0 ? S.x[l] : (sd == 1 ? S.y[l] : S.z[l]);
-                S.key[q] = ord_key(v);
-                S.val[q] = ((unsigned long long)S.id[l] << 16) | l;
-            } else {
-                S.key[q] = ~0ull;
-                S.val[q] = ~0ull;
+            // ---- 2. exact select of rank cn/2
+            uint32_t r = cn / 2, ccount = cn;
+            RadixState rs;
+            {
+                const unsigned long long kmin = kmn[sd], kmax = kmx[sd];
+                rs.kb = __clzll((long long)(kmin ^ kmax));
+                rs.kp = rs.kb == 0 ? 0ull : (rs.kb == 64 ? kmin : (kmin >> (64 - rs.kb)));
+                rs.ib = 0;
+                rs.ip = 0;
             }
-        }
-        __syncthreads();
-        if (P > 1) bitonic_blocks(S.key, S.val, total, P);
-        for (uint32_t q = threadIdx.x; q < total; q += blockDim.x) {
-            const uint32_t i = q >> lgP, k = q & (P - 1);
-            const uint32_t cn = S.tab_cn[cur][i];
-            if (k < cn) {
-                const uint32_t l = (uint32_t)(S.val[q] & 0xffffu);
-                S.perm[S.tab_st[cur][i] + k] = (uint16_t)l;
-                if (k == cn / 2) {
-                    const uint32_t sd = S.sd[i];
-                    no.split_val[S.tab_id[cur][i]] = sd == 0 ? S.x[l] : (sd == 1 ? S.y[l] : S.z[l]);
+            uint32_t *h = S.hist[warp];
+            while (ccount > 32) {
+                if (rs.kb == 64 && rs.ib == 32) {  // cannot happen with distinct ids
+                    if (lane == 0) atomicOr(err, kErrSelect);
+                    break;
                 }
+                const int w = rs.width();
+#pragma unroll
+                for (int q = 0; q < 8; ++q) h[lane * 8 + q] = 0u;
+                __syncwarp();
+                for (uint32_t k = lane; k < cn; k += 32) {
+                    const uint32_t l = S.perm[st + k];
+                    const unsigned long long key = ord_key(coord(S, sd, l));
+                    const uint32_t id = S.id[l];
+                    if (rs.match(key, id)) atomicAdd(&h[rs.digit(key, id, w)], 1u);
+                }
+                __syncwarp();
+                uint32_t mine = 0;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) mine += h[lane * 8 + q];
+                uint32_t inc = mine;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const uint32_t v = __shfl_up_sync(kFull, inc, off);
+                    if (lane >= off) inc += v;
+                }
+                const uint32_t before = inc - mine;
+                uint32_t dsel = 0, below = 0, cnt = 0;
+                const bool owner = r >= before && r < inc;
+                if (owner) {
+                    uint32_t cum = before;
+                    for (int q = 0; q < 8; ++q) {
+                        const uint32_t c = h[lane * 8 + q];
+                        if (r < cum + c) {
+                            dsel = (uint32_t)(lane * 8 + q);
+                            below = cum;
+                            cnt = c;
+                            break;
+                        }
+                        cum += c;
+                    }
+                }
+                const int src = __ffs(__ballot_sync(kFull, owner)) - 1;
+                dsel = __shfl_sync(kFull, dsel, src);
+                below = __shfl_sync(kFull, below, src);
+                cnt = __shfl_sync(kFull, cnt, src);
+                rs.fix(dsel, w);
+                r -= below;
+                ccount = cnt;
+                __syncwarp();
             }
+            // gather the <= 32 candidates, then rank them by comparison
+            uint32_t ng = 0;
+            for (uint32_t base = 0; base < cn; base += 32) {
+                const uint32_t k = base + lane;
+                bool hit = false;
+                unsigned long long key = 0;
+                uint32_t id = 0, l = 0;
+                if (k < cn) {
+                    l = S.perm[st + k];
+                    key = ord_key(coord(S, sd, l));
+                    id = S.id[l];
+                    hit = rs.match(key, id);
+                }
+                const uint32_t m = __ballot_sync(kFull, hit);
+                if (hit) {
+                    const uint32_t off = ng + __popc(m & lt);
+                    if (off < 32) {
+                        S.ckey[warp][off] = key;
+                        S.cid[warp][off] = id;
+                        S.clid[warp][off] = (uint16_t)l;
+                    }
+                }
+                ng += __popc(m);
+            }
+            __syncwarp();
+            const bool have = (uint32_t)lane < min(ng, 32u);
+            const unsigned long long mk = have ? S.ckey[warp][lane] : ~0ull;
+            const uint32_t mi = have ? S.cid[warp][lane] : kFull;
+            uint32_t rank = 0;
+            for (int q = 0; q < 32; ++q) {
+                const unsigned long long ok = __shfl_sync(kFull, mk, q);
+                const uint32_t oi = __shfl_sync(kFull, mi, q);
+                rank += (ok < mk || (ok == mk && oi < mi)) ? 1u : 0u;
+            }
+            const uint32_t wm = __ballot_sync(kFull, have && rank == r);
+            const int ml = wm ? __ffs(wm) - 1 : 0;
+            if (!wm && lane == 0) atomicOr(err, kErrSelect);
+            const unsigned long long kmed = __shfl_sync(kFull, mk, ml);
+            const uint32_t idmed = __shfl_sync(kFull, mi, ml);
+            if (lane == 0) no.split_val[nid] = coord(S, sd, S.clid[warp][ml]);
+            // ---- 3. stable partition around the median
+            const uint32_t mid = cn / 2;
+            uint32_t offL = 0, offR = 0;
+            for (uint32_t base = 0; base < cn; base += 32) {
+                const uint32_t k = base + lane;
+                bool in = k < cn, isL = false;
+                uint32_t l = 0;
+                if (in) {
+                    l = S.perm[st + k];
+                    isL = goes_left(ord_key(coord(S, sd, l)), S.id[l], kmed, idmed);
+                }
+                const uint32_t bl = __ballot_sync(kFull, in && isL);
+                const uint32_t br = __ballot_sync(kFull, in && !isL);
+                if (in) {
+                    const uint32_t dst = isL ? offL + __popc(bl & lt) : mid + offR + __popc(br & lt);
+                    if (dst < cn) S.perm2[st + dst] = (uint16_t)l;
+                }
+                offL += __popc(bl);
+                offR += __popc(br);
+            }
+            if (offL != mid && lane == 0) atomicOr(err, kErrSelect);
+            __syncwarp();
+            for (uint32_t k = lane; k < cn; k += 32) S.perm[st + k] = S.perm2[st + k];
+            __syncwarp();
         }
-        // children that are internal form the next table (order-preserving compaction)
-        const int nx = cur ^ 1;
-        if (threadIdx.x == 0) { S.G[nx] = 0; S.qmax[nx] = 0; }
+        // ---- children that are still internal, appended as the next level
         __syncthreads();
+        const uint32_t G = hi - lo;
+        uint32_t fill = hi;
         for (uint32_t base = 0; base < 2 * G; base += blockDim.x) {
             const uint32_t u = base + threadIdx.x;
             bool keep = false;
             uint32_t cst = 0, ccn = 0, cid = 0;
             if (u < 2 * G) {
-                const uint32_t i = u >> 1;
-                const uint32_t st = S.tab_st[cur][i], cn = S.tab_cn[cur][i], id = S.tab_id[cur][i];
+                const uint32_t i = lo + (u >> 1);
+                const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], id = S.tab_id[i];
                 const uint32_t lc = cn / 2;
                 if (u & 1) {
                     cst = st + lc;
@@ -751,38 +1024,114 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
             const uint32_t m = __ballot_sync(kFull, keep);
             if (lane == 0) S.wcnt[warp] = __popc(m);
             __syncthreads();
-            uint32_t off = S.G[nx];
-            for (int q = 0; q < warp; ++q) off += S.wcnt[q];
+            uint32_t off = fill;
+            uint32_t tot = 0;
+            for (int q = 0; q < kLocalWarps; ++q) {
+                if (q < warp) off += S.wcnt[q];
+                tot += S.wcnt[q];
+            }
             if (keep) {
-                const uint32_t o = off + __popc(m & ((1u << lane) - 1u));
-                S.tab_st[nx][o] = cst;
-                S.tab_cn[nx][o] = ccn;
-                S.tab_id[nx][o] = cid;
-                atomicMax(&S.qmax[nx], ccn);
+                const uint32_t slot = off + __popc(m & lt);
+                if (slot < (uint32_t)kLocalMax) {
+                    S.tab_st[slot] = (uint16_t)cst;
+                    S.tab_cn[slot] = (uint16_t)ccn;
+                    S.tab_id[slot] = cid;
+                }
             }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                uint32_t tot = 0;
-                for (int q = 0; q < nwarps; ++q) tot += S.wcnt[q];
-                S.G[nx] += tot;
-            }
+            fill += tot;
             __syncthreads();
         }
-        cur = nx;
+        if (threadIdx.x == 0) {
+            if (L + 2 > (uint32_t)kLocalLevels || fill > (uint32_t)kLocalMax) {
+                atomicOr(err, kErrSelect);
+                fill = hi;  // stop: cannot happen for segments of <= kLocalMax bodies
+            }
+            S.lvl_off[L + 2] = fill;
+            if (fill > hi) S.nlvl = L + 2;
+        }
         __syncthreads();
     }
 
+    // ================================================================ bottom-up moments
+    const bool want_d = o.recd != nullptr, want_f = o.recf != nullptr;
+    if (c0 <= leaf) {
+        if (threadIdx.x == 0) {
+            double f[4], g[4];
+            leaf_sums(S, 0, c0, o, f, g);
+            if (want_d) {
+                store_moments(o.mo, root, f);
+                o.recd[root] = make_noded(f[0], f[1], f[2], f[3], 0.0, s0, c0);
+            }
+            if (want_f) {
+                store_moments(o.mof, root, g);
+                o.recf[root] = make_nodef(g[0], g[1], g[2], g[3], 0.0, s0, c0);
+            }
+        }
+    }
+    for (int L = (int)S.nlvl - 1; L >= 0; --L) {
+        for (uint32_t i = S.lvl_off[L] + threadIdx.x; i < S.lvl_off[L + 1]; i += blockDim.x) {
+            const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
+            const uint32_t lc = cn / 2;
+            double fs[4] = {0.0, 0.0, 0.0, 0.0}, gs[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int side = 0; side < 2; ++side) {
+                const uint32_t cst = side ? st + lc : st;
+                const uint32_t ccn = side ? cn - lc : lc;
+                const uint32_t cid = side ? nid + 1 + t.ttab[lc] : nid + 1;
+                double f[4], g[4];
+                if (ccn <= leaf) {
+                    leaf_sums(S, cst, ccn, o, f, g);
+                    if (want_d) {
+                        store_moments(o.mo, cid, f);
+                        o.recd[cid] = make_noded(f[0], f[1], f[2], f[3], 0.0, s0 + cst, ccn);
+                    }
+                    if (want_f) {
+                        store_moments(o.mof, cid, g);
+                        o.recf[cid] = make_nodef(g[0], g[1], g[2], g[3], 0.0, s0 + cst, ccn);
+                    }
+                } else {
+                    if (want_d) load_moments(o.mo, cid, f);
+                    if (want_f) load_moments(o.mof, cid, g);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    fs[q] = __dadd_rn(fs[q], f[q]);
+                    gs[q] = __dadd_rn(gs[q], g[q]);
+                }
+            }
+            const double size = no.size[nid];
+            const uint32_t right = nid + 1 + t.ttab[lc];
+            if (want_d) {
+                store_moments(o.mo, nid, fs);
+                o.recd[nid] = make_noded(fs[0], fs[1], fs[2], fs[3], size, right, 0u);
+            }
+            if (want_f) {
+                store_moments(o.mof, nid, gs);
+                o.recf[nid] = make_nodef(gs[0], gs[1], gs[2], gs[3], size, right, 0u);
+            }
+        }
+        __syncthreads();
+    }
+
+    // ================================================================ tree-ordered bodies
     for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
         const uint32_t l = S.perm[k];
         const uint32_t id = S.id[l];
-        tpos[s0 + k] = make_double4_32a(S.x[l], S.y[l], S.z[l], mass[id]);
-        tid[s0 + k] = id;
+        const double x = S.x[l], y = S.y[l], z = S.z[l], mm = S.m[l];
+        o.tpos[s0 + k] = make_double4_32a(x, y, z, mm);
+        o.tid[s0 + k] = id;
+        if (want_f) {
+            const float hx = (float)x, hy = (float)y, hz = (float)z;
+            const float fm = is_heavy(id, o.heavy, o.n_heavy) ? 0.0f : (float)mm;
+            o.thi[s0 + k] = make_float4(hx, hy, hz, fm);
+            o.tlo[s0 + k] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
+                                        (float)(z - (double)hz), 0.0f);
+        }
     }
 }
 
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
-                  const NodeOut &no, const Work &w, int cur, const double *mass,
-                  dbl4 *tpos, uint32_t *tid, cudaStream_t st) {
+                  const NodeOut &no, const Work &w, int cur, const LocalOut &out, uint32_t *err,
+                  cudaStream_t st) {
     static bool attr_set = false;
     const size_t smem = sizeof(LocalSmem);
     if (!attr_set) {
@@ -790,7 +1139,53 @@ void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
         attr_set = true;
     }
     k_local<<<n_roots, kLocalThreads, smem, st>>>(t, roots, no, w.x[cur], w.y[cur], w.z[cur],
-                                                  w.id[cur], mass, tpos, tid);
+                                                  w.id[cur], out, err);
+}
+
+// ------------------------------------------------------------------ moments above the local roots
+
+// One thread per local root climbs; the second child to arrive at a parent combines both
+// children (left + right, a fixed order) and continues upward.
+__global__ void k_moments_top(Topology t, const uint32_t *roots, uint32_t n_roots, NodeOut no,
+                              LocalOut o) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_roots) return;
+    const bool want_d = o.recd != nullptr, want_f = o.recf != nullptr;
+    uint32_t node = t.parent[roots[i]];
+    uint32_t *counter = want_d ? o.mo.counter : o.mof.counter;
+    while (node != 0xffffffffu) {
+        __threadfence();
+        if (atomicAdd(&counter[node], 1u) == 0u) return;
+        __threadfence();
+        const uint32_t L = node + 1, R = t.right[node];
+        const double size = no.size[node];
+        if (want_d) {
+            double v[4];
+            v[0] = __dadd_rn(__ldcg(&o.mo.M[L]), __ldcg(&o.mo.M[R]));
+            for (int d = 0; d < 3; ++d)
+                v[1 + d] = __dadd_rn(__ldcg(&o.mo.S[3 * (size_t)L + d]),
+                                     __ldcg(&o.mo.S[3 * (size_t)R + d]));
+            store_moments(o.mo, node, v);
+            o.recd[node] = make_noded(v[0], v[1], v[2], v[3], size, R, 0u);
+        }
+        if (want_f) {
+            double v[4];
+            v[0] = __dadd_rn(__ldcg(&o.mof.M[L]), __ldcg(&o.mof.M[R]));
+            for (int d = 0; d < 3; ++d)
+                v[1 + d] = __dadd_rn(__ldcg(&o.mof.S[3 * (size_t)L + d]),
+                                     __ldcg(&o.mof.S[3 * (size_t)R + d]));
+            store_moments(o.mof, node, v);
+            o.recf[node] = make_nodef(v[0], v[1], v[2], v[3], size, R, 0u);
+        }
+        node = t.parent[node];
+    }
+}
+
+void launch_moments_top(const Topology &t, const uint32_t *roots, uint32_t n_roots,
+                        const NodeOut &no, const LocalOut &out, cudaStream_t st) {
+    uint32_t *counter = out.recd ? out.mo.counter : out.mof.counter;
+    cudaMemsetAsync(counter, 0, sizeof(uint32_t) * t.n_nodes, st);
+    k_moments_top<<<(n_roots + 127) / 128, 128, 0, st>>>(t, roots, n_roots, no, out);
 }
 
 }  // namespace kd

@@ -29,7 +29,7 @@ constexpr int kSelThreads = 512;
 constexpr uint32_t kMultiMin = 32768;  // segments above this use multi-block histograms
 constexpr int kSelMaxIters = 16;    // radix refinement passes before giving up (error)
 constexpr int kWalkWarps = 4;       // warps per walk block
-constexpr int kStackMax = 64;       // per-warp traversal stack entries
+constexpr int kStackMax = 32;       // traversal stack entries: one per lane of a warp
 constexpr int kMaxHeavy = 8;        // bodies summed directly in FP64 on the mixed path
 
 // device error flags (bit set in ctx->dev_err)
@@ -49,24 +49,27 @@ struct __align__(16) NodeD {
 };
 static_assert(sizeof(NodeD) == 56 || sizeof(NodeD) == 64, "NodeD layout");
 
-// Walk record of the mixed path: centre of mass as hi+lo floats, light mass, size^2.
+// Walk record of the mixed path: centre of mass as hi+lo floats, size^2, light mass.  The
+// opening test reads only `hi` and `a, b`; an accepted node also reads `lo`.
 struct __align__(16) NodeF {
-    float4 hi;  // cm hi x,y,z ; light mass
-    float4 lo;  // cm lo x,y,z ; size^2
+    float4 hi;  // cm hi x,y,z ; size^2
+    float4 lo;  // cm lo x,y,z ; light mass
     uint32_t a, b, pad0, pad1;
 };
 
 // Per-segment state of the median select at one level of the multi-block build.
 struct SegSel {
     uint32_t sd;      // split dimension
-    uint32_t shift;   // first-pass digit shift
-    uint32_t digit;   // selected first-pass digit
+    float scale;      // first pass: bin = (float)(v - lo) * scale, clamped to the bin range
+    uint32_t digit;   // selected first-pass bin
     uint32_t c;       // candidates left
     uint32_t r;       // rank wanted among the candidates
     uint32_t pad;
     uint64_t kmed;    // median key (order-preserving transform of the coordinate)
     uint32_t idmed;   // median body id (tie break)
     uint32_t posmed;  // position of the median inside the segment
+    float lo;         // smallest coordinate along sd, truncated to float
+    uint32_t pad2;
 };
 
 // ---------------------------------------------------------------- argument blocks
@@ -99,7 +102,7 @@ struct Work {              // ping-pong buffers of the level passes (segment ord
 };
 
 struct Scratch {
-    unsigned long long *bmin, *bmax;  // [G*3] ordered keys
+    unsigned long long *bmin[2], *bmax[2];  // [G*3] ordered keys, ping-pong by level
     SegSel *sel;
     uint32_t *hist;                   // [G*kHistBins]
     uint32_t *cand_cnt;               // [G]
@@ -114,27 +117,81 @@ struct Bodies {             // master state, original order
 };
 
 // ---------------------------------------------------------------- launchers (kd_build.cu)
-void launch_init_work(const Bodies &b, Work &w, uint32_t n, cudaStream_t st);
-// returns the number of kernels it launched
-int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
-                 Scratch &s, cudaStream_t st);
-void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
-                  const NodeOut &no, const Work &w, int cur, const double *mass,
-                  dbl4 *tpos, uint32_t *tid, cudaStream_t st);
-
-// ---------------------------------------------------------------- launchers (kd_walk.cu)
 struct Moments {
-    double *M;                // [n_nodes]
-    double *S;                // [3*n_nodes] sum m*p
-    uint32_t *counter;        // [n_nodes] arrival counters
+    double *M;                // [n_nodes] mass
+    double *S;                // [3*n_nodes] sum of m*p
+    uint32_t *counter;        // [n_nodes] arrival counters of the upward pass
 };
 
-void launch_moments_fp64(const Topology &t, const NodeOut &no, const dbl4 *tpos,
-                         Moments &mo, NodeD *rec, cudaStream_t st);
-void launch_split_mixed(const dbl4 *tpos, const uint32_t *tid, const uint32_t *heavy_ids,
-                        int n_heavy, uint32_t n, float4 *thi, float4 *tlo, cudaStream_t st);
-void launch_moments_mixed(const Topology &t, const NodeOut &no, const dbl4 *tpos,
-                          const float4 *thi, Moments &mo, NodeF *rec, cudaStream_t st);
+// What the subtree finish writes besides the tree itself.
+struct LocalOut {
+    const double *mass;          // master masses, original order
+    dbl4 *tpos;                  // bodies in tree order (x, y, z, m)
+    uint32_t *tid;               // body index of every tree position
+    float4 *thi, *tlo;           // split coordinates, tree order (mixed records only)
+    Moments mo;                  // full-mass moments (FP64 records)
+    Moments mof;                 // light-mass moments (mixed records)
+    NodeD *recd;                 // FP64 walk records, or nullptr
+    NodeF *recf;                 // mixed walk records, or nullptr
+    const uint32_t *heavy;       // bodies left out of the FP32 masses
+    int n_heavy;
+};
+
+__device__ __forceinline__ bool is_heavy(uint32_t id, const uint32_t *heavy_ids, int n_heavy) {
+    bool h = false;
+    for (int i = 0; i < n_heavy; ++i) h |= heavy_ids[i] == id;
+    return h;
+}
+
+// FP64 record: cm /= m and size*size in the reference's IEEE order
+// (array_kd_tree.rs:548-550, :606).
+__device__ __forceinline__ NodeD make_noded(double m, double sx, double sy, double sz,
+                                            double size, uint32_t a, uint32_t b) {
+    NodeD q;
+    q.cmx = __ddiv_rn(sx, m);
+    q.cmy = __ddiv_rn(sy, m);
+    q.cmz = __ddiv_rn(sz, m);
+    q.m = m;
+    q.size2 = __dmul_rn(size, size);
+    q.a = a;
+    q.b = b;
+    q.pad = 0.0;
+    return q;
+}
+
+// Mixed record: cm as hi + lo floats.  A massless node gets a NaN cm and is never accepted.
+__device__ __forceinline__ NodeF make_nodef(double m, double sx, double sy, double sz,
+                                            double size, uint32_t a, uint32_t b) {
+    NodeF r;
+    const double inv = 1.0 / m;
+    const double cx = sx * inv, cy = sy * inv, cz = sz * inv;
+    const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
+    r.hi = make_float4(hx, hy, hz, (float)(size * size));
+    r.lo = make_float4((float)(cx - (double)hx), (float)(cy - (double)hy),
+                       (float)(cz - (double)hz), (float)m);
+    r.a = a;
+    r.b = b;
+    r.pad0 = r.pad1 = 0u;
+    return r;
+}
+
+void launch_init_work(const Bodies &b, Work &w, uint32_t n, cudaStream_t st);
+// One multi-block level.  `lvl` selects the bounding-box buffers (lvl & 1); the boxes of
+// level 0 are computed here, deeper levels receive theirs from the previous level's scatter
+// (`G_next` > 0 when the next level is a multi-block level too).  Returns the number of
+// kernels launched.
+int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
+                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st);
+// Subtree finish of every local root: split decisions, tree order, and the moments and
+// walk records of all nodes below the local roots.
+void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
+                  const NodeOut &no, const Work &w, int cur, const LocalOut &out, uint32_t *err,
+                  cudaStream_t st);
+// Moments and records of the nodes above the local roots (one thread per local root climbs).
+void launch_moments_top(const Topology &t, const uint32_t *roots, uint32_t n_roots,
+                        const NodeOut &no, const LocalOut &out, cudaStream_t st);
+
+// ---------------------------------------------------------------- launchers (kd_walk.cu)
 void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
                       double theta, double *acc, uint32_t *err,
                       unsigned long long *counts, cudaStream_t st);

@@ -15,163 +15,6 @@
 namespace kd {
 
 static constexpr uint32_t kFull = 0xffffffffu;
-static constexpr uint32_t kNone = 0xffffffffu;
-
-// ------------------------------------------------------------------ upward pass
-
-// One thread per leaf sums its bodies, then climbs: the second child to arrive at a parent
-// combines both children (left + right, a fixed order) and continues upward.
-__global__ void k_moments_fp64(Topology t, NodeOut no, const dbl4 *tpos, Moments mo,
-                               NodeD *rec) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= t.n_leaves) return;
-    const uint32_t id = t.leaves[i];
-    const uint32_t st = t.start[id], cn = t.count[id];
-    double M = 0.0, Sx = 0.0, Sy = 0.0, Sz = 0.0;
-    for (uint32_t k = st; k < st + cn; ++k) {
-        const dbl4 q = tpos[k];
-        M += q.w;
-        Sx = fma(q.w, q.x, Sx);
-        Sy = fma(q.w, q.y, Sy);
-        Sz = fma(q.w, q.z, Sz);
-    }
-    mo.M[id] = M;
-    mo.S[3 * id] = Sx;
-    mo.S[3 * id + 1] = Sy;
-    mo.S[3 * id + 2] = Sz;
-    NodeD r;
-    r.cmx = Sx; r.cmy = Sy; r.cmz = Sz; r.m = M;
-    r.size2 = 0.0;
-    r.a = st;
-    r.b = cn;
-    r.pad = 0.0;
-    rec[id] = r;
-    uint32_t node = t.parent[id];
-    while (node != kNone) {
-        __threadfence();
-        if (atomicAdd(&mo.counter[node], 1u) == 0u) return;
-        __threadfence();
-        const uint32_t L = node + 1, R = t.right[node];
-        const double m = __dadd_rn(__ldcg(&mo.M[L]), __ldcg(&mo.M[R]));
-        const double sx = __dadd_rn(__ldcg(&mo.S[3 * L]), __ldcg(&mo.S[3 * R]));
-        const double sy = __dadd_rn(__ldcg(&mo.S[3 * L + 1]), __ldcg(&mo.S[3 * R + 1]));
-        const double sz = __dadd_rn(__ldcg(&mo.S[3 * L + 2]), __ldcg(&mo.S[3 * R + 2]));
-        mo.M[node] = m;
-        mo.S[3 * node] = sx;
-        mo.S[3 * node + 1] = sy;
-        mo.S[3 * node + 2] = sz;
-        const double size = no.size[node];
-        NodeD q;
-        // cm /= m as array_kd_tree.rs:548-550; size*size as :606
-        q.cmx = __ddiv_rn(sx, m);
-        q.cmy = __ddiv_rn(sy, m);
-        q.cmz = __ddiv_rn(sz, m);
-        q.m = m;
-        q.size2 = __dmul_rn(size, size);
-        q.a = R;
-        q.b = 0u;
-        q.pad = 0.0;
-        rec[node] = q;
-        node = t.parent[node];
-    }
-}
-
-void launch_moments_fp64(const Topology &t, const NodeOut &no, const dbl4 *tpos,
-                         Moments &mo, NodeD *rec, cudaStream_t st) {
-    cudaMemsetAsync(mo.counter, 0, sizeof(uint32_t) * t.n_nodes, st);
-    k_moments_fp64<<<(t.n_leaves + 255) / 256, 256, 0, st>>>(t, no, tpos, mo, rec);
-}
-
-__device__ __forceinline__ bool is_heavy(uint32_t id, const uint32_t *heavy_ids, int n_heavy) {
-    bool h = false;
-    for (int i = 0; i < n_heavy; ++i) h |= heavy_ids[i] == id;
-    return h;
-}
-
-// Tree-ordered split coordinates: hi = fl32(x), lo = fl32(x - hi); heavy bodies get a zero
-// FP32 mass (their pull is added in FP64).
-__global__ void k_split_mixed(const dbl4 *tpos, const uint32_t *tid,
-                              const uint32_t *heavy_ids, int n_heavy, uint32_t n, float4 *thi,
-                              float4 *tlo) {
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += gridDim.x * blockDim.x) {
-        const dbl4 q = tpos[k];
-        const float hx = (float)q.x, hy = (float)q.y, hz = (float)q.z;
-        const float lx = (float)(q.x - (double)hx), ly = (float)(q.y - (double)hy),
-                    lz = (float)(q.z - (double)hz);
-        const float m = is_heavy(tid[k], heavy_ids, n_heavy) ? 0.0f : (float)q.w;
-        thi[k] = make_float4(hx, hy, hz, m);
-        tlo[k] = make_float4(lx, ly, lz, 0.0f);
-    }
-}
-
-void launch_split_mixed(const dbl4 *tpos, const uint32_t *tid, const uint32_t *heavy_ids,
-                        int n_heavy, uint32_t n, float4 *thi, float4 *tlo, cudaStream_t st) {
-    int blocks = (int)((n + 255) / 256);
-    if (blocks > 8192) blocks = 8192;
-    k_split_mixed<<<blocks, 256, 0, st>>>(tpos, tid, heavy_ids, n_heavy, n, thi, tlo);
-}
-
-__device__ __forceinline__ NodeF make_nodef(double sx, double sy, double sz, double m,
-                                            double size2, uint32_t a, uint32_t b) {
-    NodeF r;
-    const double cx = sx / m, cy = sy / m, cz = sz / m;  // NaN for massless nodes: never accepted
-    const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
-    r.hi = make_float4(hx, hy, hz, (float)m);
-    r.lo = make_float4((float)(cx - (double)hx), (float)(cy - (double)hy),
-                       (float)(cz - (double)hz), (float)size2);
-    r.a = a;
-    r.b = b;
-    r.pad0 = r.pad1 = 0u;
-    return r;
-}
-
-// Upward pass of the light (FP32-summed) masses.  Moments are accumulated in FP64.
-__global__ void k_moments_mixed(Topology t, NodeOut no, const dbl4 *tpos, const float4 *thi,
-                                Moments mo, NodeF *rec) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= t.n_leaves) return;
-    const uint32_t id = t.leaves[i];
-    const uint32_t st = t.start[id], cn = t.count[id];
-    double M = 0.0, Sx = 0.0, Sy = 0.0, Sz = 0.0;
-    for (uint32_t k = st; k < st + cn; ++k) {
-        const dbl4 q = tpos[k];
-        const double m = thi[k].w == 0.0f ? 0.0 : q.w;
-        M += m;
-        Sx = fma(m, q.x, Sx);
-        Sy = fma(m, q.y, Sy);
-        Sz = fma(m, q.z, Sz);
-    }
-    mo.M[id] = M;
-    mo.S[3 * id] = Sx;
-    mo.S[3 * id + 1] = Sy;
-    mo.S[3 * id + 2] = Sz;
-    rec[id] = make_nodef(Sx, Sy, Sz, M, 0.0, st, cn);
-    uint32_t node = t.parent[id];
-    while (node != kNone) {
-        __threadfence();
-        if (atomicAdd(&mo.counter[node], 1u) == 0u) return;
-        __threadfence();
-        const uint32_t L = node + 1, R = t.right[node];
-        const double m = __ldcg(&mo.M[L]) + __ldcg(&mo.M[R]);
-        const double sx = __ldcg(&mo.S[3 * L]) + __ldcg(&mo.S[3 * R]);
-        const double sy = __ldcg(&mo.S[3 * L + 1]) + __ldcg(&mo.S[3 * R + 1]);
-        const double sz = __ldcg(&mo.S[3 * L + 2]) + __ldcg(&mo.S[3 * R + 2]);
-        mo.M[node] = m;
-        mo.S[3 * node] = sx;
-        mo.S[3 * node + 1] = sy;
-        mo.S[3 * node + 2] = sz;
-        const double size = no.size[node];
-        rec[node] = make_nodef(sx, sy, sz, m, size * size, R, 0u);
-        node = t.parent[node];
-    }
-}
-
-void launch_moments_mixed(const Topology &t, const NodeOut &no, const dbl4 *tpos,
-                          const float4 *thi, Moments &mo, NodeF *rec, cudaStream_t st) {
-    cudaMemsetAsync(mo.counter, 0, sizeof(uint32_t) * t.n_nodes, st);
-    k_moments_mixed<<<(t.n_leaves + 255) / 256, 256, 0, st>>>(t, no, tpos, thi, mo, rec);
-}
 
 // ------------------------------------------------------------------ FP64 walk
 
@@ -191,13 +34,14 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
     const NodeD *__restrict__ rec, const dbl4 *__restrict__ tpos,
     const uint32_t *__restrict__ tid, uint32_t n, double theta2, double *__restrict__ acc,
     uint32_t *err, unsigned long long *counts) {
-    __shared__ uint2 stack[kWalkWarps][kStackMax];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t s = (blockIdx.x * kWalkWarps + warp) * 32 + lane;
     const bool valid = s < n;
     uint32_t mask = __ballot_sync(kFull, valid);
     if (mask == 0) return;
     const uint32_t bit = 1u << lane;
+    // traversal stack: entry k (pending right child, lanes still descending) lives in lane k
+    uint32_t st_node = 0, st_mask = 0;
     dbl4 me = valid ? tpos[s] : make_double4_32a(0.0, 0.0, 0.0, 0.0);
     double ax = 0.0, ay = 0.0, az = 0.0;
     unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
@@ -254,7 +98,10 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
                     if (lane == 0) atomicOr(err, kErrStack);
                     break;
                 }
-                if (lane == 0) stack[warp][sp] = make_uint2(a, open);
+                if (lane == sp) {
+                    st_node = a;
+                    st_mask = open;
+                }
                 ++sp;
                 node = node + 1;
                 mask = open;
@@ -263,12 +110,9 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
         }
         if (descend) continue;
         if (sp == 0) break;
-        __syncwarp();
         --sp;
-        const uint2 e = stack[warp][sp];
-        node = e.x;
-        mask = e.y;
-        __syncwarp();
+        node = __shfl_sync(kFull, st_node, sp);
+        mask = __shfl_sync(kFull, st_mask, sp);
     }
     if (valid) {
         const uint32_t o = tid[s];
@@ -325,7 +169,6 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     const float4 *__restrict__ tlo, const uint32_t *__restrict__ tid, uint32_t n, float theta2,
     Bodies b, const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
     uint32_t *err, unsigned long long *counts) {
-    __shared__ uint2 stack[kWalkWarps][kStackMax];
     __shared__ HeavyBody heavy[kMaxHeavy];
     if (threadIdx.x < n_heavy) {
         const uint32_t h = heavy_ids[threadIdx.x];
@@ -342,17 +185,19 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     const float4 ml = valid ? tlo[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
+    uint32_t st_node = 0, st_mask = 0;  // lane k holds stack entry k
     uint32_t node = 0;
     int sp = 0;
     while (true) {
-        const NodeF r = rec[node];
+        const float4 nh = __ldg(&rec[node].hi);
+        const uint2 ab = __ldg(reinterpret_cast<const uint2 *>(&rec[node].a));
         if (kCount) c_vis += (mask & bit) ? 1 : 0;
         bool descend = false;
-        if (r.b != 0u) {
+        if (ab.y != 0u) {
             if (mask & bit) {
                 float px = 0.f, py = 0.f, pz = 0.f;
-                for (uint32_t k = 0; k < r.b; ++k) {
-                    const uint32_t j = r.a + k;
+                for (uint32_t k = 0; k < ab.y; ++k) {
+                    const uint32_t j = ab.x + k;
                     if (j == s) continue;
                     const float4 qh = __ldg(&thi[j]);
                     const float4 ql = __ldg(&tlo[j]);
@@ -374,28 +219,39 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
         } else {
             bool take = false;
             if (mask & bit) {
-                const float dx = (mh.x - r.hi.x) + (ml.x - r.lo.x);
-                const float dy = (mh.y - r.hi.y) + (ml.y - r.lo.y);
-                const float dz = (mh.z - r.hi.z) + (ml.z - r.lo.z);
-                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                // opening test on the high parts: an approximate decision suffices here
+                const float ex = mh.x - nh.x, ey = mh.y - nh.y, ez = mh.z - nh.z;
+                const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
                 if (kCount) ++c_open;
-                if (r.lo.w < theta2 * d2) {
-                    take = true;
+                take = nh.w < theta2 * e2;
+            }
+            const uint32_t tk = __ballot_sync(kFull, take);
+            if (tk) {
+                const float4 nl = __ldg(&rec[node].lo);
+                if (take) {
+                    // force on the split coordinates
+                    const float dx = (mh.x - nh.x) + (ml.x - nl.x);
+                    const float dy = (mh.y - nh.y) + (ml.y - nl.y);
+                    const float dz = (mh.z - nh.z) + (ml.z - nl.z);
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     const float inv = rsqrtf(d2);
-                    const float f = -r.hi.w * (inv * inv * inv);
+                    const float f = -nl.w * (inv * inv * inv);
                     kahan_add(sx, cx, f * dx);
                     kahan_add(sy, cy, f * dy);
                     kahan_add(sz, cz, f * dz);
                     if (kCount) ++c_m2p;
                 }
             }
-            const uint32_t open = mask & ~__ballot_sync(kFull, take);
+            const uint32_t open = mask & ~tk;
             if (open) {
                 if (sp >= kStackMax) {
                     if (lane == 0) atomicOr(err, kErrStack);
                     break;
                 }
-                if (lane == 0) stack[warp][sp] = make_uint2(r.a, open);
+                if (lane == sp) {
+                    st_node = ab.x;
+                    st_mask = open;
+                }
                 ++sp;
                 node = node + 1;
                 mask = open;
@@ -404,12 +260,9 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
         }
         if (descend) continue;
         if (sp == 0) break;
-        __syncwarp();
         --sp;
-        const uint2 e = stack[warp][sp];
-        node = e.x;
-        mask = e.y;
-        __syncwarp();
+        node = __shfl_sync(kFull, st_node, sp);
+        mask = __shfl_sync(kFull, st_mask, sp);
     }
     if (valid) {
         const uint32_t o = tid[s];
