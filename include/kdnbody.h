@@ -158,6 +158,22 @@ int kd_set_timing(kd_ctx *ctx, int32_t on);
  * tree walks; O(ns * n). */
 int kd_direct_accel(kd_ctx *ctx, const uint64_t *sinks, size_t ns, double *acc);
 
+/* Adjoint (reverse mode) of the step loop, autograd.Function style: kd_forward runs
+ * `steps` steps like kd_simple_sim (the context must use KD_PREC_MIXED) and keeps a
+ * checkpoint of (x, v) every `ckpt_every` steps in device memory; kd_backward takes the
+ * gradient of a loss with respect to the final positions and velocities (host, 3*n each,
+ * dL_dv may be NULL for zero) and returns the gradients with respect to the initial ones
+ * (host, 3*n each).  Each checkpoint segment is recomputed forward, then walked back step
+ * by step: mu = lv + dt*lx; lv = mu; lx += dt * J(x_n)^T mu, J = da/dx over the interaction
+ * set of the forward walk (tidal tensors; node sources pushed down to their bodies with
+ * weight m_i/M).  The bodies are left at the final state.  A tape may be consumed by
+ * several kd_backward calls; kd_tape_free releases it.  No counterpart in the reference
+ * (which has no derivatives); it differentiates simple_sim (array_kd_tree.rs:623-664). */
+int kd_forward(kd_ctx *ctx, double dt, int64_t steps, int64_t ckpt_every, kd_tape **tape);
+int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double *g_x0,
+                double *g_v0);
+void kd_tape_free(kd_tape *tape);
+
 /* Interaction counts of the last walk, summed over bodies: out[0] = pair (P2P)
  * interactions, out[1] = opening tests at internal nodes, out[2] = accepted multipole
  * (M2P) interactions, out[3] = nodes visited by the warps.  Counting is enabled by

@@ -82,6 +82,10 @@ SIGNATURES = {
     "kd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(KdStats)]),
     "kd_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "kd_direct_accel": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "kd_forward": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, C.c_int64,
+                             C.POINTER(C.c_void_p)]),
+    "kd_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "kd_tape_free": (None, [C.c_void_p]),
     "kd_set_counting": (C.c_int, [C.c_void_p, C.c_int32]),
     "kd_get_counts": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
 }

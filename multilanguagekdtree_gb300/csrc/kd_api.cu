@@ -166,7 +166,7 @@ struct kd_ctx {
     NodeF *recf = nullptr;
     dbl4 *tpos = nullptr;
     uint32_t *tid = nullptr;
-    float4 *thi = nullptr, *tlo = nullptr;
+    float4 *thi = nullptr, *tlo = nullptr, *trel = nullptr;
     uint32_t *dev_err = nullptr;
     unsigned long long *d_counts = nullptr;
     uint32_t *d_heavy = nullptr, *d_nheavy = nullptr;
@@ -184,6 +184,13 @@ struct kd_ctx {
     cudaEvent_t ev[6] = {};
 
     std::vector<void *> owned;
+
+    // adjoint state, allocated by the first kd_forward
+    bool adj_ready = false;
+    int64_t adj_every = 0;
+    double *lx = nullptr, *lv = nullptr, *amu = nullptr, *ay = nullptr, *ysink = nullptr,
+           *yheavy = nullptr, *segbuf = nullptr;
+    float *aU = nullptr, *aG = nullptr;
 
     int fail(int code, const char *fmt, ...) {
         char buf[512];
@@ -304,6 +311,7 @@ int setup(kd_ctx *c) {
     KD_CHECK(c, c->alloc(&c->tid, n));
     KD_CHECK(c, c->alloc(&c->thi, n));
     KD_CHECK(c, c->alloc(&c->tlo, n));
+    KD_CHECK(c, c->alloc(&c->trel, n));
     KD_CHECK(c, c->alloc(&c->d_counts, 4));
     KD_CHECK(c, c->alloc(&c->d_heavy, kMaxHeavy));
     KD_CHECK(c, c->alloc(&c->d_nheavy, 1));
@@ -356,6 +364,7 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     o.tid = c->tid;
     o.thi = c->thi;
     o.tlo = c->tlo;
+    o.trel = c->trel;
     o.mo = c->mom;
     o.mof = c->momf;
     o.recd = want_d ? c->recd : nullptr;
@@ -372,7 +381,7 @@ void enqueue_walk(kd_ctx *c) {
     c->launches += 1;
     unsigned long long *cnt = c->counting ? c->d_counts : nullptr;
     if (c->prm.precision == KD_PREC_MIXED)
-        launch_walk_mixed(c->recf, c->thi, c->tlo, c->tid, (uint32_t)c->n, c->prm.theta,
+        launch_walk_mixed(c->recf, c->thi, c->tlo, c->trel, c->tid, (uint32_t)c->n, c->prm.theta,
                           c->bodies, c->d_heavy, c->n_heavy, c->acc, c->dev_err, cnt, c->st);
     else
         launch_walk_fp64(c->recd, c->tpos, c->tid, (uint32_t)c->n, c->prm.theta, c->acc,
@@ -400,6 +409,59 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 }  // namespace
+
+struct kd_tape_impl {
+    kd_ctx *ctx;
+    double dt;
+    int64_t steps, every;
+    std::vector<double *> ck;  // per checkpoint: x|y|z|vx|vy|vz (6n)
+    double *final_state;       // 6n
+};
+
+int copy_state(kd_ctx *c, double *dst6, bool to_buffer) {
+    const size_t n = c->n, b = n * sizeof(double);
+    double *arr[6] = {c->bodies.x, c->bodies.y, c->bodies.z,
+                      c->bodies.vx, c->bodies.vy, c->bodies.vz};
+    for (int k = 0; k < 6; ++k) {
+        if (to_buffer)
+            KD_CHECK(c, cudaMemcpyAsync(dst6 + k * n, arr[k], b, cudaMemcpyDeviceToDevice, c->st));
+        else
+            KD_CHECK(c, cudaMemcpyAsync(arr[k], dst6 + k * n, b, cudaMemcpyDeviceToDevice, c->st));
+    }
+    return KD_OK;
+}
+
+int adj_alloc(kd_ctx *c, int64_t every) {
+    if (c->adj_ready && c->adj_every >= every) return KD_OK;
+    const size_t n = c->n;
+    if (!c->adj_ready) {
+        KD_CHECK(c, c->alloc(&c->lx, 3 * n));
+        KD_CHECK(c, c->alloc(&c->lv, 3 * n));
+        KD_CHECK(c, c->alloc(&c->amu, 3 * n));
+        KD_CHECK(c, c->alloc(&c->ay, 3 * n));
+        KD_CHECK(c, c->alloc(&c->ysink, 3 * n));
+        KD_CHECK(c, c->alloc(&c->yheavy, 3 * kMaxHeavy));
+        KD_CHECK(c, c->alloc(&c->aU, 3 * n));
+        KD_CHECK(c, c->alloc(&c->aG, 3 * (size_t)c->plan.n_nodes));
+    }
+    if (c->segbuf) {
+        cudaFree(c->segbuf);
+        c->owned.erase(std::find(c->owned.begin(), c->owned.end(), (void *)c->segbuf));
+        c->segbuf = nullptr;
+    }
+    KD_CHECK(c, c->alloc(&c->segbuf, 3 * n * (size_t)every));
+    c->adj_every = every;
+    c->adj_ready = true;
+    return KD_OK;
+}
+
+void enqueue_step(kd_ctx *c, double dt) {
+    const bool mixed = c->prm.precision == KD_PREC_MIXED;
+    enqueue_build(c, !mixed, mixed);
+    enqueue_walk(c);
+    launch_kick_drift(c->bodies, c->acc, (uint32_t)c->n, dt, c->st);
+    c->launches += 1;
+}
 
 // ====================================================================== C ABI
 
@@ -697,6 +759,154 @@ int kd_get_stats(const kd_ctx *c, kd_stats *out) {
     if (!c || !out) return KD_EINVAL;
     *out = c->stats;
     return KD_OK;
+}
+
+int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape **out) {
+    if (!c) return KD_EINVAL;
+    if (!out) return c->fail(KD_EINVAL, "tape pointer is NULL");
+    *out = nullptr;
+    if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
+    if (c->prm.precision != KD_PREC_MIXED)
+        return c->fail(KD_EINVAL, "the adjoint is implemented for KD_PREC_MIXED contexts");
+    if (steps < 1 || ckpt_every < 1) return c->fail(KD_EINVAL, "steps and ckpt_every must be >= 1");
+    if (dt == 0.0) dt = c->prm.dt;
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    int rc = adj_alloc(c, ckpt_every);
+    if (rc) return rc;
+    kd_tape_impl *t = new (std::nothrow) kd_tape_impl();
+    if (!t) return c->fail(KD_ENOMEM, "out of host memory");
+    t->ctx = c;
+    t->dt = dt;
+    t->steps = steps;
+    t->every = ckpt_every;
+    t->final_state = nullptr;
+    const size_t nck = (size_t)((steps + ckpt_every - 1) / ckpt_every);
+    cudaError_t e = cudaSuccess;
+    for (size_t k = 0; k < nck && e == cudaSuccess; ++k) {
+        double *p = nullptr;
+        e = cudaMalloc((void **)&p, 6 * c->n * sizeof(double));
+        if (e == cudaSuccess) t->ck.push_back(p);
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void **)&t->final_state, 6 * c->n * sizeof(double));
+    if (e != cudaSuccess) {
+        kd_tape_free(reinterpret_cast<kd_tape *>(t));
+        return c->cuda_fail(e, "checkpoint allocation");
+    }
+    c->launches = 0;
+    KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
+    for (int64_t s = 0; s < steps; ++s) {
+        if (s % ckpt_every == 0) {
+            rc = copy_state(c, t->ck[(size_t)(s / ckpt_every)], true);
+            if (rc) break;
+        }
+        enqueue_step(c, dt);
+    }
+    if (!rc) rc = copy_state(c, t->final_state, true);
+    KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
+    if (!rc) rc = check_device(c);
+    if (rc) {
+        kd_tape_free(reinterpret_cast<kd_tape *>(t));
+        return rc;
+    }
+    c->has_tree = false;
+    c->stats = kd_stats{};
+    c->stats.total_ms = elapsed(c->ev[0], c->ev[1]);
+    c->stats.steps = (uint64_t)steps;
+    c->stats.launches = c->launches;
+    *out = reinterpret_cast<kd_tape *>(t);
+    return KD_OK;
+}
+
+int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double *g_x0,
+                double *g_v0) {
+    if (!tape) return KD_EINVAL;
+    kd_tape_impl *t = reinterpret_cast<kd_tape_impl *>(tape);
+    kd_ctx *c = t->ctx;
+    if (!dL_dx || !g_x0 || !g_v0) return c->fail(KD_EINVAL, "NULL gradient buffer");
+    if (c->prm.precision != KD_PREC_MIXED)
+        return c->fail(KD_EINVAL, "the adjoint is implemented for KD_PREC_MIXED contexts");
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    int rc = adj_alloc(c, t->every);
+    if (rc) return rc;
+    const size_t n = c->n, b3 = 3 * n * sizeof(double);
+    KD_CHECK(c, cudaMemcpyAsync(c->lx, dL_dx, b3, cudaMemcpyHostToDevice, c->st));
+    if (dL_dv)
+        KD_CHECK(c, cudaMemcpyAsync(c->lv, dL_dv, b3, cudaMemcpyHostToDevice, c->st));
+    else
+        KD_CHECK(c, cudaMemsetAsync(c->lv, 0, b3, c->st));
+    AdjArgs a;
+    a.topo = c->topo;
+    a.recf = c->recf;
+    a.thi = c->thi;
+    a.tlo = c->tlo;
+    a.trel = c->trel;
+    a.tid = c->tid;
+    a.n = (uint32_t)n;
+    a.theta = c->prm.theta;
+    a.dt = t->dt;
+    a.bodies = c->bodies;
+    a.heavy = c->d_heavy;
+    a.n_heavy = c->n_heavy;
+    a.lx = c->lx;
+    a.lv = c->lv;
+    a.mu = c->amu;
+    a.y = c->ay;
+    a.ysink = c->ysink;
+    a.yheavy = c->yheavy;
+    a.U = c->aU;
+    a.G = c->aG;
+    a.err = c->dev_err;
+    c->launches = 0;
+    KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
+    const int64_t nseg = (t->steps + t->every - 1) / t->every;
+    double *pos[3] = {c->bodies.x, c->bodies.y, c->bodies.z};
+    for (int64_t seg = nseg - 1; seg >= 0 && !rc; --seg) {
+        const int64_t n0 = seg * t->every, n1 = std::min(t->steps, n0 + t->every);
+        rc = copy_state(c, t->ck[(size_t)seg], false);
+        if (rc) break;
+        // recompute the segment forward, keeping the positions at the start of every step
+        for (int64_t s = n0; s < n1; ++s) {
+            double *dst = c->segbuf + 3 * n * (size_t)(s - n0);
+            for (int k = 0; k < 3; ++k)
+                KD_CHECK(c, cudaMemcpyAsync(dst + k * n, pos[k], n * sizeof(double),
+                                            cudaMemcpyDeviceToDevice, c->st));
+            if (s + 1 < n1) enqueue_step(c, t->dt);
+        }
+        for (int64_t s = n1 - 1; s >= n0; --s) {
+            const double *src = c->segbuf + 3 * n * (size_t)(s - n0);
+            for (int k = 0; k < 3; ++k)
+                KD_CHECK(c, cudaMemcpyAsync(pos[k], src + k * n, n * sizeof(double),
+                                            cudaMemcpyDeviceToDevice, c->st));
+            enqueue_build(c, false, true);
+            c->launches += launch_adjoint_step(a, c->st);
+        }
+    }
+    if (!rc) rc = copy_state(c, t->final_state, false);
+    KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
+    KD_CHECK(c, cudaGetLastError());
+    if (rc) return rc;
+    KD_CHECK(c, cudaMemcpyAsync(g_x0, c->lx, b3, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaMemcpyAsync(g_v0, c->lv, b3, cudaMemcpyDeviceToHost, c->st));
+    rc = check_device(c);
+    if (rc) return rc;
+    c->has_tree = false;
+    c->stats = kd_stats{};
+    c->stats.total_ms = elapsed(c->ev[0], c->ev[1]);
+    c->stats.steps = (uint64_t)t->steps;
+    c->stats.launches = c->launches;
+    return KD_OK;
+}
+
+void kd_tape_free(kd_tape *tape) {
+    if (!tape) return;
+    kd_tape_impl *t = reinterpret_cast<kd_tape_impl *>(tape);
+    if (t->ctx) {
+        cudaSetDevice(t->ctx->prm.device);
+        cudaStreamSynchronize(t->ctx->st);
+    }
+    for (double *p : t->ck) cudaFree(p);
+    if (t->final_state) cudaFree(t->final_state);
+    delete t;
 }
 
 int kd_set_timing(kd_ctx *c, int32_t on) {

@@ -773,6 +773,29 @@ __device__ __forceinline__ double coord(const LocalSmem &S, uint32_t sd, uint32_
     return sd == 0 ? S.x[l] : (sd == 1 ? S.y[l] : S.z[l]);
 }
 
+// Mixed leaf record: origin o = position of the leaf's first body, as hi + lo floats; each
+// body's offset from o is written to trel.
+__device__ __forceinline__ NodeF leaf_nodef(const LocalSmem &S, uint32_t st, uint32_t cn,
+                                            uint32_t s0, const LocalOut &o) {
+    const uint32_t l0 = S.perm[st];
+    const double ox = S.x[l0], oy = S.y[l0], oz = S.z[l0];
+    for (uint32_t k = st; k < st + cn; ++k) {
+        const uint32_t l = S.perm[k];
+        const float fm = is_heavy(S.id[l], o.heavy, o.n_heavy) ? 0.0f : (float)S.m[l];
+        o.trel[s0 + k] = make_float4((float)(S.x[l] - ox), (float)(S.y[l] - oy),
+                                     (float)(S.z[l] - oz), fm);
+    }
+    NodeF r;
+    const float hx = (float)ox, hy = (float)oy, hz = (float)oz;
+    r.hi = make_float4(hx, hy, hz, 0.0f);
+    r.lo = make_float4((float)(ox - (double)hx), (float)(oy - (double)hy),
+                       (float)(oz - (double)hz), 0.0f);
+    r.a = s0 + st;
+    r.b = cn;
+    r.pad0 = r.pad1 = 0u;
+    return r;
+}
+
 // Sums of a leaf's bodies (tree positions [st, st+cn) of this block), full and light mass.
 __device__ __forceinline__ void leaf_sums(const LocalSmem &S, uint32_t st, uint32_t cn,
                                           const LocalOut &o, double f[4], double g[4]) {
@@ -1064,7 +1087,7 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
             }
             if (want_f) {
                 store_moments(o.mof, root, g);
-                o.recf[root] = make_nodef(g[0], g[1], g[2], g[3], 0.0, s0, c0);
+                o.recf[root] = leaf_nodef(S, 0, c0, s0, o);
             }
         }
     }
@@ -1086,7 +1109,7 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
                     }
                     if (want_f) {
                         store_moments(o.mof, cid, g);
-                        o.recf[cid] = make_nodef(g[0], g[1], g[2], g[3], 0.0, s0 + cst, ccn);
+                        o.recf[cid] = leaf_nodef(S, cst, ccn, s0, o);
                     }
                 } else {
                     if (want_d) load_moments(o.mo, cid, f);

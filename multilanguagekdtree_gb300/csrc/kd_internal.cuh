@@ -50,7 +50,9 @@ struct __align__(16) NodeD {
 static_assert(sizeof(NodeD) == 56 || sizeof(NodeD) == 64, "NodeD layout");
 
 // Walk record of the mixed path: centre of mass as hi+lo floats, size^2, light mass.  The
-// opening test reads only `hi` and `a, b`; an accepted node also reads `lo`.
+// opening test reads only `hi` and `a, b`; an accepted node also reads `lo`.  A leaf record
+// holds instead its origin o (the position of its first body) as hi+lo floats; the bodies of
+// a leaf are stored as FP32 offsets from o.
 struct __align__(16) NodeF {
     float4 hi;  // cm hi x,y,z ; size^2
     float4 lo;  // cm lo x,y,z ; light mass
@@ -129,6 +131,7 @@ struct LocalOut {
     dbl4 *tpos;                  // bodies in tree order (x, y, z, m)
     uint32_t *tid;               // body index of every tree position
     float4 *thi, *tlo;           // split coordinates, tree order (mixed records only)
+    float4 *trel;                // offset from the leaf origin, light mass (mixed only)
     Moments mo;                  // full-mass moments (FP64 records)
     Moments mof;                 // light-mass moments (mixed records)
     NodeD *recd;                 // FP64 walk records, or nullptr
@@ -196,6 +199,7 @@ void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, u
                       double theta, double *acc, uint32_t *err,
                       unsigned long long *counts, cudaStream_t st);
 void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
+                       const float4 *trel,
                        const uint32_t *tid, uint32_t n, double theta, const Bodies &b,
                        const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
                        unsigned long long *counts, cudaStream_t st);
@@ -209,5 +213,27 @@ void launch_direct(const Bodies &b, uint32_t n, const uint64_t *sinks, uint32_t 
                    double *partial, double *acc, cudaStream_t st);
 void launch_find_heavy(const Bodies &b, uint32_t n, double frac, double *scratch_total,
                        uint32_t *heavy_ids, uint32_t *n_heavy, uint32_t *err, cudaStream_t st);
+
+// ---------------------------------------------------------------- adjoint (kd_adjoint.cu)
+struct AdjArgs {
+    Topology topo;
+    const NodeF *recf;
+    const float4 *thi, *tlo, *trel;
+    const uint32_t *tid;
+    uint32_t n;
+    double theta, dt;
+    Bodies bodies;
+    const uint32_t *heavy;
+    int n_heavy;
+    double *lx, *lv;        // adjoints of x and v, original order, 3n
+    double *mu, *y;         // 3n scratch
+    double *ysink;          // 3n, tree order
+    double *yheavy;         // 3 * kMaxHeavy
+    float *U;               // 3n, tree order: pair-source sums
+    float *G;               // 3 * n_nodes: node-source sums
+    uint32_t *err;
+};
+// One backward step over the tree currently built (mixed records).  Returns kernels launched.
+int launch_adjoint_step(const AdjArgs &a, cudaStream_t st);
 
 }  // namespace kd

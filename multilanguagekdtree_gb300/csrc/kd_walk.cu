@@ -166,8 +166,9 @@ struct HeavyBody {
 template <bool kCount>
 __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
-    const float4 *__restrict__ tlo, const uint32_t *__restrict__ tid, uint32_t n, float theta2,
-    Bodies b, const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
+    const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
+    const uint32_t *__restrict__ tid, uint32_t n, float theta2, Bodies b,
+    const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
     uint32_t *err, unsigned long long *counts) {
     __shared__ HeavyBody heavy[kMaxHeavy];
     if (threadIdx.x < n_heavy) {
@@ -183,7 +184,10 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     const uint32_t bit = 1u << lane;
     const float4 mh = valid ? thi[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 ml = valid ? tlo[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // compensated body sum (s, c); multipole terms gather in the plain partial p, which is
+    // folded into the compensated sum at every leaf
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    float px = 0.f, py = 0.f, pz = 0.f;
     unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
     uint32_t st_node = 0, st_mask = 0;  // lane k holds stack entry k
     uint32_t node = 0;
@@ -195,18 +199,19 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
         bool descend = false;
         if (ab.y != 0u) {
             if (mask & bit) {
-                float px = 0.f, py = 0.f, pz = 0.f;
+                // sink position relative to the leaf origin, in split precision
+                const float4 ol = __ldg(&rec[node].lo);
+                const float qx = (mh.x - nh.x) + (ml.x - ol.x);
+                const float qy = (mh.y - nh.y) + (ml.y - ol.y);
+                const float qz = (mh.z - nh.z) + (ml.z - ol.z);
                 for (uint32_t k = 0; k < ab.y; ++k) {
                     const uint32_t j = ab.x + k;
                     if (j == s) continue;
-                    const float4 qh = __ldg(&thi[j]);
-                    const float4 ql = __ldg(&tlo[j]);
-                    const float dx = (mh.x - qh.x) + (ml.x - ql.x);
-                    const float dy = (mh.y - qh.y) + (ml.y - ql.y);
-                    const float dz = (mh.z - qh.z) + (ml.z - ql.z);
+                    const float4 r = __ldg(&trel[j]);
+                    const float dx = qx - r.x, dy = qy - r.y, dz = qz - r.z;
                     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     const float inv = rsqrtf(d2);
-                    const float f = -qh.w * (inv * inv * inv);
+                    const float f = -r.w * (inv * inv * inv);
                     px = fmaf(f, dx, px);
                     py = fmaf(f, dy, py);
                     pz = fmaf(f, dz, pz);
@@ -215,6 +220,7 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
                 kahan_add(sx, cx, px);
                 kahan_add(sy, cy, py);
                 kahan_add(sz, cz, pz);
+                px = py = pz = 0.f;
             }
         } else {
             bool take = false;
@@ -236,9 +242,9 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
                     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     const float inv = rsqrtf(d2);
                     const float f = -nl.w * (inv * inv * inv);
-                    kahan_add(sx, cx, f * dx);
-                    kahan_add(sy, cy, f * dy);
-                    kahan_add(sz, cz, f * dz);
+                    px = fmaf(f, dx, px);
+                    py = fmaf(f, dy, py);
+                    pz = fmaf(f, dz, pz);
                     if (kCount) ++c_m2p;
                 }
             }
@@ -264,6 +270,9 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
         node = __shfl_sync(kFull, st_node, sp);
         mask = __shfl_sync(kFull, st_mask, sp);
     }
+    kahan_add(sx, cx, px);
+    kahan_add(sy, cy, py);
+    kahan_add(sz, cz, pz);
     if (valid) {
         const uint32_t o = tid[s];
         double ax = (double)sx - (double)cx;
@@ -304,17 +313,18 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
 }
 
 void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
-                       const uint32_t *tid, uint32_t n, double theta, const Bodies &b,
+                       const float4 *trel, const uint32_t *tid, uint32_t n, double theta,
+                       const Bodies &b,
                        const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
                        unsigned long long *counts, cudaStream_t st) {
     const uint32_t threads = kWalkWarps * 32;
     const uint32_t blocks = (n + threads - 1) / threads;
     const float theta2 = (float)(theta * theta);
     if (counts)
-        k_walk_mixed<true><<<blocks, threads, 0, st>>>(rec, thi, tlo, tid, n, theta2, b,
+        k_walk_mixed<true><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n, theta2, b,
                                                        heavy_ids, n_heavy, acc, err, counts);
     else
-        k_walk_mixed<false><<<blocks, threads, 0, st>>>(rec, thi, tlo, tid, n, theta2, b,
+        k_walk_mixed<false><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n, theta2, b,
                                                         heavy_ids, n_heavy, acc, err, nullptr);
 }
 
