@@ -26,7 +26,7 @@ import numpy as np
 from . import _lib
 from ._lib import NODE_DTYPE, PARTICLE_DTYPE, KDError
 
-__all__ = ["KDTreeSim", "allocate_node_vec", "nodes_needed", "build_tree", "calc_accel",
+__all__ = ["KDTreeSim", "Tape", "allocate_node_vec", "nodes_needed", "build_tree", "calc_accel",
            "simple_sim", "KDError", "NODE_DTYPE", "LAYOUTS", "PRECISIONS"]
 
 LAYOUTS = {"dfs": _lib.KD_LAYOUT_DFS, "par4": _lib.KD_LAYOUT_PAR4}
@@ -145,6 +145,13 @@ class KDTreeSim:
     def set_precision(self, precision) -> None:
         self._check(self._lib.kd_set_precision(self._ctx, _precision(precision)))
 
+    def forward(self, dt: float, steps: int, ckpt_every: int = 32) -> "Tape":
+        """Run `steps` steps like simple_sim, keeping checkpoints for backward()."""
+        t = C.c_void_p()
+        self._check(self._lib.kd_forward(self._ctx, float(dt), int(steps), int(ckpt_every),
+                                         C.byref(t)))
+        return Tape(self, t)
+
     def set_timing(self, on: bool) -> None:
         self._check(self._lib.kd_set_timing(self._ctx, 1 if on else 0))
 
@@ -167,6 +174,44 @@ class KDTreeSim:
         s = _lib.KdStats()
         self._check(self._lib.kd_get_stats(self._ctx, C.byref(s)))
         return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+class Tape:
+    """Checkpoints of one forward sweep; backward() maps the gradient at the final state to
+    the gradient at the initial state (the autograd.Function contract: forward saves,
+    backward consumes grad-outputs and returns grad-inputs)."""
+
+    def __init__(self, sim: KDTreeSim, handle: C.c_void_p):
+        self._sim = sim
+        self._h = handle
+
+    def backward(self, dL_dx: np.ndarray, dL_dv: np.ndarray | None = None):
+        n = self._sim.n
+        gx = np.ascontiguousarray(dL_dx, dtype=np.float64).reshape(n, 3)
+        gv = None if dL_dv is None else np.ascontiguousarray(dL_dv, dtype=np.float64).reshape(n, 3)
+        ox = np.empty((n, 3))
+        ov = np.empty((n, 3))
+        self._sim._check(self._sim._lib.kd_backward(
+            self._h, _lib.ptr(gx), _lib.ptr(gv) if gv is not None else None, _lib.ptr(ox),
+            _lib.ptr(ov)))
+        return ox, ov
+
+    def close(self) -> None:
+        if self._h:
+            self._sim._lib.kd_tape_free(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def build_tree(bodies: np.ndarray, leaf_size: int = 7, layout="dfs", device: int = 0):

@@ -62,6 +62,9 @@ class Oracle:
                                          C.c_double, C.c_uint64, _vp]),
             "orc_direct_accel": (None, [_vp, C.c_size_t, _vp, C.c_size_t, _vp]),
             "orc_energy": (None, [_vp, C.c_size_t, _vp]),
+            "orc_adjoint_direct": (C.c_int, [_vp, C.c_size_t, C.c_double, C.c_int64, _vp, _vp,
+                                             _vp, _vp, _vp, _vp, _vp]),
+            "orc_tree_jt": (C.c_int, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_double, _vp, _vp]),
             "orc_omp_threads": (C.c_int, []),
             "orc_set_threads": (None, [C.c_int]),
         }
@@ -163,6 +166,37 @@ class Oracle:
         acc = np.zeros((len(s), 3))
         self.lib.orc_direct_accel(_p(b), len(b), _p(s), len(s), _p(acc))
         return acc
+
+    def adjoint_direct(self, bodies, dt: float, steps: int, target=None, dL_dx=None,
+                       dL_dv=None):
+        """FP64 direct-sum forward + exact reverse sweep.  With `target` (n,3) the loss is
+        (1/n) sum |x_T - target|^2.  Returns dict(g_x0, g_v0, xT, loss)."""
+        b = self._bodies(bodies)
+        n = len(b)
+        gx = np.zeros((n, 3))
+        gv = np.zeros((n, 3))
+        xT = np.zeros((n, 3))
+        loss = np.zeros(1)
+        tgt = None if target is None else np.ascontiguousarray(target, dtype=np.float64)
+        ldx = None if dL_dx is None else np.ascontiguousarray(dL_dx, dtype=np.float64)
+        ldv = None if dL_dv is None else np.ascontiguousarray(dL_dv, dtype=np.float64)
+        rc = self.lib.orc_adjoint_direct(_p(b), n, dt, steps, _p(ldx) if ldx is not None else None,
+                                         _p(ldv) if ldv is not None else None,
+                                         _p(tgt) if tgt is not None else None, _p(loss),
+                                         _p(gx), _p(gv), _p(xT))
+        if rc != 0:
+            raise RuntimeError("orc_adjoint_direct failed")
+        return {"g_x0": gx, "g_v0": gv, "xT": xT, "loss": float(loss[0])}
+
+    def tree_jt(self, bodies, nodes, mu, theta: float = 0.3) -> np.ndarray:
+        """y = J^T mu over the Barnes-Hut interaction set of the given tree (FP64)."""
+        b = self._bodies(bodies)
+        nodes = np.ascontiguousarray(nodes, dtype=NODE)
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        y = np.zeros((len(b), 3))
+        if self.lib.orc_tree_jt(_p(b), len(b), _p(nodes), len(nodes), theta, _p(mu), _p(y)):
+            raise RuntimeError("orc_tree_jt failed")
+        return y
 
     def energy(self, bodies):
         b = self._bodies(bodies)

@@ -456,6 +456,190 @@ void orc_energy(const orc_particle *P, size_t n, double out[2]) {
     out[1] = pe;
 }
 
+/* ---------------------------------------------------------------- direct-sum adjoint */
+
+/* Unit tidal product w = |d|^-3 (mu - 3 (d.mu) |d|^-2 d), d = xi - xj. */
+static inline void tidal_w(const double d[3], const double mu[3], double w[3]) {
+    double d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    double inv2 = 1.0 / d2;
+    double inv3 = inv2 / sqrt(d2);
+    double dm = d[0] * mu[0] + d[1] * mu[1] + d[2] * mu[2];
+    double c3 = 3.0 * dm * inv2;
+    for (int k = 0; k < 3; ++k) w[k] = inv3 * (mu[k] - c3 * d[k]);
+}
+
+/* Direct-sum accelerations of all n bodies from positions x (3n), FP64. */
+static void direct_all(const double *x, const double *m, size_t n, double *a) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (size_t i = 0; i < n; ++i) {
+        double ax = 0, ay = 0, az = 0;
+        for (size_t j = 0; j < n; ++j) {
+            if (j == i) continue;
+            double dx = x[3 * i] - x[3 * j], dy = x[3 * i + 1] - x[3 * j + 1],
+                   dz = x[3 * i + 2] - x[3 * j + 2];
+            double dp2 = dx * dx + dy * dy + dz * dz;
+            double dist = sqrt(dp2);
+            double magi = -m[j] / (dist * dist * dist);
+            ax += magi * dx; ay += magi * dy; az += magi * dz;
+        }
+        a[3 * i] = ax; a[3 * i + 1] = ay; a[3 * i + 2] = az;
+    }
+}
+
+/* FP64 direct-sum forward (semi-implicit Euler of array_kd_tree.rs:649-658 with all-pairs
+ * forces) for `steps` steps, then the exact reverse sweep:
+ *   mu = lv + dt lx;  lv = mu;  lx += dt J^T mu,
+ *   (J^T mu)_i = sum_{j != i} [ -m_j w(x_i - x_j, mu_i) + m_i w(x_j - x_i, mu_j) ].
+ * dL_dx / dL_dv: gradient at the final state (3n each; dL_dv may be NULL).  When
+ * `loss_target` is not NULL, dL_dx is ignored and the loss (1/n) sum |x_T - target|^2 is
+ * used instead; its value is stored in *loss.  Outputs the gradients at the initial state
+ * and the final positions x_T (3n). */
+int orc_adjoint_direct(const orc_particle *P, size_t n, double dt, int64_t steps,
+                       const double *dL_dx, const double *dL_dv, const double *loss_target,
+                       double *loss, double *g_x0, double *g_v0, double *xT) {
+    double *xs = (double *)malloc((size_t)(steps + 1) * 3 * n * sizeof(double));
+    double *v = (double *)malloc(3 * n * sizeof(double));
+    double *m = (double *)malloc(n * sizeof(double));
+    double *a = (double *)malloc(3 * n * sizeof(double));
+    double *lx = (double *)malloc(3 * n * sizeof(double));
+    double *lv = (double *)malloc(3 * n * sizeof(double));
+    double *mu = (double *)malloc(3 * n * sizeof(double));
+    double *y = (double *)malloc(3 * n * sizeof(double));
+    if (!xs || !v || !m || !a || !lx || !lv || !mu || !y) {
+        free(xs); free(v); free(m); free(a); free(lx); free(lv); free(mu); free(y);
+        return -2;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) { xs[3 * i + k] = P[i].p[k]; v[3 * i + k] = P[i].v[k]; }
+        m[i] = P[i].m;
+    }
+    for (int64_t s = 0; s < steps; ++s) {
+        double *x0 = xs + (size_t)s * 3 * n, *x1 = x0 + 3 * n;
+        direct_all(x0, m, n, a);
+        for (size_t k = 0; k < 3 * n; ++k) {
+            v[k] += dt * a[k];
+            x1[k] = x0[k] + dt * v[k];
+        }
+    }
+    double *xe = xs + (size_t)steps * 3 * n;
+    memcpy(xT, xe, 3 * n * sizeof(double));
+    if (loss_target) {
+        double L = 0.0;
+        for (size_t k = 0; k < 3 * n; ++k) {
+            double e = xe[k] - loss_target[k];
+            L += e * e;
+            lx[k] = 2.0 * e / (double)n;
+        }
+        *loss = L / (double)n;
+    } else {
+        memcpy(lx, dL_dx, 3 * n * sizeof(double));
+    }
+    if (dL_dv) memcpy(lv, dL_dv, 3 * n * sizeof(double));
+    else memset(lv, 0, 3 * n * sizeof(double));
+    for (int64_t s = steps - 1; s >= 0; --s) {
+        const double *x = xs + (size_t)s * 3 * n;
+        for (size_t k = 0; k < 3 * n; ++k) mu[k] = lv[k] + dt * lx[k];
+#pragma omp parallel for schedule(dynamic, 16)
+        for (size_t i = 0; i < n; ++i) {
+            double yi[3] = {0, 0, 0};
+            for (size_t j = 0; j < n; ++j) {
+                if (j == i) continue;
+                double d[3] = {x[3 * i] - x[3 * j], x[3 * i + 1] - x[3 * j + 1],
+                               x[3 * i + 2] - x[3 * j + 2]};
+                double w[3], e[3] = {-d[0], -d[1], -d[2]};
+                tidal_w(d, &mu[3 * i], w);
+                for (int k = 0; k < 3; ++k) yi[k] -= m[j] * w[k];
+                tidal_w(e, &mu[3 * j], w);
+                for (int k = 0; k < 3; ++k) yi[k] += m[i] * w[k];
+            }
+            for (int k = 0; k < 3; ++k) y[3 * i + k] = yi[k];
+        }
+        for (size_t k = 0; k < 3 * n; ++k) {
+            lx[k] += dt * y[k];
+            lv[k] = mu[k];
+        }
+    }
+    memcpy(g_x0, lx, 3 * n * sizeof(double));
+    memcpy(g_v0, lv, 3 * n * sizeof(double));
+    free(xs); free(v); free(m); free(a); free(lx); free(lv); free(mu); free(y);
+    return 0;
+}
+
+/* Transpose Jacobian product of one Barnes-Hut evaluation, y = J^T mu, over the interaction
+ * set of accel_recur (array_kd_tree.rs:585-617): for every sink i and interaction with a
+ * source of mass m at c, w = w(x_i - c, mu_i):  y_i -= m w;  a pair source j gets m_j w; a
+ * node K passes w down to each of its bodies l as m_l w. */
+static void jt_recur(size_t cur, size_t p, const orc_particle *P, const orc_node *nodes,
+                     double theta2, const double *mu, double *ys, double *y, double *Gn) {
+    const orc_node *n = &nodes[cur];
+    if (n->num_parts > 0) {
+        for (uint64_t k = 0; k < n->num_parts; ++k) {
+            size_t j = (size_t)n->particles[k];
+            if (j == p) continue;
+            double d[3] = {P[p].p[0] - P[j].p[0], P[p].p[1] - P[j].p[1], P[p].p[2] - P[j].p[2]};
+            double w[3];
+            tidal_w(d, &mu[3 * p], w);
+            for (int q = 0; q < 3; ++q) {
+                ys[q] -= P[j].m * w[q];
+#pragma omp atomic
+                y[3 * j + q] += P[j].m * w[q];
+            }
+        }
+        return;
+    }
+    double d[3] = {P[p].p[0] - n->cm[0], P[p].p[1] - n->cm[1], P[p].p[2] - n->cm[2]};
+    double d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (n->size * n->size < theta2 * d2) {
+        double w[3];
+        tidal_w(d, &mu[3 * p], w);
+        for (int q = 0; q < 3; ++q) {
+            ys[q] -= n->m * w[q];
+#pragma omp atomic
+            Gn[3 * cur + q] += w[q];
+        }
+    } else {
+        jt_recur(n->left, p, P, nodes, theta2, mu, ys, y, Gn);
+        jt_recur(n->right, p, P, nodes, theta2, mu, ys, y, Gn);
+    }
+}
+
+static void jt_down(size_t cur, const orc_particle *P, const orc_node *nodes, const double *Gn,
+                    double acc0, double acc1, double acc2, double *y) {
+    const orc_node *n = &nodes[cur];
+    if (n->num_parts > 0) {
+        for (uint64_t k = 0; k < n->num_parts; ++k) {
+            size_t l = (size_t)n->particles[k];
+            y[3 * l] += P[l].m * acc0;
+            y[3 * l + 1] += P[l].m * acc1;
+            y[3 * l + 2] += P[l].m * acc2;
+        }
+        return;
+    }
+    acc0 += Gn[3 * cur]; acc1 += Gn[3 * cur + 1]; acc2 += Gn[3 * cur + 2];
+    jt_down(n->left, P, nodes, Gn, acc0, acc1, acc2, y);
+    jt_down(n->right, P, nodes, Gn, acc0, acc1, acc2, y);
+}
+
+int orc_tree_jt(const orc_particle *P, size_t n, const orc_node *nodes, size_t n_nodes,
+                double theta, const double *mu, double *y) {
+    double *Gn = (double *)calloc(3 * n_nodes, sizeof(double));
+    if (!Gn) return -2;
+    memset(y, 0, 3 * n * sizeof(double));
+    double theta2 = theta * theta;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (size_t i = 0; i < n; ++i) {
+        double ys[3] = {0.0, 0.0, 0.0};
+        jt_recur(0, i, P, nodes, theta2, mu, ys, y, Gn);
+        for (int q = 0; q < 3; ++q) {
+#pragma omp atomic
+            y[3 * i + q] += ys[q];
+        }
+    }
+    jt_down(0, P, nodes, Gn, 0.0, 0.0, 0.0, y);
+    free(Gn);
+    return 0;
+}
+
 int orc_omp_threads(void) { return max_threads(); }
 
 void orc_set_threads(int n) {
