@@ -112,8 +112,8 @@ size_t kd_nodes_needed(size_t n, int32_t leaf_size, int32_t layout);
 kd_ctx *kd_create(size_t n, const kd_params *params);
 void kd_destroy(kd_ctx *ctx);
 
-/* Last error message of ctx (or of the calling thread's last failed kd_create when ctx is
- * NULL).  Never NULL. */
+/* Last error message of ctx (or of the calling thread's last failed kd_create or
+ * kd_direct_accel_noalloc when ctx is NULL).  Never NULL. */
 const char *kd_last_error(const kd_ctx *ctx);
 
 /* Copy n bodies host -> device (Vec<Particle> handed to simple_sim/build_tree).  Checks
@@ -173,6 +173,26 @@ int kd_forward(kd_ctx *ctx, double dt, int64_t steps, int64_t ckpt_every, kd_tap
 int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double *g_x0,
                 double *g_v0);
 void kd_tape_free(kd_tape *tape);
+
+/* kd_direct_accel without a context and without allocating device memory, for callers that
+ * cannot allocate: a host whose device memory is fully committed to its own simulation
+ * state, or one that measures accuracy inside its step loop, where the device-wide
+ * synchronisation of cudaMalloc/cudaFree would stall its other streams.  No counterpart in
+ * the reference.  All pointers are device pointers of the current device: positions x, y,
+ * z and masses m of n bodies (FP64, n < 2^31), ns sink indices, and acc (3*ns doubles,
+ * acc[3k+d] for sinks[k]); an out-of-range sink index yields NaN.  Work is queued on
+ * `stream` (a cudaStream_t; NULL = default stream) and not waited for.
+ * Limit: ns <= 43690 -- the partial sums live in one 1 MiB __device__ array of the library
+ * (131072 doubles, 3 per sink and source chunk; sources are chunked to fit), which every GPU
+ * that loads the library holds until exit; larger ns returns KD_EINVAL and
+ * kd_last_error(NULL) says why.  The first call on a device looks up that array's address
+ * (cudaGetSymbolAddress) with the device current; make that first call before any stream
+ * capture.  Every call overwrites all the partials it reads, so no clearing is needed, but
+ * all calls share the one array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. */
+int kd_direct_accel_noalloc(const double *x, const double *y, const double *z,
+                            const double *m, size_t n, const uint64_t *sinks, size_t ns,
+                            double *acc, void *stream);
 
 /* Interaction counts of the last walk, summed over bodies: out[0] = pair (P2P)
  * interactions, out[1] = opening tests at internal nodes, out[2] = accepted multipole

@@ -86,6 +86,9 @@ SIGNATURES = {
                              C.POINTER(C.c_void_p)]),
     "kd_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "kd_tape_free": (None, [C.c_void_p]),
+    "kd_direct_accel_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
+                                          C.c_void_p]),
     "kd_set_counting": (C.c_int, [C.c_void_p, C.c_int32]),
     "kd_get_counts": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
 }

@@ -463,6 +463,10 @@ void enqueue_step(kd_ctx *c, double dt) {
     c->launches += 1;
 }
 
+namespace kd {
+void set_thread_error(const char *msg) { g_create_error = msg ? msg : ""; }
+}  // namespace kd
+
 // ====================================================================== C ABI
 
 extern "C" {
