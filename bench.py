@@ -58,9 +58,14 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--err-samples", type=int, default=4096)
     ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--adjoint-steps", type=int, default=4)
+    ap.add_argument("--build-n", type=int, default=10_000_000,
+                    help="bodies of the build-only measurement (circular_orbits, leaf 8, PAR4)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="only the headline timing (used for profiling captures)")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="only one forward + reverse sweep of --adjoint-steps steps (profiling)")
     return ap.parse_args()
 
 
@@ -188,6 +193,30 @@ def run_reference(a, ws, rank):
 
 # ------------------------------------------------------------------ GPU arm
 
+def adjoint_timing(kd, bodies, a, dev):
+    """Forward sweep with checkpoints (every 32 steps) and the reverse sweep of the loss
+    mean |x_T - R_z(1 rad) x_0|^2, timed by the library's events."""
+    n = len(bodies)
+    adj = kd.KDTreeSim(n, leaf_size=a.leaf, layout="dfs", precision="mixed", theta=a.theta,
+                       dt=a.dt, device=dev)
+    adj.set_bodies(bodies)
+    adj.simple_sim(a.dt, 1)
+    adj.set_bodies(bodies)
+    with adj.forward(a.dt, a.adjoint_steps, 32) as tape:
+        fwd_ms = adj.stats()["total_ms"]
+        xT = adj.get_bodies()["p"]
+        tgt = bodies["p"] @ np.array([[np.cos(1.0), -np.sin(1.0), 0.0],
+                                      [np.sin(1.0), np.cos(1.0), 0.0], [0.0, 0.0, 1.0]]).T
+        tape.backward(2.0 * (xT - tgt) / n)
+        bwd_ms = adj.stats()["total_ms"]
+    adj.close()
+    return {"steps": a.adjoint_steps, "forward_ms_per_step": fwd_ms / a.adjoint_steps,
+            "backward_ms_per_step": bwd_ms / a.adjoint_steps,
+            "adjoint_over_forward": bwd_ms / fwd_ms,
+            "note": "backward = recompute of the checkpoint segment + rebuild + "
+                    "transpose-Jacobian walk per step; loss = mean |x_T - R_z(1) x_0|^2"}
+
+
 def pinned_bodies(n):
     import torch
     from multilanguagekdtree_gb300 import PARTICLE_DTYPE
@@ -203,6 +232,12 @@ def run_ours(a, ws, rank, local):
     torch.cuda.set_device(dev)
     bodies = kd.ring(a.n, seed=a.seed + rank)
     n = a.n
+
+    if a.adjoint_only:
+        line = {"metric": METRIC, "config": {"workload": f"adjoint ring N={n}"},
+                "adjoint": adjoint_timing(kd, bodies, a, dev)}
+        print(json.dumps(line))
+        return
 
     # ---- headline: mixed precision, bodies resident
     sim = kd.KDTreeSim(n, leaf_size=a.leaf, layout="dfs", precision="mixed", theta=a.theta,
@@ -322,6 +357,22 @@ def run_ours(a, ws, rank, local):
     line["mixed_over_fp64"] = value / ws / fp64_rate
     f64.close()
 
+    # ---- adjoint: forward sweep with checkpoints, then the reverse sweep, same bodies
+    line["adjoint"] = adjoint_timing(kd, bodies, a, dev)
+
+    # ---- build only: the reference's bench_build_tree input (circular_orbits, leaf 8, PAR4)
+    cb = kd.circular_orbits(a.build_n - 1, seed=a.seed)
+    bo = kd.KDTreeSim(len(cb), leaf_size=8, layout="par4", precision="fp64", device=dev)
+    bo.set_bodies(cb)
+    bo.build_tree()
+    times = []
+    for _ in range(3):
+        bo.build_tree()
+        times.append(bo.stats()["build_ms"])
+    bo.close()
+    line["build_only"] = {"n_bodies": len(cb), "input": "circular_orbits, leaf 8, PAR4 numbering",
+                          "gpu_ms": min(times), "note": "tree + FP64 moments + walk records"}
+
     # ---- end to end through the C ABI with host buffers
     keep, host = pinned_bodies(n)
     host[:] = bodies
@@ -346,6 +397,12 @@ def run_ours(a, ws, rank, local):
 
     # ---- CPU baseline (oracle port of the reference algorithm)
     if not a.no_cpu_baseline:
+        from oracle import Oracle
+        orc = Oracle()
+        t0 = time.perf_counter()
+        orc.build_tree_par4(cb, leaf=8)
+        line["build_only"]["cpu_ms"] = 1e3 * (time.perf_counter() - t0)
+        line["build_only"]["cpu_threads"] = orc.threads()
         rate, threads, t = cpu_step_rate(bodies, a.cpu_steps, a.leaf, a.theta, a.dt)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{a.cpu_steps} full FP64 step(s) of the {n}-body "

@@ -54,26 +54,43 @@ __device__ __forceinline__ double ord_val(unsigned long long k) {
     return __longlong_as_double((long long)b);
 }
 
-__device__ __forceinline__ const double *pick(const double *x, const double *y,
-                                              const double *z, uint32_t d) {
-    return d == 0 ? x : (d == 1 ? y : z);
-}
-
 // Split dimension and size from a bounding box, as array_kd_tree.rs:532-557: the box starts
-// at +-1e100, the extent is max - min, the first strictly larger extent wins.
+// at +-1e100, the extent is max - min in FP64, the first strictly larger extent wins.  The
+// comparison is decided on FP32 estimates of the extents whenever their error bounds
+// separate them, so FP64 instructions run only for `size` and for near ties.
 __device__ __forceinline__ void choose_split(const double mn_in[3], const double mx_in[3],
                                              uint32_t &sd, double &size) {
     double mn[3], mx[3];
+    float ef[3], er[3];
+    bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        mn[d] = fmin(1e100, mn_in[d]);
-        mx[d] = fmax(-1e100, mx_in[d]);
+        // clamps at +-1e100 on order-preserving keys (integer operations)
+        mn[d] = ord_val(min(ord_key(mn_in[d]), ord_key(1e100)));
+        mx[d] = ord_val(max(ord_key(mx_in[d]), ord_key(-1e100)));
+        const float a = trunc_float(mx[d]), b = trunc_float(mn[d]);
+        ef[d] = a - b;
+        er[d] = 2.4e-7f * (fabsf(a) + fabsf(b)) + 1.2e-7f * fabsf(ef[d]);
+        ok = ok && isfinite(ef[d]) && isfinite(er[d]);
     }
     sd = 0;
 #pragma unroll
-    for (int d = 1; d < 3; ++d)
-        if (__dsub_rn(mx[d], mn[d]) > __dsub_rn(mx[sd], mn[sd])) sd = (uint32_t)d;
+    for (int d = 1; d < 3; ++d) {
+        bool gt;
+        if (ok && ef[d] - er[d] > ef[sd] + er[sd])
+            gt = true;
+        else if (ok && ef[d] + er[d] < ef[sd] - er[sd])
+            gt = false;
+        else
+            gt = __dsub_rn(mx[d], mn[d]) > __dsub_rn(mx[sd], mn[sd]);
+        if (gt) sd = (uint32_t)d;
+    }
     size = __dsub_rn(mx[sd], mn[sd]);
+}
+
+__device__ __forceinline__ const double *pick(const double *x, const double *y,
+                                              const double *z, uint32_t d) {
+    return d == 0 ? x : (d == 1 ? y : z);
 }
 
 // In-place bitonic sort of `total` (key, val) pairs made of independent power-of-two
@@ -396,10 +413,11 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
         }
     };
 
-    for (int iter = 0; c > (uint32_t)kSelCap; ++iter) {
+    // sort directly only small candidate sets; larger ones take one radix/bin pass first
+    for (int iter = 0; c > (uint32_t)kSortDirect; ++iter) {
         if (iter >= kSelMaxIters) {
             if (threadIdx.x == 0) atomicOr(s.err, kErrSelect);
-            c = kSelCap;
+            c = min(c, (uint32_t)kSelCap);
             if (r >= c) r = c - 1;
             break;
         }

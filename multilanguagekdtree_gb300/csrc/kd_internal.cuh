@@ -24,7 +24,8 @@ constexpr int kTile = 2048;         // elements per block in the multi-block lev
 constexpr int kTileThreads = 256;
 constexpr int kHistBits = 12;       // radix digit of the median select
 constexpr int kHistBins = 1 << kHistBits;
-constexpr int kSelCap = 2048;       // candidates sorted in shared memory by one block
+constexpr int kSelCap = 2048;       // capacity of the select's shared-memory sort
+constexpr int kSortDirect = 256;    // candidate sets this small are sorted without a pass
 constexpr int kSelThreads = 512;
 constexpr uint32_t kMultiMin = 32768;  // segments above this use multi-block histograms
 constexpr int kSelMaxIters = 16;    // radix refinement passes before giving up (error)
@@ -146,14 +147,16 @@ __device__ __forceinline__ bool is_heavy(uint32_t id, const uint32_t *heavy_ids,
     return h;
 }
 
-// FP64 record: cm /= m and size*size in the reference's IEEE order
-// (array_kd_tree.rs:548-550, :606).
+// FP64 record: cm = S * (1/m) (the reference divides, array_kd_tree.rs:548-550; its sums
+// already differ from ours in order, so one more rounding stays within the moment bound),
+// size*size in the reference's IEEE order (:606).
 __device__ __forceinline__ NodeD make_noded(double m, double sx, double sy, double sz,
                                             double size, uint32_t a, uint32_t b) {
     NodeD q;
-    q.cmx = __ddiv_rn(sx, m);
-    q.cmy = __ddiv_rn(sy, m);
-    q.cmz = __ddiv_rn(sz, m);
+    const double inv = __ddiv_rn(1.0, m);
+    q.cmx = __dmul_rn(sx, inv);
+    q.cmy = __dmul_rn(sy, inv);
+    q.cmz = __dmul_rn(sz, inv);
     q.m = m;
     q.size2 = __dmul_rn(size, size);
     q.a = a;

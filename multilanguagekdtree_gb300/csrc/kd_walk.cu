@@ -163,6 +163,75 @@ struct HeavyBody {
     double x, y, z, m;
 };
 
+// Interactions of the lanes in `mask` with one child node of an opened node: the pair sums
+// of a leaf (folded into the compensated sum), or the opening test and, where accepted, the
+// multipole term (into the partial p).  Returns the lanes that open the node.
+template <bool kCount>
+__device__ __forceinline__ uint32_t visit_mixed(
+    const NodeF *__restrict__ rec, const float4 *__restrict__ trel, uint32_t node,
+    const float4 &nh, const uint2 &ab, uint32_t mask, uint32_t bit, uint32_t s,
+    const float4 &mh, const float4 &ml, float theta2, float &px, float &py, float &pz,
+    float &sx, float &sy, float &sz, float &cx, float &cy, float &cz,
+    unsigned long long &c_p2p, unsigned long long &c_open, unsigned long long &c_m2p,
+    unsigned long long &c_vis) {
+    const bool act = (mask & bit) != 0;
+    if (kCount) c_vis += act ? 1 : 0;
+    if (ab.y != 0u) {
+        if (act) {
+            // sink position relative to the leaf origin, in split precision
+            const float4 ol = __ldg(&rec[node].lo);
+            const float qx = (mh.x - nh.x) + (ml.x - ol.x);
+            const float qy = (mh.y - nh.y) + (ml.y - ol.y);
+            const float qz = (mh.z - nh.z) + (ml.z - ol.z);
+            for (uint32_t k = 0; k < ab.y; ++k) {
+                const uint32_t j = ab.x + k;
+                if (j == s) continue;
+                const float4 r = __ldg(&trel[j]);
+                const float dx = qx - r.x, dy = qy - r.y, dz = qz - r.z;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const float inv = rsqrtf(d2);
+                const float f = -r.w * (inv * inv * inv);
+                px = fmaf(f, dx, px);
+                py = fmaf(f, dy, py);
+                pz = fmaf(f, dz, pz);
+                if (kCount) ++c_p2p;
+            }
+            kahan_add(sx, cx, px);
+            kahan_add(sy, cy, py);
+            kahan_add(sz, cz, pz);
+            px = py = pz = 0.f;
+        }
+        return 0u;
+    }
+    // opening test on the high parts: an approximate decision suffices here
+    const float ex = mh.x - nh.x, ey = mh.y - nh.y, ez = mh.z - nh.z;
+    const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+    const bool take = act && nh.w < theta2 * e2;
+    if (kCount) c_open += act ? 1 : 0;
+    const uint32_t tk = __ballot_sync(kFull, take);
+    if (tk) {
+        const float4 nl = __ldg(&rec[node].lo);
+        if (take) {
+            // force on the split coordinates
+            const float dx = ex + (ml.x - nl.x);
+            const float dy = ey + (ml.y - nl.y);
+            const float dz = ez + (ml.z - nl.z);
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float inv = rsqrtf(d2);
+            const float f = -nl.w * (inv * inv * inv);
+            px = fmaf(f, dx, px);
+            py = fmaf(f, dy, py);
+            pz = fmaf(f, dz, pz);
+            if (kCount) ++c_m2p;
+        }
+    }
+    return mask & ~tk;
+}
+
+// The traversal handles both children of an opened node per iteration: their two records
+// are loaded together and tested together, and the stack keeps (node, right child, lanes)
+// of opened nodes whose children are still to be visited.  Every lane's decisions are the
+// same as in a one-node-at-a-time walk; only the order of the terms differs.
 template <bool kCount>
 __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
@@ -189,86 +258,58 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     float px = 0.f, py = 0.f, pz = 0.f;
     unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
-    uint32_t st_node = 0, st_mask = 0;  // lane k holds stack entry k
-    uint32_t node = 0;
+    // lane k holds stack entry k: an opened node (its right child) and the lanes that opened it
+    uint32_t st_node = 0, st_right = 0, st_mask = 0;
     int sp = 0;
-    while (true) {
-        const float4 nh = __ldg(&rec[node].hi);
-        const uint2 ab = __ldg(reinterpret_cast<const uint2 *>(&rec[node].a));
-        if (kCount) c_vis += (mask & bit) ? 1 : 0;
-        bool descend = false;
-        if (ab.y != 0u) {
-            if (mask & bit) {
-                // sink position relative to the leaf origin, in split precision
-                const float4 ol = __ldg(&rec[node].lo);
-                const float qx = (mh.x - nh.x) + (ml.x - ol.x);
-                const float qy = (mh.y - nh.y) + (ml.y - ol.y);
-                const float qz = (mh.z - nh.z) + (ml.z - ol.z);
-                for (uint32_t k = 0; k < ab.y; ++k) {
-                    const uint32_t j = ab.x + k;
-                    if (j == s) continue;
-                    const float4 r = __ldg(&trel[j]);
-                    const float dx = qx - r.x, dy = qy - r.y, dz = qz - r.z;
-                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float inv = rsqrtf(d2);
-                    const float f = -r.w * (inv * inv * inv);
-                    px = fmaf(f, dx, px);
-                    py = fmaf(f, dy, py);
-                    pz = fmaf(f, dz, pz);
-                    if (kCount) ++c_p2p;
-                }
-                kahan_add(sx, cx, px);
-                kahan_add(sy, cy, py);
-                kahan_add(sz, cz, pz);
-                px = py = pz = 0.f;
-            }
-        } else {
-            bool take = false;
-            if (mask & bit) {
-                // opening test on the high parts: an approximate decision suffices here
-                const float ex = mh.x - nh.x, ey = mh.y - nh.y, ez = mh.z - nh.z;
-                const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-                if (kCount) ++c_open;
-                take = nh.w < theta2 * e2;
-            }
-            const uint32_t tk = __ballot_sync(kFull, take);
-            if (tk) {
-                const float4 nl = __ldg(&rec[node].lo);
-                if (take) {
-                    // force on the split coordinates
-                    const float dx = (mh.x - nh.x) + (ml.x - nl.x);
-                    const float dy = (mh.y - nh.y) + (ml.y - nl.y);
-                    const float dz = (mh.z - nh.z) + (ml.z - nl.z);
-                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float inv = rsqrtf(d2);
-                    const float f = -nl.w * (inv * inv * inv);
-                    px = fmaf(f, dx, px);
-                    py = fmaf(f, dy, py);
-                    pz = fmaf(f, dz, pz);
-                    if (kCount) ++c_m2p;
-                }
-            }
-            const uint32_t open = mask & ~tk;
-            if (open) {
+    // the root alone
+    uint32_t cur, cur_right;
+    {
+        const float4 nh = __ldg(&rec[0].hi);
+        const uint2 ab = __ldg(reinterpret_cast<const uint2 *>(&rec[0].a));
+        mask = visit_mixed<kCount>(rec, trel, 0u, nh, ab, mask, bit, s, mh, ml, theta2, px, py,
+                                   pz, sx, sy, sz, cx, cy, cz, c_p2p, c_open, c_m2p, c_vis);
+        cur = 0u;
+        cur_right = ab.x;
+    }
+    while (mask) {
+        const uint32_t L = cur + 1, R = cur_right;
+        const float4 hL = __ldg(&rec[L].hi);
+        const uint2 aL = __ldg(reinterpret_cast<const uint2 *>(&rec[L].a));
+        const float4 hR = __ldg(&rec[R].hi);
+        const uint2 aR = __ldg(reinterpret_cast<const uint2 *>(&rec[R].a));
+        const uint32_t oL = visit_mixed<kCount>(rec, trel, L, hL, aL, mask, bit, s, mh, ml,
+                                                theta2, px, py, pz, sx, sy, sz, cx, cy, cz,
+                                                c_p2p, c_open, c_m2p, c_vis);
+        const uint32_t oR = visit_mixed<kCount>(rec, trel, R, hR, aR, mask, bit, s, mh, ml,
+                                                theta2, px, py, pz, sx, sy, sz, cx, cy, cz,
+                                                c_p2p, c_open, c_m2p, c_vis);
+        if (oL) {
+            if (oR) {
                 if (sp >= kStackMax) {
                     if (lane == 0) atomicOr(err, kErrStack);
                     break;
                 }
                 if (lane == sp) {
-                    st_node = ab.x;
-                    st_mask = open;
+                    st_node = R;
+                    st_right = aR.x;
+                    st_mask = oR;
                 }
                 ++sp;
-                node = node + 1;
-                mask = open;
-                descend = true;
             }
+            cur = L;
+            cur_right = aL.x;
+            mask = oL;
+        } else if (oR) {
+            cur = R;
+            cur_right = aR.x;
+            mask = oR;
+        } else {
+            if (sp == 0) break;
+            --sp;
+            cur = __shfl_sync(kFull, st_node, sp);
+            cur_right = __shfl_sync(kFull, st_right, sp);
+            mask = __shfl_sync(kFull, st_mask, sp);
         }
-        if (descend) continue;
-        if (sp == 0) break;
-        --sp;
-        node = __shfl_sync(kFull, st_node, sp);
-        mask = __shfl_sync(kFull, st_mask, sp);
     }
     kahan_add(sx, cx, px);
     kahan_add(sy, cy, py);
@@ -279,11 +320,11 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
         double ay = (double)sy - (double)cy;
         double az = (double)sz - (double)cz;
         // heavy bodies in FP64, pair kernel of array_particle.rs:67-76
-        const double px = b.x[o], py = b.y[o], pz = b.z[o];
+        const double px64 = b.x[o], py64 = b.y[o], pz64 = b.z[o];
         for (int h = 0; h < n_heavy; ++h) {
             if (heavy_ids[h] == o) continue;
             const HeavyBody q = heavy[h];
-            const double dx = px - q.x, dy = py - q.y, dz = pz - q.z;
+            const double dx = px64 - q.x, dy = py64 - q.y, dz = pz64 - q.z;
             const double dp2 = dx * dx + dy * dy + dz * dz;
             const double dist = sqrt(dp2);
             const double magi = -q.m / (dist * dist * dist);
