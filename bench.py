@@ -295,9 +295,13 @@ def run_ours(a, ws, rank, local):
     line["phases_ms_per_step"] = {k: ph[k] / 2 for k in ("build_ms", "moments_ms", "walk_ms",
                                                          "kick_ms")}
     line["interactions_per_body"] = {k: v / n for k, v in cnt.items()}
+    # DRAM bytes per launch: ncu capture of the 1M-body walk (117.0 MB read + 18.4 MB
+    # written, profiles/k_walk_mixed_ring1M.md) scaled by the number of bodies
+    walk_traffic = 135.4 * n
     line["roofline"] = {
         "kernel": "k_walk_mixed", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-        "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+        "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": walk_traffic,
+        "traffic_unit": "bytes per launch (ncu, 1M ring, scaled by N)",
         "note": "walk flops = 18 P2P + 10 opening tests + 9 M2P per body (counted on the "
                 "device); peak = 152 SMs x 128 FP32 lanes x 2 x sampled SM clock (nominal "
                 "rate; no measured FP32 figure exists)"}
