@@ -91,13 +91,21 @@ def barrier(ws):
 
 
 def max_over_ranks(ws, v: float) -> float:
+    """The slowest replica's time: every rank gets the maximum."""
     if ws == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(ws: int, bodies_per_rank: int, steps: int, t_max_s: float) -> float:
+    """Whole-job body-steps/s of N independent replicas (weak scaling): every rank advances
+    its own bodies, the job's time is the slowest rank's."""
+    return ws * bodies_per_rank * steps / t_max_s
 
 
 # ------------------------------------------------------------------ clocks
@@ -258,7 +266,7 @@ def run_ours(a, ws, rank, local):
     dev_s = st["total_ms"] / 1e3
     launches = int(st["launches"])
     t_max = max_over_ranks(ws, dev_s)
-    value = ws * n * a.steps / t_max
+    value = replica_value(ws, n, a.steps, t_max)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps, "higher_is_better": True,
