@@ -112,8 +112,8 @@ size_t kd_nodes_needed(size_t n, int32_t leaf_size, int32_t layout);
 kd_ctx *kd_create(size_t n, const kd_params *params);
 void kd_destroy(kd_ctx *ctx);
 
-/* Last error message of ctx (or of the calling thread's last failed kd_create or
- * kd_direct_accel_noalloc when ctx is NULL).  Never NULL. */
+/* Last error message of ctx (or of the calling thread's last failed kd_create,
+ * kd_quickstat_index or kd_direct_accel_noalloc when ctx is NULL).  Never NULL. */
 const char *kd_last_error(const kd_ctx *ctx);
 
 /* Copy n bodies host -> device (Vec<Particle> handed to simple_sim/build_tree).  Checks
@@ -132,6 +132,25 @@ int kd_build_tree(kd_ctx *ctx, size_t *last_node);
  * cap must be >= the node count (kd_nodes_needed for PAR4, last_node+1 for DFS);
  * *count receives the number of records written. */
 int kd_get_nodes(kd_ctx *ctx, kd_node_c *out, size_t cap, size_t *count);
+
+/* quickstat_index (Parallel/RustVersion/src/quickstat.rs:9-34) on the GPU, no context:
+ * reorders the index vector idx[0..n) (host, values < n_vals, into vals[0..n_vals), host)
+ * so that vals[idx[i]] < vals[idx[goal]] for i < goal and vals[idx[i]] >= vals[idx[goal]]
+ * for i >= goal -- the post-condition of quickstat.rs:211-216.  Equal values are ordered by
+ * index value (the reference's order among equal values depends on its random pivots).
+ * Non-finite values and out-of-range indices are rejected (KD_ENUMERIC).  *gpu_ms (may be
+ * NULL) receives the device time of the selection and partition, transfers excluded.
+ * Allocates and frees its own device memory; kd_last_error(NULL) reports failures. */
+int kd_quickstat_index(const double *vals, size_t n_vals, uint64_t *idx, size_t n, size_t goal,
+                       int32_t device, double *gpu_ms);
+
+/* print_tree (array_kd_tree.rs:666-692) of the last kd_build_tree, written to `path` (the
+ * reference writes tree{step}.txt): the node-vector length on the first line, then in slot
+ * order "L num_parts" followed by one "x y z" line per body, or
+ * "I split_dim split_val left right"; numbers as Rust's `{}` prints them (shortest
+ * round-trip digits, no exponent).  The length is allocate_node_vec(n) for PAR4 and the
+ * grown sequential Vec for DFS, whose unused slots print as "L 0". */
+int kd_print_tree(kd_ctx *ctx, const char *path);
 
 /* calc_accel (array_kd_tree.rs:619-621) for every body at once, over the tree of the last
  * kd_build_tree: acc[3*i+d] = d-th component of the acceleration of body i. */

@@ -77,6 +77,9 @@ SIGNATURES = {
     "kd_build_tree": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
     "kd_get_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "kd_calc_accel": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "kd_print_tree": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "kd_quickstat_index": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_size_t,
+                                     C.c_int32, C.POINTER(C.c_double)]),
     "kd_simple_sim": (C.c_int, [C.c_void_p, C.c_double, C.c_int64]),
     "kd_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
     "kd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(KdStats)]),

@@ -132,6 +132,14 @@ class KDTreeSim:
         self._check(self._lib.kd_get_nodes(self._ctx, _lib.ptr(out), cap, C.byref(cnt)))
         return out[: cnt.value]
 
+    def print_tree(self, step: int | None = None, path: str | None = None) -> str:
+        """print_tree (array_kd_tree.rs:666-692): write the last built tree to `path`, or to
+        tree{step}.txt as the reference names it.  Returns the path."""
+        if path is None:
+            path = f"tree{0 if step is None else int(step)}.txt"
+        self._check(self._lib.kd_print_tree(self._ctx, str(path).encode()))
+        return str(path)
+
     # ------------------------------------------------------------- forces and steps
     def calc_accel(self, out: np.ndarray | None = None) -> np.ndarray:
         if out is None:

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <charconv>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -353,6 +354,8 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
         lv.G = (uint32_t)p.glevels[l].size();
         lv.tiles = (p.gmax[l] + kTile - 1) / kTile;
         lv.multi = p.gmax[l] > kMultiMin;
+        lv.rank = kMedianRank;
+        lv.med_pos = nullptr;
         const uint32_t G_next = l + 1 < p.glevels.size() ? (uint32_t)p.glevels[l + 1].size() : 0u;
         c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, (int)l, G_next,
                                     c->st);
@@ -466,6 +469,36 @@ void enqueue_step(kd_ctx *c, double dt) {
 namespace kd {
 void set_thread_error(const char *msg) { g_create_error = msg ? msg : ""; }
 }  // namespace kd
+
+// Rust's `{}` for f64: the shortest digits that round-trip, written positionally (never in
+// exponent form); "NaN", "inf", "-inf", "-0".
+std::string rust_f64(double v) {
+    if (std::isnan(v)) return "NaN";
+    if (std::isinf(v)) return v < 0 ? "-inf" : "inf";
+    char buf[64];
+    auto r = std::to_chars(buf, buf + sizeof buf, v, std::chars_format::scientific);
+    std::string sci(buf, r.ptr);  // [-]d[.ddd]e(+|-)xx
+    std::string out;
+    size_t i = 0;
+    if (sci[0] == '-') {
+        out = "-";
+        i = 1;
+    }
+    const size_t epos = sci.find('e');
+    std::string digits;
+    for (size_t k = i; k < epos; ++k)
+        if (sci[k] != '.') digits += sci[k];
+    const int e = std::stoi(sci.substr(epos + 1));  // value = d.ddd * 10^e
+    const int nd = (int)digits.size();
+    if (e >= nd - 1) {
+        out += digits + std::string((size_t)(e - (nd - 1)), '0');
+    } else if (e >= 0) {
+        out += digits.substr(0, (size_t)e + 1) + "." + digits.substr((size_t)e + 1);
+    } else {
+        out += "0." + std::string((size_t)(-e - 1), '0') + digits;
+    }
+    return out;
+}
 
 // ====================================================================== C ABI
 
@@ -679,6 +712,156 @@ int kd_get_nodes(kd_ctx *c, kd_node_c *out, size_t cap, size_t *count) {
         }
     }
     if (count) *count = need;
+    return KD_OK;
+}
+
+int kd_quickstat_index(const double *vals, size_t n_vals, uint64_t *idx, size_t n, size_t goal,
+                       int32_t device, double *gpu_ms) {
+    if (!vals || !idx || n < 1 || n >= (1ull << 31) || goal >= n || n_vals < 1) {
+        g_create_error = "kd_quickstat_index: need vals, idx, 1 <= n < 2^31 and goal < n";
+        return KD_EINVAL;
+    }
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        g_create_error = cudaGetErrorString(e);
+        return KD_ECUDA;
+    }
+    const uint32_t nn = (uint32_t)n;
+    const uint32_t tiles = (nn + kTile - 1) / kTile;
+    std::vector<void *> mem;
+    auto get = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (e == cudaSuccess) e = cudaMalloc(&p, bytes ? bytes : 1);
+        if (e == cudaSuccess) mem.push_back(p);
+        return p;
+    };
+    double *d_vals = (double *)get(n_vals * sizeof(double));
+    uint64_t *d_idx = (uint64_t *)get(n * sizeof(uint64_t));
+    Work w{};
+    Scratch sc{};
+    for (int k = 0; k < 2; ++k) {
+        w.x[k] = w.y[k] = w.z[k] = (double *)get(n * sizeof(double));
+        w.id[k] = (uint32_t *)get(n * sizeof(uint32_t));
+        sc.ckey[k] = (unsigned long long *)get(n * sizeof(unsigned long long));
+        sc.cpos[k] = (uint32_t *)get(n * sizeof(uint32_t));
+        sc.bmin[k] = (unsigned long long *)get(3 * sizeof(unsigned long long));
+        sc.bmax[k] = (unsigned long long *)get(3 * sizeof(unsigned long long));
+    }
+    sc.sel = (SegSel *)get(sizeof(SegSel));
+    sc.hist = (uint32_t *)get(kHistBins * sizeof(uint32_t));
+    sc.cand_cnt = (uint32_t *)get(sizeof(uint32_t));
+    sc.tile_cnt = (uint32_t *)get(tiles * sizeof(uint32_t));
+    sc.tile_off = (uint32_t *)get(tiles * sizeof(uint32_t));
+    sc.err = (uint32_t *)get(sizeof(uint32_t));
+    uint32_t *d_seg = (uint32_t *)get(3 * sizeof(uint32_t));  // start, count, node id
+    uint32_t *d_med = (uint32_t *)get(sizeof(uint32_t));
+    NodeOut no;
+    no.split_dim = (uint8_t *)get(8);
+    no.split_val = (double *)get(8);
+    no.size = (double *)get(8);
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    const uint32_t seg_h[3] = {0u, nn, 0u};
+    uint32_t err_h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_vals, vals, n_vals * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_idx, idx, n * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_seg, seg_h, sizeof seg_h, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sc.err, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) {
+        // one segment [0, n): its start / count live where a tree's node arrays would
+        Topology t{};
+        t.n = nn;
+        t.n_nodes = 1;
+        t.start = d_seg;
+        t.count = d_seg + 1;
+        LevelArgs lv;
+        lv.ids = d_seg + 2;
+        lv.G = 1;
+        lv.tiles = tiles;
+        lv.multi = nn > kMultiMin;
+        lv.rank = (uint32_t)goal;
+        lv.med_pos = d_med;
+        cudaEventRecord(ev[0], st);
+        launch_gather_keys(d_vals, n_vals, d_idx, nn, w.x[0], w.id[0], sc.err, st);
+        launch_level(t, lv, no, w, 0, sc, 0, 0, st);
+        launch_place_selected(w.id[1], d_med, (uint32_t)goal, st);
+        cudaEventRecord(ev[1], st);
+        e = cudaGetLastError();
+    }
+    std::vector<uint32_t> out(n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), w.id[1], n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err_h, sc.err, sizeof err_h, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    float ms = 0.f;
+    if (e == cudaSuccess && gpu_ms) {
+        cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        *gpu_ms = ms;
+    }
+    for (auto &x : ev)
+        if (x) cudaEventDestroy(x);
+    if (st) cudaStreamDestroy(st);
+    for (void *p : mem) cudaFree(p);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("kd_quickstat_index: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? KD_ENOMEM : KD_ECUDA;
+    }
+    if (err_h & kErrNumeric) {
+        g_create_error = "kd_quickstat_index: an index is out of range or a value is not finite";
+        return KD_ENUMERIC;
+    }
+    if (err_h) {
+        g_create_error = "kd_quickstat_index: select failed to converge";
+        return KD_EDEVICE;
+    }
+    for (size_t i = 0; i < n; ++i) idx[i] = out[i];
+    return KD_OK;
+}
+
+int kd_print_tree(kd_ctx *c, const char *path) {
+    if (!c) return KD_EINVAL;
+    if (!path) return c->fail(KD_EINVAL, "path is NULL");
+    const Plan &p = c->plan;
+    const bool par4 = c->prm.layout == KD_LAYOUT_PAR4;
+    const size_t slots = par4 ? (size_t)p.par4_slots : (size_t)p.n_nodes;
+    std::vector<kd_node_c> nodes(slots);
+    size_t count = 0;
+    int rc = kd_get_nodes(c, nodes.data(), slots, &count);
+    if (rc) return rc;
+    std::vector<kd_particle_c> b(c->n);
+    rc = kd_get_bodies(c, b.data(), c->n);
+    if (rc) return rc;
+    // the Vec the reference prints: allocate_node_vec(n) slots (grown on demand for DFS)
+    const size_t len = par4 ? count
+                            : std::max(count, (size_t)needed_seq(c->n, (uint32_t)c->prm.leaf_size));
+    FILE *f = fopen(path, "w");
+    if (!f) return c->fail(KD_EINVAL, "cannot open %s", path);
+    std::string out = std::to_string(len) + "\n";
+    for (size_t i = 0; i < len; ++i) {
+        if (i >= count) {
+            out += "L 0\n";
+        } else if (nodes[i].num_parts > 0 || (nodes[i].left == 0 && nodes[i].right == 0)) {
+            out += "L " + std::to_string(nodes[i].num_parts) + "\n";
+            for (uint64_t k = 0; k < nodes[i].num_parts; ++k) {
+                const kd_particle_c &q = b[nodes[i].particles[k]];
+                out += rust_f64(q.p[0]) + " " + rust_f64(q.p[1]) + " " + rust_f64(q.p[2]) + "\n";
+            }
+        } else {
+            out += "I " + std::to_string(nodes[i].split_dim) + " " + rust_f64(nodes[i].split_val) +
+                   " " + std::to_string(nodes[i].left) + " " + std::to_string(nodes[i].right) +
+                   "\n";
+        }
+        if (out.size() > (1u << 20)) {
+            fputs(out.c_str(), f);
+            out.clear();
+        }
+    }
+    fputs(out.c_str(), f);
+    const bool bad = ferror(f) != 0;
+    fclose(f);
+    if (bad) return c->fail(KD_EINVAL, "write to %s failed", path);
     return KD_OK;
 }
 

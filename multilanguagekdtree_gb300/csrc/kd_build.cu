@@ -140,6 +140,39 @@ void launch_init_work(const Bodies &b, Work &w, uint32_t n, cudaStream_t st) {
     k_init_work<<<blocks, 256, 0, st>>>(b, w.x[0], w.y[0], w.z[0], w.id[0], n);
 }
 
+__global__ void k_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx,
+                              uint32_t n, double *key, uint32_t *id, uint32_t *err) {
+    bool bad = false;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const uint64_t j = idx[i];
+        const bool ok = j < n_vals && j <= 0xffffffffull;
+        key[i] = ok ? vals[j] : 0.0;
+        id[i] = (uint32_t)j;
+        bad |= !ok || !isfinite(ok ? vals[j] : 0.0);
+    }
+    if (bad) atomicOr(err, kErrNumeric);
+}
+
+void launch_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx, uint32_t n,
+                        double *key, uint32_t *id, uint32_t *err, cudaStream_t st) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_gather_keys<<<blocks, 256, 0, st>>>(vals, n_vals, idx, n, key, id, err);
+}
+
+// The partition leaves the selected element somewhere in [goal, n); swap it to goal.
+__global__ void k_place_selected(uint32_t *id, const uint32_t *med_pos, uint32_t goal) {
+    const uint32_t p = *med_pos;
+    const uint32_t t = id[goal];
+    id[goal] = id[p];
+    id[p] = t;
+}
+
+void launch_place_selected(uint32_t *id, const uint32_t *med_pos, uint32_t goal, cudaStream_t st) {
+    k_place_selected<<<1, 1, 0, st>>>(id, med_pos, goal);
+}
+
 // ------------------------------------------------------------------ level passes
 
 struct TileRef {
@@ -256,7 +289,7 @@ __global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin
     s.scale = (range > 0.0f && isfinite(scale)) ? scale : 0.0f;
     s.digit = 0;
     s.c = cnt;
-    s.r = cnt / 2;
+    s.r = split_rank(lv, cnt);
     s.pad = 0;
     s.kmed = 0;
     s.idmed = 0;
@@ -582,7 +615,7 @@ __global__ __launch_bounds__(256) void k_tile_scan(Topology t, LevelArgs lv,
         if (threadIdx.x == blockDim.x - 1) carry += wpre + inc;
         __syncthreads();
     }
-    if (threadIdx.x == 0 && carry != cnt / 2) atomicOr(err, kErrSelect);
+    if (threadIdx.x == 0 && carry != split_rank(lv, cnt)) atomicOr(err, kErrSelect);
 }
 
 // Stable partition: bodies keep their relative order inside each child.  With `nbmin`
@@ -598,7 +631,7 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
     unsigned long long cmn[2][3] = {{~0ull, ~0ull, ~0ull}, {~0ull, ~0ull, ~0ull}};
     unsigned long long cmx[2][3] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
     const SegSel s = sel[r.seg];
-    const uint32_t mid = r.cnt / 2;
+    const uint32_t mid = split_rank(lv, r.cnt);
     const uint32_t lbase = tile_off[(size_t)r.seg * lv.tiles + r.tile];
     const uint32_t rbase = r.lo - lbase;
     __shared__ uint32_t wl[kTileThreads / 32], wr[kTileThreads / 32];
@@ -637,6 +670,7 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
             dy[dst] = vy;
             dz[dst] = vz;
             did[dst] = id;
+            if (lv.med_pos && id == s.idmed && key == s.kmed) *lv.med_pos = dst;
         }
         if (nbmin && in) {
             if (isL) {

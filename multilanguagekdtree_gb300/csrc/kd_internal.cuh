@@ -97,7 +97,14 @@ struct LevelArgs {
     uint32_t G;              // number of segments
     uint32_t tiles;          // tiles per segment
     bool multi;              // multi-block select
+    uint32_t rank;           // rank to select; kMedianRank = len/2 of every segment
+    uint32_t *med_pos;       // if set: receives where the selected element was written
 };
+constexpr uint32_t kMedianRank = 0xffffffffu;
+
+__host__ __device__ __forceinline__ uint32_t split_rank(const LevelArgs &lv, uint32_t cnt) {
+    return lv.rank == kMedianRank ? cnt / 2 : lv.rank;
+}
 
 struct Work {              // ping-pong buffers of the level passes (segment order)
     double *x[2], *y[2], *z[2];
@@ -182,6 +189,11 @@ __device__ __forceinline__ NodeF make_nodef(double m, double sx, double sy, doub
 }
 
 void launch_init_work(const Bodies &b, Work &w, uint32_t n, cudaStream_t st);
+// quickselect set-up: key[i] = vals[idx[i]], id[i] = idx[i]; flags an index >= n_vals
+void launch_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx, uint32_t n,
+                        double *key, uint32_t *id, uint32_t *err, cudaStream_t st);
+// puts the selected element at position `goal` (it was written at *med_pos)
+void launch_place_selected(uint32_t *id, const uint32_t *med_pos, uint32_t goal, cudaStream_t st);
 // One multi-block level.  `lvl` selects the bounding-box buffers (lvl & 1); the boxes of
 // level 0 are computed here, deeper levels receive theirs from the previous level's scatter
 // (`G_next` > 0 when the next level is a multi-block level too).  Returns the number of
