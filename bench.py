@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=4)
     ap.add_argument("--build-n", type=int, default=10_000_000,
                     help="bodies of the build-only measurement (circular_orbits, leaf 8, PAR4)")
+    ap.add_argument("--select-n", type=int, default=100_000_000,
+                    help="values of the selection measurement (bench_quickstat: 1e8 uniform)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="only the headline timing (used for profiling captures)")
@@ -385,6 +387,20 @@ def run_ours(a, ws, rank, local):
     line["build_only"] = {"n_bodies": len(cb), "input": "circular_orbits, leaf 8, PAR4 numbering",
                           "gpu_ms": min(times), "note": "tree + FP64 moments + walk records"}
 
+    # ---- selection only: the reference's bench_quickstat input (1e8 uniform doubles)
+    rng = np.random.default_rng(a.seed)
+    sv = rng.random(a.select_n)
+    goal = int(rng.integers(0, a.select_n))
+    kd.quickstat_index(sv[:1000], 10)  # load / warm the path
+    t0 = time.perf_counter()
+    sidx, sel_ms = kd.quickstat_index(sv, goal, timing=True)
+    sel_e2e = time.perf_counter() - t0
+    line["select_only"] = {"n": a.select_n, "input": "uniform [0,1) doubles, random goal",
+                           "gpu_ms": sel_ms, "e2e_ms": 1e3 * sel_e2e,
+                           "note": "device time of select + partition; e2e adds the host "
+                                   "transfers of values and indices"}
+    del sidx
+
     # ---- end to end through the C ABI with host buffers
     keep, host = pinned_bodies(n)
     host[:] = bodies
@@ -415,6 +431,10 @@ def run_ours(a, ws, rank, local):
         orc.build_tree_par4(cb, leaf=8)
         line["build_only"]["cpu_ms"] = 1e3 * (time.perf_counter() - t0)
         line["build_only"]["cpu_threads"] = orc.threads()
+        t0 = time.perf_counter()
+        orc.quickstat_index(sv, goal)
+        line["select_only"]["cpu_ms"] = 1e3 * (time.perf_counter() - t0)
+        line["select_only"]["cpu_kind"] = "oracle quickstat_index (sequential, as quickstat.rs)"
         rate, threads, t = cpu_step_rate(bodies, a.cpu_steps, a.leaf, a.theta, a.dt)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{a.cpu_steps} full FP64 step(s) of the {n}-body "

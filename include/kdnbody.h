@@ -119,6 +119,17 @@ const char *kd_last_error(const kd_ctx *ctx);
 /* Copy n bodies host -> device (Vec<Particle> handed to simple_sim/build_tree).  Checks
  * that every p, v, m is finite and m >= 0. */
 int kd_set_bodies(kd_ctx *ctx, const kd_particle_c *bodies, size_t n);
+/* Generate n bodies on the device, straight into the context (no host arrays): the
+ * initial conditions of array_particle.rs without the host-to-device copy.  KD_GEN_RING: body
+ * 0 of mass 1 at rest at the origin, bodies 1..n-1 of mass 1e-14 with r ~ U[0.8, 1.2],
+ * phi ~ U[0, 2 pi), z ~ Normal(0, 1e-4), circular speed sqrt(1/r).  KD_GEN_PLUMMER: Plummer
+ * sphere (G = M = a = 1, equal masses, radii below 20, speeds from the distribution
+ * function), centre of mass at rest at the origin.  KD_GEN_CIRCULAR: circular_orbits(n-1) of
+ * array_particle.rs:19-44.  Each body draws from its own counter-based stream, so the result
+ * depends on (n, seed) only. */
+enum { KD_GEN_RING = 0, KD_GEN_PLUMMER = 1, KD_GEN_CIRCULAR = 2 };
+int kd_generate(kd_ctx *ctx, int32_t kind, uint64_t seed);
+
 /* Copy the bodies device -> host (the &mut Vec<Particle> after simple_sim returns). */
 int kd_get_bodies(kd_ctx *ctx, kd_particle_c *bodies, size_t n);
 

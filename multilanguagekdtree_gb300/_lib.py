@@ -26,6 +26,9 @@ KD_LAYOUT_DFS = 0
 KD_LAYOUT_PAR4 = 1
 KD_PREC_FP64 = 0
 KD_PREC_MIXED = 1
+KD_GEN_RING = 0
+KD_GEN_PLUMMER = 1
+KD_GEN_CIRCULAR = 2
 
 ERROR_NAMES = {
     KD_EINVAL: "KD_EINVAL", KD_ENOMEM: "KD_ENOMEM", KD_ECUDA: "KD_ECUDA",
@@ -74,6 +77,7 @@ SIGNATURES = {
     "kd_last_error": (C.c_char_p, [C.c_void_p]),
     "kd_set_bodies": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "kd_get_bodies": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kd_generate": (C.c_int, [C.c_void_p, C.c_int32, C.c_uint64]),
     "kd_build_tree": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
     "kd_get_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "kd_calc_accel": (C.c_int, [C.c_void_p, C.c_void_p]),

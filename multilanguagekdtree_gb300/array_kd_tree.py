@@ -108,6 +108,13 @@ class KDTreeSim:
         b = np.ascontiguousarray(bodies, dtype=PARTICLE_DTYPE)
         self._check(self._lib.kd_set_bodies(self._ctx, _lib.ptr(b), b.shape[0]))
 
+    def generate(self, kind: str = "ring", seed: int = 0) -> None:
+        """Generate the bodies on the device: "ring", "plummer" or "circular"
+        (circular_orbits(n-1))."""
+        kinds = {"ring": _lib.KD_GEN_RING, "plummer": _lib.KD_GEN_PLUMMER,
+                 "circular": _lib.KD_GEN_CIRCULAR}
+        self._check(self._lib.kd_generate(self._ctx, kinds[kind], int(seed)))
+
     def get_bodies(self, out: np.ndarray | None = None) -> np.ndarray:
         if out is None:
             out = np.empty(self.n, dtype=PARTICLE_DTYPE)

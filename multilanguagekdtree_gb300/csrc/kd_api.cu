@@ -172,6 +172,7 @@ struct kd_ctx {
     unsigned long long *d_counts = nullptr;
     uint32_t *d_heavy = nullptr, *d_nheavy = nullptr;
     double *d_total = nullptr;
+    double *gen_scratch = nullptr;
     int n_heavy = 0;
     std::vector<uint32_t> heavy;
     int final_buf = 0;
@@ -317,6 +318,7 @@ int setup(kd_ctx *c) {
     KD_CHECK(c, c->alloc(&c->d_heavy, kMaxHeavy));
     KD_CHECK(c, c->alloc(&c->d_nheavy, 1));
     KD_CHECK(c, c->alloc(&c->d_total, 1));
+    KD_CHECK(c, c->alloc(&c->gen_scratch, 6 * 256));
     KD_CHECK(c, cudaMemset(c->dev_err, 0, sizeof(uint32_t)));
     KD_CHECK(c, cudaMemset(c->nout.split_dim, 0, nn));
     KD_CHECK(c, cudaMemset(c->nout.split_val, 0, nn * sizeof(double)));
@@ -409,6 +411,45 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
     return ms;
+}
+
+}  // namespace
+
+namespace {
+
+// After new bodies landed in the master arrays: check the device error word (non-finite
+// input), list the heavy bodies (m >= heavy_frac * total mass).
+int accept_bodies(kd_ctx *c) {
+    const size_t n = c->n;
+    launch_find_heavy(c->bodies, (uint32_t)n, c->prm.heavy_frac > 0 ? c->prm.heavy_frac : 2.0,
+                      c->d_total, c->d_heavy, c->d_nheavy, c->dev_err, c->st);
+    uint32_t nh = 0;
+    uint32_t ids[kMaxHeavy];
+    KD_CHECK(c, cudaMemcpyAsync(&nh, c->d_nheavy, sizeof nh, cudaMemcpyDeviceToHost, c->st));
+    KD_CHECK(c, cudaMemcpyAsync(ids, c->d_heavy, sizeof ids, cudaMemcpyDeviceToHost, c->st));
+    int rc = check_device(c);
+    c->has_tree = false;
+    if (rc) {
+        c->has_bodies = false;
+        return rc;
+    }
+    c->heavy.assign(ids, ids + std::min<uint32_t>(nh, kMaxHeavy));
+    std::sort(c->heavy.begin(), c->heavy.end());
+    c->n_heavy = (int)c->heavy.size();
+    if (nh > (uint32_t)kMaxHeavy) {
+        c->n_heavy = 0;
+        c->heavy.clear();
+        if (c->prm.precision == KD_PREC_MIXED) {
+            c->has_bodies = false;
+            return c->fail(KD_EINVAL, "%u bodies exceed heavy_frac of the total mass; at most %d",
+                           nh, kMaxHeavy);
+        }
+    }
+    if (c->n_heavy)
+        KD_CHECK(c, cudaMemcpyAsync(c->d_heavy, c->heavy.data(), c->n_heavy * sizeof(uint32_t),
+                                    cudaMemcpyHostToDevice, c->st));
+    c->has_bodies = true;
+    return KD_OK;
 }
 
 }  // namespace
@@ -598,35 +639,17 @@ int kd_set_bodies(kd_ctx *c, const kd_particle_c *bodies, size_t n) {
     KD_CHECK(c, cudaMemcpyAsync(c->aos, bodies, n * sizeof(kd_particle_c),
                                 cudaMemcpyHostToDevice, c->st));
     launch_aos_to_soa(c->aos, c->bodies, (uint32_t)n, c->dev_err, c->st);
-    launch_find_heavy(c->bodies, (uint32_t)n, c->prm.heavy_frac > 0 ? c->prm.heavy_frac : 2.0,
-                      c->d_total, c->d_heavy, c->d_nheavy, c->dev_err, c->st);
-    uint32_t nh = 0;
-    uint32_t ids[kMaxHeavy];
-    KD_CHECK(c, cudaMemcpyAsync(&nh, c->d_nheavy, sizeof nh, cudaMemcpyDeviceToHost, c->st));
-    KD_CHECK(c, cudaMemcpyAsync(ids, c->d_heavy, sizeof ids, cudaMemcpyDeviceToHost, c->st));
-    int rc = check_device(c);
-    c->has_tree = false;
-    if (rc) {
-        c->has_bodies = false;
-        return rc;
-    }
-    c->heavy.assign(ids, ids + std::min<uint32_t>(nh, kMaxHeavy));
-    std::sort(c->heavy.begin(), c->heavy.end());
-    c->n_heavy = (int)c->heavy.size();
-    if (nh > (uint32_t)kMaxHeavy) {
-        c->n_heavy = 0;
-        c->heavy.clear();
-        if (c->prm.precision == KD_PREC_MIXED) {
-            c->has_bodies = false;
-            return c->fail(KD_EINVAL, "%u bodies exceed heavy_frac of the total mass; at most %d",
-                           nh, kMaxHeavy);
-        }
-    }
-    if (c->n_heavy)
-        KD_CHECK(c, cudaMemcpyAsync(c->d_heavy, c->heavy.data(), c->n_heavy * sizeof(uint32_t),
-                                    cudaMemcpyHostToDevice, c->st));
-    c->has_bodies = true;
-    return KD_OK;
+    return accept_bodies(c);
+}
+
+int kd_generate(kd_ctx *c, int32_t kind, uint64_t seed) {
+    if (!c) return KD_EINVAL;
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    KD_CHECK(c, cudaMemsetAsync(c->dev_err, 0, sizeof(uint32_t), c->st));
+    if (launch_generate(kind, c->bodies, (uint32_t)c->n, seed, c->gen_scratch, c->st) < 0)
+        return c->fail(KD_EINVAL, "unknown generator %d", kind);
+    KD_CHECK(c, cudaGetLastError());
+    return accept_bodies(c);
 }
 
 int kd_get_bodies(kd_ctx *c, kd_particle_c *bodies, size_t n) {

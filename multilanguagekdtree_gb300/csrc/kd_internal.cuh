@@ -229,6 +229,12 @@ void launch_direct(const Bodies &b, uint32_t n, const uint64_t *sinks, uint32_t 
 void launch_find_heavy(const Bodies &b, uint32_t n, double frac, double *scratch_total,
                        uint32_t *heavy_ids, uint32_t *n_heavy, uint32_t *err, cudaStream_t st);
 
+// ---------------------------------------------------------------- generators (kd_generate.cu)
+// kind 0 ring, 1 Plummer, 2 circular_orbits; `scratch` holds 6*256 doubles.  Returns the
+// number of kernels launched, or -1 for an unknown kind.
+int launch_generate(int kind, Bodies &b, uint32_t n, uint64_t seed, double *scratch,
+                    cudaStream_t st);
+
 // ---------------------------------------------------------------- adjoint (kd_adjoint.cu)
 struct AdjArgs {
     Topology topo;
