@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="only the headline timing (used for profiling captures)")
+    ap.add_argument("--workload", default="ring", choices=["ring", "plummer", "adjoint-check"],
+                    help="ring: the headline line; plummer: the 2e7-body Plummer stress case; "
+                         "adjoint-check: the 1e5-body, 1000-step gradient check")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="only one forward + reverse sweep of --adjoint-steps steps (profiling)")
     return ap.parse_args()
@@ -330,6 +333,15 @@ def run_ours(a, ws, rank, local):
         "frac": build_bytes / build_s / 1e9 / hbm, "traffic": None,
         "peak_source": "MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
 
+    # ---- energy drift over the timed run length
+    sim.set_bodies(bodies)
+    e0 = sim.energy()
+    sim.simple_sim(a.dt, a.steps)
+    e1 = sim.energy()
+    line["energy"] = {"steps": a.steps, "start": e0, "end": e1,
+                      "relative_drift": (sum(e1) - sum(e0)) / abs(sum(e0)),
+                      "potential": "mixed tree walk (theta as above), FP64 central-mass term"}
+
     # ---- accuracy of the mixed walk against the FP64 direct sum
     rng = np.random.default_rng(12345)
     sinks = np.sort(rng.choice(np.arange(1, n), a.err_samples, replace=False))
@@ -442,11 +454,143 @@ def run_ours(a, ws, rank, local):
     print(json.dumps(line))
 
 
+def rel_rows(x, y):
+    return np.linalg.norm(x - y, axis=1) / np.linalg.norm(y, axis=1)
+
+
+def run_plummer(a, dev):
+    """Clustered stress case: Plummer sphere (G = M = a = 1, equal masses, radii <= 20),
+    theta 0.5, leaf 7, dt 1e-4, 20 mixed-precision steps, then a reverse sweep over the same
+    20 steps; error of the mixed walk against the FP64 direct sum on 4,096 bodies."""
+    import torch
+
+    import multilanguagekdtree_gb300 as kd
+    n = a.n if a.n != 10_000_000 else 20_000_000
+    theta, dt, steps = 0.5, 1e-4, 20
+    s = kd.KDTreeSim(n, leaf_size=a.leaf, precision="mixed", theta=theta, dt=dt, device=dev)
+    s.generate("plummer", a.seed)
+    e0 = s.energy()
+    s.simple_sim(dt, 1)
+    s.generate("plummer", a.seed)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    torch.cuda.synchronize()
+    s.simple_sim(dt, steps)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    fwd = s.stats()
+    e1 = s.energy()
+    line = {"workload": f"plummer N={n} theta={theta} leaf={a.leaf} dt={dt} mixed",
+            "steps": steps, "value": n * steps / (fwd["total_ms"] / 1e3), "unit": UNIT,
+            "ms_per_step": fwd["total_ms"] / steps,
+            "energy": {"start": e0, "end": e1,
+                       "relative_drift": (sum(e1) - sum(e0)) / abs(sum(e0))},
+            "gpu_launches": int(fwd["launches"]), "clocks": clk}
+    s.set_timing(True)
+    s.simple_sim(dt, 2)
+    ph = s.stats()
+    s.set_timing(False)
+    line["phases_ms_per_step"] = {k: ph[k] / 2 for k in ("build_ms", "walk_ms", "kick_ms")}
+    s.build_tree()
+    s.set_counting(True)
+    s.calc_accel()
+    cnt = s.counts()
+    s.set_counting(False)
+    flops = 18 * cnt["p2p"] + 10 * cnt["opened"] + 9 * cnt["m2p"]
+    peak = 152 * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
+    walk_s = ph["walk_ms"] / 2 / 1e3
+    line["interactions_per_body"] = {k: v / n for k, v in cnt.items()}
+    line["roofline_walk"] = {"bound": "fp32", "achieved": flops / walk_s / 1e12, "peak": peak,
+                             "unit": "TFLOP/s", "frac": flops / walk_s / 1e12 / peak}
+    try:
+        hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", 6800.0)
+    except (OSError, ValueError):
+        hbm = 6800.0
+    levels = max(1, int(np.ceil(np.log2(n / 1024.0))))
+    bb = n * (40 * levels + 32) / (ph["build_ms"] / 2 / 1e3) / 1e9
+    line["roofline_build"] = {"bound": "hbm", "achieved": bb, "peak": hbm, "unit": "GB/s",
+                              "frac": bb / hbm}
+    rng = np.random.default_rng(12345)
+    sinks = np.sort(rng.choice(n, a.err_samples, replace=False))
+    acc = s.calc_accel()
+    ref = s.direct_accel(sinks)
+    e = rel_rows(acc[sinks], ref)
+    line["accuracy"] = {"samples": int(a.err_samples), "reference": "FP64 direct sum",
+                        "mixed_max_rel": float(e.max()),
+                        "mixed_rms_rel": float(np.sqrt(np.mean(e ** 2))),
+                        "mixed_median_rel": float(np.median(e))}
+    s.generate("plummer", a.seed)
+    with s.forward(dt, steps, 32) as tape:
+        f_ms = s.stats()["total_ms"]
+        xT = s.get_bodies()["p"]
+        tape.backward(np.zeros_like(xT), np.ones_like(xT) / n)
+        b_ms = s.stats()["total_ms"]
+    line["adjoint"] = {"steps": steps, "forward_ms": f_ms, "backward_ms": b_ms,
+                       "adjoint_over_forward": b_ms / f_ms,
+                       "loss": "sum of final velocities / n (dL/dv_T = 1/n)"}
+    s.close()
+    print(json.dumps(line))
+
+
+def run_adjoint_check(a, dev):
+    """Gradient check: 100,000-body ring, theta 0.3, dt 1e-3, 1,000 steps, checkpoints every
+    32 steps, loss = mean |x_T - R_z(1 rad) x_0|^2.  dL/dv0 from the reverse sweep against
+    central differences (h = 1e-6) of the forward on 64 seeded coordinates."""
+    import multilanguagekdtree_gb300 as kd
+    n = a.n if a.n != 10_000_000 else 100_000
+    steps, dt, h = 1000, 1e-3, 1e-6
+    R = np.array([[np.cos(1.0), -np.sin(1.0), 0.0], [np.sin(1.0), np.cos(1.0), 0.0],
+                  [0.0, 0.0, 1.0]])
+
+    def grad(bodies):
+        m = len(bodies)
+        tgt = bodies["p"] @ R.T
+        with kd.KDTreeSim(m, leaf_size=a.leaf, precision="mixed", theta=a.theta,
+                          device=dev) as s:
+            s.set_bodies(bodies)
+            with s.forward(dt, steps, 32) as tape:
+                fms = s.stats()["total_ms"]
+                xT = s.get_bodies()["p"]
+                gx, gv = tape.backward(2.0 * (xT - tgt) / m)
+                bms = s.stats()["total_ms"]
+        return gx, gv, fms, bms, tgt
+
+    b = kd.ring(n, seed=a.seed)
+    gx, gv, fms, bms, tgt = grad(b)
+    rng = np.random.default_rng(77)
+    coords = list(zip(rng.choice(np.arange(1, n), 64, replace=False).tolist(),
+                      rng.integers(0, 2, 64).tolist()))
+    errs = []
+    with kd.KDTreeSim(n, leaf_size=a.leaf, precision="mixed", theta=a.theta, device=dev) as s:
+        def final(bb):
+            s.set_bodies(bb)
+            s.simple_sim(dt, steps)
+            return s.get_bodies()["p"].copy()
+        for i, d in coords:
+            bp = b.copy(); bp["v"][i, d] += h
+            bm = b.copy(); bm["v"][i, d] -= h
+            lp = np.sum((final(bp) - tgt) ** 2, axis=1)
+            lm = np.sum((final(bm) - tgt) ** 2, axis=1)
+            fd = np.sum(lp - lm) / n / (2 * h)
+            errs.append(abs(fd - gv[i, d]) / abs(gv[i, d]))
+    line = {"workload": f"adjoint-check ring N={n} theta={a.theta} dt={dt} steps={steps} ckpt=32",
+            "forward_ms": fms, "backward_ms": bms, "adjoint_over_forward": bms / fms,
+            "fd": {"coords": 64, "h": h, "max_rel_err": float(max(errs)),
+                   "median_rel_err": float(np.median(errs))},
+            "cpu_direct_adjoint": "2,000-body, 1,000-step comparison with the FP64 direct-sum "
+                                  "adjoint: tests/test_gpu_adjoint.py"}
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     ws, rank, local = dist_setup()
     if a.impl == "reference":
         run_reference(a, ws, rank)
+    elif a.workload == "plummer":
+        run_plummer(a, local)
+    elif a.workload == "adjoint-check":
+        run_adjoint_check(a, local)
     else:
         run_ours(a, ws, rank, local)
     if ws > 1:

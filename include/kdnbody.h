@@ -172,6 +172,12 @@ int kd_calc_accel(kd_ctx *ctx, double *acc);
  * params.dt. */
 int kd_simple_sim(kd_ctx *ctx, double dt, int64_t steps);
 
+/* Energies of the current bodies: out[0] = sum of m v^2 / 2, out[1] = sum of m phi / 2 with
+ * each body's potential phi from a mixed-precision walk over a tree built for this call
+ * (theta of the context; heavy bodies in FP64).  Used for energy-drift reports; the
+ * reference has no energy diagnostic.  Invalidates the tree of the last kd_build_tree. */
+int kd_energy(kd_ctx *ctx, double out[2]);
+
 /* Switch the arithmetic of later walks (KD_PREC_*). */
 int kd_set_precision(kd_ctx *ctx, int32_t precision);
 

@@ -86,6 +86,7 @@ SIGNATURES = {
                                      C.c_int32, C.POINTER(C.c_double)]),
     "kd_simple_sim": (C.c_int, [C.c_void_p, C.c_double, C.c_int64]),
     "kd_set_precision": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kd_energy": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "kd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(KdStats)]),
     "kd_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "kd_direct_accel": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),

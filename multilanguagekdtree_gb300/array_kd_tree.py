@@ -157,6 +157,12 @@ class KDTreeSim:
     def simple_sim(self, dt: float, steps: int) -> None:
         self._check(self._lib.kd_simple_sim(self._ctx, float(dt), int(steps)))
 
+    def energy(self) -> tuple[float, float]:
+        """(kinetic, potential) energy of the current bodies (potential from a tree walk)."""
+        out = (C.c_double * 2)()
+        self._check(self._lib.kd_energy(self._ctx, out))
+        return float(out[0]), float(out[1])
+
     def set_precision(self, precision) -> None:
         self._check(self._lib.kd_set_precision(self._ctx, _precision(precision)))
 

@@ -173,6 +173,7 @@ struct kd_ctx {
     uint32_t *d_heavy = nullptr, *d_nheavy = nullptr;
     double *d_total = nullptr;
     double *gen_scratch = nullptr;
+    double *phi = nullptr;  // potentials, allocated by the first kd_energy
     int n_heavy = 0;
     std::vector<uint32_t> heavy;
     int final_buf = 0;
@@ -840,6 +841,34 @@ int kd_quickstat_index(const double *vals, size_t n_vals, uint64_t *idx, size_t 
         return KD_EDEVICE;
     }
     for (size_t i = 0; i < n; ++i) idx[i] = out[i];
+    return KD_OK;
+}
+
+int kd_energy(kd_ctx *c, double out[2]) {
+    if (!c) return KD_EINVAL;
+    if (!out) return c->fail(KD_EINVAL, "out is NULL");
+    if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    if (!c->phi) KD_CHECK(c, c->alloc(&c->phi, c->n));
+    constexpr int kBlocks = 256;
+    enqueue_build(c, false, true);
+    launch_walk_mixed(c->recf, c->thi, c->tlo, c->trel, c->tid, (uint32_t)c->n, c->prm.theta,
+                      c->bodies, c->d_heavy, c->n_heavy, c->acc, c->dev_err, nullptr, c->st,
+                      c->phi);
+    launch_energy_partial(c->bodies, c->phi, (uint32_t)c->n, c->gen_scratch, kBlocks, c->st);
+    double part[2 * kBlocks];
+    KD_CHECK(c, cudaMemcpyAsync(part, c->gen_scratch, sizeof part, cudaMemcpyDeviceToHost,
+                                c->st));
+    int rc = check_device(c);
+    c->has_tree = false;  // only the mixed records of this tree were built
+    if (rc) return rc;
+    double k = 0.0, p = 0.0;
+    for (int i = 0; i < kBlocks; ++i) {
+        k += part[2 * i];
+        p += part[2 * i + 1];
+    }
+    out[0] = k;
+    out[1] = p;
     return KD_OK;
 }
 

@@ -213,11 +213,15 @@ void launch_moments_top(const Topology &t, const uint32_t *roots, uint32_t n_roo
 void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
                       double theta, double *acc, uint32_t *err,
                       unsigned long long *counts, cudaStream_t st);
+// phi (optional): also the potential of every body (original order)
 void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
-                       const float4 *trel,
-                       const uint32_t *tid, uint32_t n, double theta, const Bodies &b,
-                       const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
-                       unsigned long long *counts, cudaStream_t st);
+                       const float4 *trel, const uint32_t *tid, uint32_t n, double theta,
+                       const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
+                       uint32_t *err, unsigned long long *counts, cudaStream_t st,
+                       double *phi = nullptr);
+// per-block sums (kinetic, potential) of 0.5 m v^2 and 0.5 m phi into part[2*blocks]
+void launch_energy_partial(const Bodies &b, const double *phi, uint32_t n, double *part,
+                           int blocks, cudaStream_t st);
 void launch_kick_drift(Bodies &b, double *acc, uint32_t n, double dt, cudaStream_t st);
 void launch_aos_to_soa(const void *aos, Bodies &b, uint32_t n, uint32_t *err, cudaStream_t st);
 void launch_soa_to_aos(const Bodies &b, void *aos, uint32_t n, cudaStream_t st);

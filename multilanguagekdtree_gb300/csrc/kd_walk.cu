@@ -166,14 +166,14 @@ struct HeavyBody {
 // Interactions of the lanes in `mask` with one child node of an opened node: the pair sums
 // of a leaf (folded into the compensated sum), or the opening test and, where accepted, the
 // multipole term (into the partial p).  Returns the lanes that open the node.
-template <bool kCount>
+template <bool kCount, bool kPot>
 __device__ __forceinline__ uint32_t visit_mixed(
     const NodeF *__restrict__ rec, const float4 *__restrict__ trel, uint32_t node,
     const float4 &nh, const uint2 &ab, uint32_t mask, uint32_t bit, uint32_t s,
     const float4 &mh, const float4 &ml, float theta2, float &px, float &py, float &pz,
-    float &sx, float &sy, float &sz, float &cx, float &cy, float &cz,
-    unsigned long long &c_p2p, unsigned long long &c_open, unsigned long long &c_m2p,
-    unsigned long long &c_vis) {
+    float &sx, float &sy, float &sz, float &cx, float &cy, float &cz, float &pp, float &sp,
+    float &cp, unsigned long long &c_p2p, unsigned long long &c_open,
+    unsigned long long &c_m2p, unsigned long long &c_vis) {
     const bool act = (mask & bit) != 0;
     if (kCount) c_vis += act ? 1 : 0;
     if (ab.y != 0u) {
@@ -194,12 +194,17 @@ __device__ __forceinline__ uint32_t visit_mixed(
                 px = fmaf(f, dx, px);
                 py = fmaf(f, dy, py);
                 pz = fmaf(f, dz, pz);
+                if (kPot) pp = fmaf(-r.w, inv, pp);
                 if (kCount) ++c_p2p;
             }
             kahan_add(sx, cx, px);
             kahan_add(sy, cy, py);
             kahan_add(sz, cz, pz);
             px = py = pz = 0.f;
+            if (kPot) {
+                kahan_add(sp, cp, pp);
+                pp = 0.f;
+            }
         }
         return 0u;
     }
@@ -222,6 +227,7 @@ __device__ __forceinline__ uint32_t visit_mixed(
             px = fmaf(f, dx, px);
             py = fmaf(f, dy, py);
             pz = fmaf(f, dz, pz);
+            if (kPot) pp = fmaf(-nl.w, inv, pp);
             if (kCount) ++c_m2p;
         }
     }
@@ -232,13 +238,13 @@ __device__ __forceinline__ uint32_t visit_mixed(
 // are loaded together and tested together, and the stack keeps (node, right child, lanes)
 // of opened nodes whose children are still to be visited.  Every lane's decisions are the
 // same as in a one-node-at-a-time walk; only the order of the terms differs.
-template <bool kCount>
+template <bool kCount, bool kPot>
 __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
     const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
     const uint32_t *__restrict__ tid, uint32_t n, float theta2, Bodies b,
     const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
-    uint32_t *err, unsigned long long *counts) {
+    double *__restrict__ phi, uint32_t *err, unsigned long long *counts) {
     __shared__ HeavyBody heavy[kMaxHeavy];
     if (threadIdx.x < n_heavy) {
         const uint32_t h = heavy_ids[threadIdx.x];
@@ -257,6 +263,7 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     // folded into the compensated sum at every leaf
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     float px = 0.f, py = 0.f, pz = 0.f;
+    float pp = 0.f, sp_ = 0.f, cp = 0.f;  // potential: partial, compensated sum
     unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
     // lane k holds stack entry k: an opened node (its right child) and the lanes that opened it
     uint32_t st_node = 0, st_right = 0, st_mask = 0;
@@ -266,8 +273,9 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     {
         const float4 nh = __ldg(&rec[0].hi);
         const uint2 ab = __ldg(reinterpret_cast<const uint2 *>(&rec[0].a));
-        mask = visit_mixed<kCount>(rec, trel, 0u, nh, ab, mask, bit, s, mh, ml, theta2, px, py,
-                                   pz, sx, sy, sz, cx, cy, cz, c_p2p, c_open, c_m2p, c_vis);
+        mask = visit_mixed<kCount, kPot>(rec, trel, 0u, nh, ab, mask, bit, s, mh, ml, theta2, px,
+                                         py, pz, sx, sy, sz, cx, cy, cz, pp, sp_, cp, c_p2p,
+                                         c_open, c_m2p, c_vis);
         cur = 0u;
         cur_right = ab.x;
     }
@@ -277,12 +285,14 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
         const uint2 aL = __ldg(reinterpret_cast<const uint2 *>(&rec[L].a));
         const float4 hR = __ldg(&rec[R].hi);
         const uint2 aR = __ldg(reinterpret_cast<const uint2 *>(&rec[R].a));
-        const uint32_t oL = visit_mixed<kCount>(rec, trel, L, hL, aL, mask, bit, s, mh, ml,
-                                                theta2, px, py, pz, sx, sy, sz, cx, cy, cz,
-                                                c_p2p, c_open, c_m2p, c_vis);
-        const uint32_t oR = visit_mixed<kCount>(rec, trel, R, hR, aR, mask, bit, s, mh, ml,
-                                                theta2, px, py, pz, sx, sy, sz, cx, cy, cz,
-                                                c_p2p, c_open, c_m2p, c_vis);
+        const uint32_t oL = visit_mixed<kCount, kPot>(rec, trel, L, hL, aL, mask, bit, s, mh,
+                                                      ml, theta2, px, py, pz, sx, sy, sz, cx,
+                                                      cy, cz, pp, sp_, cp, c_p2p, c_open, c_m2p,
+                                                      c_vis);
+        const uint32_t oR = visit_mixed<kCount, kPot>(rec, trel, R, hR, aR, mask, bit, s, mh,
+                                                      ml, theta2, px, py, pz, sx, sy, sz, cx,
+                                                      cy, cz, pp, sp_, cp, c_p2p, c_open, c_m2p,
+                                                      c_vis);
         if (oL) {
             if (oR) {
                 if (sp >= kStackMax) {
@@ -314,11 +324,13 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
     kahan_add(sx, cx, px);
     kahan_add(sy, cy, py);
     kahan_add(sz, cz, pz);
+    if (kPot) kahan_add(sp_, cp, pp);
     if (valid) {
         const uint32_t o = tid[s];
         double ax = (double)sx - (double)cx;
         double ay = (double)sy - (double)cy;
         double az = (double)sz - (double)cz;
+        double ph = (double)sp_ - (double)cp;
         // heavy bodies in FP64, pair kernel of array_particle.rs:67-76
         const double px64 = b.x[o], py64 = b.y[o], pz64 = b.z[o];
         for (int h = 0; h < n_heavy; ++h) {
@@ -331,10 +343,12 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
             ax += magi * dx;
             ay += magi * dy;
             az += magi * dz;
+            if (kPot) ph -= q.m / dist;
         }
         acc[3 * (size_t)o] = ax;
         acc[3 * (size_t)o + 1] = ay;
         acc[3 * (size_t)o + 2] = az;
+        if (kPot) phi[o] = ph;
     }
     if (kCount) {
 #pragma unroll
@@ -355,18 +369,54 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
 
 void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
                        const float4 *trel, const uint32_t *tid, uint32_t n, double theta,
-                       const Bodies &b,
-                       const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
-                       unsigned long long *counts, cudaStream_t st) {
+                       const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
+                       uint32_t *err, unsigned long long *counts, cudaStream_t st,
+                       double *phi) {
     const uint32_t threads = kWalkWarps * 32;
     const uint32_t blocks = (n + threads - 1) / threads;
     const float theta2 = (float)(theta * theta);
-    if (counts)
-        k_walk_mixed<true><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n, theta2, b,
-                                                       heavy_ids, n_heavy, acc, err, counts);
+    if (phi)
+        k_walk_mixed<false, true><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n, theta2,
+                                                              b, heavy_ids, n_heavy, acc, phi,
+                                                              err, nullptr);
+    else if (counts)
+        k_walk_mixed<true, false><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n, theta2,
+                                                              b, heavy_ids, n_heavy, acc, nullptr,
+                                                              err, counts);
     else
-        k_walk_mixed<false><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n, theta2, b,
-                                                        heavy_ids, n_heavy, acc, err, nullptr);
+        k_walk_mixed<false, false><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n,
+                                                               theta2, b, heavy_ids, n_heavy, acc,
+                                                               nullptr, err, nullptr);
+}
+
+// 0.5 m v^2 and 0.5 m phi summed per block in a fixed order (then on the host, in order).
+__global__ void k_energy_partial(Bodies b, const double *phi, uint32_t n, double *part) {
+    __shared__ double rk[256], rp[256];
+    double k = 0.0, p = 0.0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double m = b.m[i];
+        k += 0.5 * m * (b.vx[i] * b.vx[i] + b.vy[i] * b.vy[i] + b.vz[i] * b.vz[i]);
+        p += 0.5 * m * phi[i];
+    }
+    rk[threadIdx.x] = k;
+    rp[threadIdx.x] = p;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            rk[threadIdx.x] += rk[threadIdx.x + h];
+            rp[threadIdx.x] += rp[threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = rk[0];
+        part[2 * blockIdx.x + 1] = rp[0];
+    }
+}
+
+void launch_energy_partial(const Bodies &b, const double *phi, uint32_t n, double *part,
+                           int blocks, cudaStream_t st) {
+    k_energy_partial<<<blocks, 256, 0, st>>>(b, phi, n, part);
 }
 
 // ------------------------------------------------------------------ kick-drift

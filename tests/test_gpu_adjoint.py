@@ -85,6 +85,19 @@ def test_ring_sweep_matches_direct_sum_adjoint(kd, oracle):
     assert rel_rows(gx, ref["g_x0"]).max() <= 1e-5
 
 
+def test_long_ring_sweep_matches_direct_sum_adjoint(kd, oracle):
+    """2,000-body ring, theta 0.3, 1,000 steps, checkpoints every 32 steps: the sweep length
+    of the 100,000-body gradient check, at a size the FP64 direct-sum adjoint finishes."""
+    n = 2000
+    b = kd.ring(n, seed=11)
+    tgt = rot_z(b["p"])
+    gx, gv, xT = gpu_grad(kd, b, 1e-3, 1000, tgt)
+    ref = oracle.adjoint_direct(b, 1e-3, 1000, target=tgt)
+    assert rel_rows(gv, ref["g_v0"]).max() <= 1e-4
+    assert np.median(rel_rows(gv, ref["g_v0"])) <= 1e-5
+    assert rel_rows(gx, ref["g_x0"]).max() <= 1e-4
+
+
 def test_ring_sweep_matches_finite_differences(kd):
     """Central differences (h = 1e-6) of the GPU forward on 16 seeded coordinates of v0.  The
     loss difference is summed per body so that the bodies the perturbation does not reach

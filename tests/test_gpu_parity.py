@@ -257,3 +257,18 @@ def test_mixed_precision_plummer(kd, oracle):
     assert np.sqrt(np.mean(err ** 2)) <= 1e-5
     assert err.max() <= 1e-3
     s.close()
+
+
+# ------------------------------------------------------------------ energy diagnostic
+
+@pytest.mark.parametrize("gen,theta,tol", [("ring", 0.3, 1e-9), ("plummer", 0.3, 1e-3),
+                                           ("plummer", 0.0, 1e-6)])
+def test_energy_matches_direct_sum(kd, oracle, gen, theta, tol):
+    n = 3000
+    b = kd.ring(n, seed=9) if gen == "ring" else kd.plummer(n, seed=9)
+    with kd.KDTreeSim(n, theta=theta) as s:
+        s.set_bodies(b)
+        ke, pe = s.energy()
+    rke, rpe = oracle.energy(b)
+    assert ke == pytest.approx(rke, rel=1e-12)
+    assert pe == pytest.approx(rpe, rel=tol)
