@@ -231,8 +231,10 @@ int kd_direct_accel_noalloc(const double *x, const double *y, const double *z,
                             double *acc, void *stream);
 
 /* Interaction counts of the last walk, summed over bodies: out[0] = pair (P2P)
- * interactions, out[1] = opening tests at internal nodes, out[2] = accepted multipole
- * (M2P) interactions, out[3] = nodes visited by the warps.  Counting is enabled by
+ * interactions, out[2] = accepted multipole (M2P) interactions.  FP64 walk: out[1] =
+ * opening tests at internal nodes, out[3] = node visits, both per body.  Mixed (grouped)
+ * walk: out[1] = node tests, each made once for a group of up to 32 bodies, out[3] = the
+ * same tests counted once per body of the group.  Counting is enabled by
  * kd_set_counting(ctx, 1) (it costs a few percent). */
 int kd_set_counting(kd_ctx *ctx, int32_t on);
 int kd_get_counts(const kd_ctx *ctx, uint64_t out[4]);

@@ -1,6 +1,6 @@
 """Build recipe of libkdnbody.so: nvcc, sm_103a only, in-tree.
 
-The three CUDA translation units are compiled in parallel and linked into
+The CUDA translation units are compiled in parallel and linked into
 ``multilanguagekdtree_gb300/libkdnbody.so`` next to this file.  A rebuild happens only when
 a source or header is newer than the library.
 """
@@ -17,8 +17,8 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 OBJDIR = PKG.parent / "_build" / "kdnbody"
 LIB = PKG / "libkdnbody.so"
-SOURCES = ["kd_build.cu", "kd_walk.cu", "kd_adjoint.cu", "kd_generate.cu", "kd_api.cu",
-           "kd_noalloc.cu"]
+SOURCES = ["kd_build.cu", "kd_walk.cu", "kd_group.cu", "kd_adjoint.cu", "kd_generate.cu",
+           "kd_api.cu", "kd_noalloc.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",

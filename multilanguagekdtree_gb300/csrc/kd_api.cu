@@ -53,6 +53,9 @@ struct Plan {
     std::vector<uint32_t> ttab;
     uint64_t par4_slots = 0, par4_last = 0;
     bool par4_ok = true;
+    uint32_t depth = 0;                   // deepest node (root = 0)
+    std::vector<uint32_t> gstart;         // sink groups of the grouped walk (tree positions)
+    std::vector<uint32_t> gsplit;         // per group: split of the deepest node holding it
 };
 
 struct Memo {
@@ -93,7 +96,9 @@ bool make_plan(uint32_t n, uint32_t leaf, Plan &p, std::string &err) {
     };
     std::vector<E> cur{{0u, 0u, n, kNone, 0ull, p.par4_slots}}, nxt;
     bool local_found = false;
+    uint32_t level = 0;
     while (!cur.empty()) {
+        p.depth = level++;
         uint32_t mx = 0;
         for (const E &e : cur) mx = std::max(mx, e.cn);
         if (!local_found && mx <= (uint32_t)kLocalMax) {
@@ -131,6 +136,41 @@ bool make_plan(uint32_t n, uint32_t leaf, Plan &p, std::string &err) {
         }
         cur.swap(nxt);
     }
+    // Sink groups: whole leaves in tree order, packed greedily up to 32 bodies.
+    std::vector<std::pair<uint32_t, uint32_t>> lv;
+    lv.reserve(p.leaves.size());
+    for (uint32_t id : p.leaves) lv.emplace_back(p.start[id], p.count[id]);
+    std::sort(lv.begin(), lv.end());
+    p.gstart.clear();
+    uint32_t fill = 32;
+    for (const auto &e : lv) {
+        if (fill + e.second > 32) {
+            p.gstart.push_back(e.first);
+            fill = 0;
+        }
+        fill += e.second;
+    }
+    p.gstart.push_back(n);
+    // The split position of the deepest node that holds a group whole (a node of c bodies
+    // at position st splits at st + c/2); a one-leaf group has none (its end).
+    p.gsplit.resize(p.gstart.size() - 1);
+    for (size_t g = 0; g + 1 < p.gstart.size(); ++g) {
+        const uint32_t g0 = p.gstart[g], g1 = p.gstart[g + 1];
+        uint32_t st = 0, cn = n, sp = g1;
+        while (cn > leaf) {
+            const uint32_t mid = st + cn / 2;
+            if (g1 <= mid) {
+                cn = cn / 2;
+            } else if (g0 >= mid) {
+                st = mid;
+                cn = cn - cn / 2;
+            } else {
+                sp = mid;
+                break;
+            }
+        }
+        p.gsplit[g] = sp;
+    }
     return true;
 }
 
@@ -152,7 +192,9 @@ struct kd_ctx {
 
     // static topology on the device
     uint32_t *d_start = nullptr, *d_count = nullptr, *d_right = nullptr, *d_parent = nullptr,
-             *d_leaves = nullptr, *d_ttab = nullptr, *d_local_roots = nullptr;
+             *d_leaves = nullptr, *d_ttab = nullptr, *d_local_roots = nullptr,
+             *d_gstart = nullptr, *d_gsplit = nullptr;
+    uint32_t n_groups = 0, group_stack = 0;
     std::vector<uint32_t *> d_glevels;
     Topology topo{};
 
@@ -246,6 +288,11 @@ int setup(kd_ctx *c) {
     if ((rc = upload(c, &c->d_leaves, p.leaves))) return rc;
     if ((rc = upload(c, &c->d_ttab, p.ttab))) return rc;
     if ((rc = upload(c, &c->d_local_roots, p.local_roots))) return rc;
+    if ((rc = upload(c, &c->d_gstart, p.gstart))) return rc;
+    if ((rc = upload(c, &c->d_gsplit, p.gsplit))) return rc;
+    c->n_groups = (uint32_t)p.gstart.size() - 1;
+    // a wave pops <= 32 entries and pushes <= 64: at most 32 wait per depth, plus one push
+    c->group_stack = 32u * (p.depth + 2u) + 64u;
     c->d_glevels.resize(p.glevels.size());
     size_t maxG = 1, maxGT = 1, maxGmulti = 1;
     for (size_t l = 0; l < p.glevels.size(); ++l) {
@@ -383,10 +430,15 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     c->final_buf = cur;
 }
 
-void enqueue_walk(kd_ctx *c) {
+// grouped = false: the per-body mixed walk, whose interaction set the adjoint sweep follows
+void enqueue_walk(kd_ctx *c, bool grouped = true) {
     c->launches += 1;
     unsigned long long *cnt = c->counting ? c->d_counts : nullptr;
-    if (c->prm.precision == KD_PREC_MIXED)
+    if (c->prm.precision == KD_PREC_MIXED && grouped)
+        launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart, c->d_gsplit, c->n_groups,
+                          c->group_stack, c->prm.theta, c->bodies, c->d_heavy, c->n_heavy,
+                          c->acc, c->dev_err, cnt, c->st);
+    else if (c->prm.precision == KD_PREC_MIXED)
         launch_walk_mixed(c->recf, c->thi, c->tlo, c->trel, c->tid, (uint32_t)c->n, c->prm.theta,
                           c->bodies, c->d_heavy, c->n_heavy, c->acc, c->dev_err, cnt, c->st);
     else
@@ -500,10 +552,10 @@ int adj_alloc(kd_ctx *c, int64_t every) {
     return KD_OK;
 }
 
-void enqueue_step(kd_ctx *c, double dt) {
+void enqueue_step(kd_ctx *c, double dt, bool grouped = true) {
     const bool mixed = c->prm.precision == KD_PREC_MIXED;
     enqueue_build(c, !mixed, mixed);
-    enqueue_walk(c);
+    enqueue_walk(c, grouped);
     launch_kick_drift(c->bodies, c->acc, (uint32_t)c->n, dt, c->st);
     c->launches += 1;
 }
@@ -852,9 +904,9 @@ int kd_energy(kd_ctx *c, double out[2]) {
     if (!c->phi) KD_CHECK(c, c->alloc(&c->phi, c->n));
     constexpr int kBlocks = 256;
     enqueue_build(c, false, true);
-    launch_walk_mixed(c->recf, c->thi, c->tlo, c->trel, c->tid, (uint32_t)c->n, c->prm.theta,
-                      c->bodies, c->d_heavy, c->n_heavy, c->acc, c->dev_err, nullptr, c->st,
-                      c->phi);
+    launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart, c->d_gsplit, c->n_groups,
+                      c->group_stack, c->prm.theta, c->bodies, c->d_heavy, c->n_heavy, c->acc,
+                      c->dev_err, nullptr, c->st, c->phi);
     launch_energy_partial(c->bodies, c->phi, (uint32_t)c->n, c->gen_scratch, kBlocks, c->st);
     double part[2 * kBlocks];
     KD_CHECK(c, cudaMemcpyAsync(part, c->gen_scratch, sizeof part, cudaMemcpyDeviceToHost,
@@ -1038,7 +1090,7 @@ int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape 
             rc = copy_state(c, t->ck[(size_t)(s / ckpt_every)], true);
             if (rc) break;
         }
-        enqueue_step(c, dt);
+        enqueue_step(c, dt, false);
     }
     if (!rc) rc = copy_state(c, t->final_state, true);
     KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
@@ -1109,7 +1161,7 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
             for (int k = 0; k < 3; ++k)
                 KD_CHECK(c, cudaMemcpyAsync(dst + k * n, pos[k], n * sizeof(double),
                                             cudaMemcpyDeviceToDevice, c->st));
-            if (s + 1 < n1) enqueue_step(c, t->dt);
+            if (s + 1 < n1) enqueue_step(c, t->dt, false);
         }
         for (int64_t s = n1 - 1; s >= n0; --s) {
             const double *src = c->segbuf + 3 * n * (size_t)(s - n0);

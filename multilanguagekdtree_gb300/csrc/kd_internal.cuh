@@ -213,6 +213,22 @@ void launch_moments_top(const Topology &t, const uint32_t *roots, uint32_t n_roo
 void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
                       double theta, double *acc, uint32_t *err,
                       unsigned long long *counts, cudaStream_t st);
+// Grouped mixed walk: groups of whole leaves, <= 32 bodies, gstart[g]..gstart[g+1] in tree
+// order, boxed in two parts split at gsplit[g]; stk_cap = per-warp stack entries (a multiple
+// of 32).
+constexpr int kGroupWarps = 4;
+constexpr int kGroupFlush = 256;
+constexpr int kGroupListCap = kGroupFlush + 32 * 8;
+// shared memory of one warp: interaction list, own-leaf list and positions, stack
+__host__ __device__ inline uint32_t group_warp_bytes(uint32_t stk_cap) {
+    return (uint32_t)((kGroupListCap + 32) * sizeof(float4) + 32 * sizeof(uint32_t) +
+                      stk_cap * sizeof(uint32_t));
+}
+void launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
+                       const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
+                       const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta, const Bodies &b,
+                       const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
+                       unsigned long long *counts, cudaStream_t st, double *phi = nullptr);
 // phi (optional): also the potential of every body (original order)
 void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
                        const float4 *trel, const uint32_t *tid, uint32_t n, double theta,

@@ -65,6 +65,8 @@ class Oracle:
             "orc_adjoint_direct": (C.c_int, [_vp, C.c_size_t, C.c_double, C.c_int64, _vp, _vp,
                                              _vp, _vp, _vp, _vp, _vp]),
             "orc_tree_jt": (C.c_int, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_double, _vp, _vp]),
+            "orc_calc_accel_group": (C.c_int, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_double, _vp,
+                                               _vp]),
             "orc_omp_threads": (C.c_int, []),
             "orc_set_threads": (None, [C.c_int]),
         }
@@ -144,6 +146,20 @@ class Oracle:
         self.lib.orc_walk_counts(_p(b), _p(nodes), theta, _p(s), len(s), _p(out))
         return {"p2p": int(out[0]), "opened": int(out[1]), "m2p": int(out[2]),
                 "visits": int(out[3])}
+
+    def calc_accel_group(self, bodies, nodes, theta: float = 0.3):
+        """FP64 restatement of the grouped walk of the mixed path: sinks in groups of whole
+        leaves (depth-first, <= 32 bodies), node accepted for a group when
+        size^2 < theta^2 dmin^2 to the group's bounding box.  Returns (acc, counts)."""
+        b = self._bodies(bodies)
+        nodes = np.ascontiguousarray(nodes, dtype=NODE)
+        acc = np.zeros((len(b), 3))
+        out = np.zeros(4, dtype=np.uint64)
+        if self.lib.orc_calc_accel_group(_p(b), len(b), _p(nodes), len(nodes), theta, _p(acc),
+                                         _p(out)):
+            raise RuntimeError("orc_calc_accel_group: out of memory")
+        return acc, {"p2p": int(out[0]), "tests": int(out[1]), "m2p": int(out[2]),
+                     "opened": int(out[3])}
 
     def simple_sim(self, bodies, dt: float, steps: int, leaf: int = 7, layout: str = "dfs",
                    theta: float = 0.3, seed: int = 1, trace: bool = False):

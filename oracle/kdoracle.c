@@ -375,6 +375,169 @@ void orc_walk_counts(const orc_particle *P, const orc_node *nodes, double theta,
     out[0] = tot.p2p; out[1] = tot.opened; out[2] = tot.m2p; out[3] = tot.visits;
 }
 
+/* ---------------------------------------------------------------- grouped walk */
+
+/* The sink groups of the GPU's grouped mixed walk: whole leaves in depth-first order
+ * (left before right), packed greedily up to 32 bodies.  A node is accepted for a whole
+ * group when size^2 < theta^2 dmin^2, dmin the distance from the node's centre of mass to
+ * the nearer of the group's two bounding boxes (Barnes 1990, J. Comput. Phys. 87:161); leaves
+ * reached are summed pairwise, self excluded by index.  Everything in FP64, each sink's
+ * terms added in traversal order. */
+static size_t dfs_leaves(const orc_node *nodes, size_t cur, size_t *out, size_t k) {
+    if (nodes[cur].num_parts > 0) {
+        out[k] = cur;
+        return k + 1;
+    }
+    k = dfs_leaves(nodes, nodes[cur].left, out, k);
+    return dfs_leaves(nodes, nodes[cur].right, out, k);
+}
+
+/* Squared distance from c to the box [lo, hi] (infinite for an empty box, lo > hi). */
+static double box_dist2(const double c[3], const double lo[3], const double hi[3]) {
+    if (lo[0] > hi[0]) return INFINITY;
+    double e2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        double e = lo[d] - c[d];
+        if (c[d] - hi[d] > e) e = c[d] - hi[d];
+        if (e > 0.0) e2 += e * e;
+    }
+    return e2;
+}
+
+static void group_recur(size_t cur, const orc_particle *P, const orc_node *nodes,
+                        const uint64_t *sinks, size_t ns, const double lo[2][3],
+                        const double hi[2][3], double theta2, double *acc, orc_counts *c) {
+    const orc_node *nd = &nodes[cur];
+    c->visits++;
+    if (nd->num_parts > 0) {
+        for (size_t k = 0; k < ns; ++k)
+            for (uint64_t i = 0; i < nd->num_parts; ++i) {
+                if (nd->particles[i] == sinks[k]) continue;
+                double pa[3];
+                pp_accel(&P[sinks[k]], &P[nd->particles[i]], pa);
+                acc[3 * k] += pa[0];
+                acc[3 * k + 1] += pa[1];
+                acc[3 * k + 2] += pa[2];
+                c->p2p++;
+            }
+        return;
+    }
+    double e2 = box_dist2(nd->cm, lo[0], hi[0]);
+    const double f2 = box_dist2(nd->cm, lo[1], hi[1]);
+    if (f2 < e2) e2 = f2;
+    if (nd->size * nd->size < theta2 * e2) {
+        for (size_t k = 0; k < ns; ++k) {
+            const double *p = P[sinks[k]].p;
+            double dx = p[0] - nd->cm[0], dy = p[1] - nd->cm[1], dz = p[2] - nd->cm[2];
+            double dist_sqr = dx * dx + dy * dy + dz * dz;
+            double dist = sqrt(dist_sqr);
+            double magi = -nd->m / (dist_sqr * dist);
+            acc[3 * k] += dx * magi;
+            acc[3 * k + 1] += dy * magi;
+            acc[3 * k + 2] += dz * magi;
+            c->m2p++;
+        }
+        return;
+    }
+    c->opened++;
+    group_recur(nd->left, P, nodes, sinks, ns, lo, hi, theta2, acc, c);
+    group_recur(nd->right, P, nodes, sinks, ns, lo, hi, theta2, acc, c);
+}
+
+/* The group's bodies are boxed in two parts, split where the deepest node holding the whole
+ * group splits (a node of c bodies at depth-first position st splits at st + c/2); the test
+ * uses the nearer box. */
+static size_t group_split(const orc_node *nodes, size_t n, size_t g0, size_t g1) {
+    size_t cur = 0, st = 0, cn = n;
+    while (nodes[cur].num_parts == 0) {
+        const size_t mid = st + cn / 2;
+        if (g1 <= mid) {
+            cn = cn / 2;
+            cur = nodes[cur].left;
+        } else if (g0 >= mid) {
+            st = mid;
+            cn = cn - cn / 2;
+            cur = nodes[cur].right;
+        } else {
+            return mid;
+        }
+    }
+    return g1;
+}
+
+/* Groups of the tree: first body of every group in depth-first body order (`order`, n
+ * entries) and group offsets (`gstart`, n_groups + 1).  Returns n_groups. */
+static size_t make_groups(const orc_node *nodes, size_t n_nodes, uint64_t *order,
+                          size_t *gstart) {
+    size_t *lv = (size_t *)malloc(sizeof(size_t) * (n_nodes + 1));
+    size_t nl = dfs_leaves(nodes, 0, lv, 0), pos = 0, ng = 0, fill = 32;
+    for (size_t k = 0; k < nl; ++k) {
+        const orc_node *nd = &nodes[lv[k]];
+        if (fill + nd->num_parts > 32) {
+            gstart[ng++] = pos;
+            fill = 0;
+        }
+        for (uint64_t i = 0; i < nd->num_parts; ++i) order[pos++] = nd->particles[i];
+        fill += nd->num_parts;
+    }
+    gstart[ng] = pos;
+    free(lv);
+    return ng;
+}
+
+/* acc (n*3, original body order); counts: p2p and m2p per sink, node tests per group,
+ * internal nodes opened per group. */
+int orc_calc_accel_group(const orc_particle *P, size_t n, const orc_node *nodes, size_t n_nodes,
+                         double theta, double *acc, uint64_t counts[4]) {
+    uint64_t *order = (uint64_t *)malloc(sizeof(uint64_t) * n);
+    size_t *gstart = (size_t *)malloc(sizeof(size_t) * (n + 1));
+    if (!order || !gstart) {
+        free(order);
+        free(gstart);
+        return -1;
+    }
+    const size_t ng = make_groups(nodes, n_nodes, order, gstart);
+    const double theta2 = theta * theta;
+    uint64_t p2p = 0, m2p = 0, tests = 0, opened = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : p2p, m2p, tests, opened)
+    for (size_t g = 0; g < ng; ++g) {
+        const uint64_t *sk = order + gstart[g];
+        const size_t ns = gstart[g + 1] - gstart[g];
+        const size_t sp = group_split(nodes, n, gstart[g], gstart[g + 1]) - gstart[g];
+        double lo[2][3], hi[2][3], a[3 * 32];
+        for (int h = 0; h < 2; ++h)
+            for (int d = 0; d < 3; ++d) {
+                lo[h][d] = INFINITY;
+                hi[h][d] = -INFINITY;
+            }
+        for (size_t k = 0; k < ns; ++k) {
+            const int h = k < sp ? 0 : 1;
+            for (int d = 0; d < 3; ++d) {
+                if (P[sk[k]].p[d] < lo[h][d]) lo[h][d] = P[sk[k]].p[d];
+                if (P[sk[k]].p[d] > hi[h][d]) hi[h][d] = P[sk[k]].p[d];
+            }
+        }
+        for (size_t k = 0; k < 3 * ns; ++k) a[k] = 0.0;
+        orc_counts c = {0, 0, 0, 0};
+        group_recur(0, P, nodes, sk, ns, lo, hi, theta2, a, &c);
+        for (size_t k = 0; k < ns; ++k)
+            for (int d = 0; d < 3; ++d) acc[3 * sk[k] + d] = a[3 * k + d];
+        p2p += c.p2p;
+        m2p += c.m2p;
+        tests += c.visits;
+        opened += c.opened;
+    }
+    if (counts) {
+        counts[0] = p2p;
+        counts[1] = tests;
+        counts[2] = m2p;
+        counts[3] = opened;
+    }
+    free(order);
+    free(gstart);
+    return 0;
+}
+
 /* ---------------------------------------------------------------- step loop */
 
 /* simple_sim, Parallel/RustVersion/src/array_kd_tree.rs:623-664 (layout 1 = build_tree_par4)
