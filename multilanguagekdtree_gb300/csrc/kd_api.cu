@@ -235,7 +235,7 @@ struct kd_ctx {
     int64_t adj_every = 0;
     double *lx = nullptr, *lv = nullptr, *amu = nullptr, *ay = nullptr, *ysink = nullptr,
            *yheavy = nullptr, *segbuf = nullptr;
-    float *aU = nullptr, *aG = nullptr;
+    double *aU = nullptr, *aG = nullptr;
 
     int fail(int code, const char *fmt, ...) {
         char buf[512];
@@ -430,17 +430,13 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     c->final_buf = cur;
 }
 
-// grouped = false: the per-body mixed walk, whose interaction set the adjoint sweep follows
-void enqueue_walk(kd_ctx *c, bool grouped = true) {
+void enqueue_walk(kd_ctx *c) {
     c->launches += 1;
     unsigned long long *cnt = c->counting ? c->d_counts : nullptr;
-    if (c->prm.precision == KD_PREC_MIXED && grouped)
-        launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart, c->d_gsplit, c->n_groups,
-                          c->group_stack, c->prm.theta, c->bodies, c->d_heavy, c->n_heavy,
-                          c->acc, c->dev_err, cnt, c->st);
-    else if (c->prm.precision == KD_PREC_MIXED)
-        launch_walk_mixed(c->recf, c->thi, c->tlo, c->trel, c->tid, (uint32_t)c->n, c->prm.theta,
-                          c->bodies, c->d_heavy, c->n_heavy, c->acc, c->dev_err, cnt, c->st);
+    if (c->prm.precision == KD_PREC_MIXED)
+        launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart, c->d_gsplit,
+                          c->n_groups, c->group_stack, c->prm.theta, c->bodies, c->d_heavy,
+                          c->n_heavy, c->acc, c->dev_err, cnt, c->st);
     else
         launch_walk_fp64(c->recd, c->tpos, c->tid, (uint32_t)c->n, c->prm.theta, c->acc,
                          c->dev_err, cnt, c->st);
@@ -552,10 +548,10 @@ int adj_alloc(kd_ctx *c, int64_t every) {
     return KD_OK;
 }
 
-void enqueue_step(kd_ctx *c, double dt, bool grouped = true) {
+void enqueue_step(kd_ctx *c, double dt) {
     const bool mixed = c->prm.precision == KD_PREC_MIXED;
     enqueue_build(c, !mixed, mixed);
-    enqueue_walk(c, grouped);
+    enqueue_walk(c);
     launch_kick_drift(c->bodies, c->acc, (uint32_t)c->n, dt, c->st);
     c->launches += 1;
 }
@@ -1059,6 +1055,8 @@ int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape 
     if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
     if (c->prm.precision != KD_PREC_MIXED)
         return c->fail(KD_EINVAL, "the adjoint is implemented for KD_PREC_MIXED contexts");
+    if (c->plan.n_nodes >= 0x80000000u)
+        return c->fail(KD_EINVAL, "the adjoint supports trees of fewer than 2^31 nodes");
     if (steps < 1 || ckpt_every < 1) return c->fail(KD_EINVAL, "steps and ckpt_every must be >= 1");
     if (dt == 0.0) dt = c->prm.dt;
     KD_CHECK(c, cudaSetDevice(c->prm.device));
@@ -1090,7 +1088,7 @@ int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape 
             rc = copy_state(c, t->ck[(size_t)(s / ckpt_every)], true);
             if (rc) break;
         }
-        enqueue_step(c, dt, false);
+        enqueue_step(c, dt);
     }
     if (!rc) rc = copy_state(c, t->final_state, true);
     KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
@@ -1116,6 +1114,8 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
     if (!dL_dx || !g_x0 || !g_v0) return c->fail(KD_EINVAL, "NULL gradient buffer");
     if (c->prm.precision != KD_PREC_MIXED)
         return c->fail(KD_EINVAL, "the adjoint is implemented for KD_PREC_MIXED contexts");
+    if (c->plan.n_nodes >= 0x80000000u)
+        return c->fail(KD_EINVAL, "the adjoint supports trees of fewer than 2^31 nodes");
     KD_CHECK(c, cudaSetDevice(c->prm.device));
     int rc = adj_alloc(c, t->every);
     if (rc) return rc;
@@ -1147,6 +1147,10 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
     a.U = c->aU;
     a.G = c->aG;
     a.err = c->dev_err;
+    a.gstart = c->d_gstart;
+    a.gsplit = c->d_gsplit;
+    a.n_groups = c->n_groups;
+    a.stk_cap = c->group_stack;
     c->launches = 0;
     KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
     const int64_t nseg = (t->steps + t->every - 1) / t->every;
@@ -1161,7 +1165,7 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
             for (int k = 0; k < 3; ++k)
                 KD_CHECK(c, cudaMemcpyAsync(dst + k * n, pos[k], n * sizeof(double),
                                             cudaMemcpyDeviceToDevice, c->st));
-            if (s + 1 < n1) enqueue_step(c, t->dt, false);
+            if (s + 1 < n1) enqueue_step(c, t->dt);
         }
         for (int64_t s = n1 - 1; s >= n0; --s) {
             const double *src = c->segbuf + 3 * n * (size_t)(s - n0);

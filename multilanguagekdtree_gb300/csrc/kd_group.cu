@@ -1,4 +1,4 @@
-// kd_group.cu -- grouped theta-opening walk of the mixed-precision path.
+// kd_group.cu -- grouped theta-opening walk of the mixed-precision path, and its adjoint.
 //
 // The sinks are cut into groups of whole leaves, consecutive in tree order, at most 32
 // bodies each (one per lane).  A warp walks the tree once for its group: the 32 lanes test
@@ -9,8 +9,8 @@
 // group splits: a run of leaves that crosses a high-level split joins two far-apart corners
 // of the tree, and one box around both would open nearly every node for that group.
 // Accepted nodes and the bodies of reached leaves go to an interaction list in shared
-// memory; whenever the list holds kFlush entries every lane sums it for its own body, so the
-// force loop runs without divergence and without per-lane traversal state.
+// memory; whenever the list holds kGroupFlush entries every lane sums it for its own body,
+// so the force loop runs without divergence and without per-lane traversal state.
 //
 // A node the group accepts passes the reference's per-body test (array_kd_tree.rs:600-609)
 // for every body of the group, because dmin is at most each body's distance: every body's
@@ -19,7 +19,14 @@
 //
 // Coordinates are relative to the group's first body (split hi + lo to FP32), forces are
 // FP32 with compensated (Kahan) sums per block of 32 list entries, and the heavy bodies are
-// summed in FP64 at the end, as in the per-body mixed walk.
+// summed in FP64 at the end.
+//
+// The adjoint walk runs the same traversal (the same code, so the same decisions) and
+// evaluates each block of 32 list entries against the 32 sinks with a rotation: at step k
+// lane l pairs its sink with entry (l + k) mod 32 and passes the entry's source-side
+// accumulator one lane down, so after 32 steps lane l holds the sum over all sinks for
+// entry l -- both sides of J^T mu from one tidal product per pair, one FP64 atomic per entry
+// and component (the sums over groups then carry no FP32 rounding).
 #include "kd_internal.cuh"
 
 namespace kd {
@@ -27,6 +34,9 @@ namespace kd {
 namespace {
 
 constexpr uint32_t kFull = 0xffffffffu;
+constexpr uint32_t kNodeTarget = 0x80000000u;  // adjoint list target: node id (else body)
+constexpr uint32_t kNoTarget = 0xffffffffu;
+constexpr float kFar = 1e15f;  // position of padding entries: contributes exactly nothing
 
 __device__ __forceinline__ float rsqrt_ftz(float x) {
     float y;
@@ -66,8 +76,180 @@ __device__ __forceinline__ float warp_max(float v) {
     return v;
 }
 
-// Sum of the list entries [0, nl) on the lane's body at (qx, qy, qz): plain FP32 partial
-// sums over 32 entries, each folded into the compensated sums.
+// Per-warp shared memory: interaction list, own-leaf list, stack, and (adjoint) the list's
+// source targets.  An own-list entry k is own[2k] = (hi xyz, light mass) and
+// own[2k+1] = (lo xyz, tree position as bits): pairs inside the group are formed from the
+// split absolute positions, so a close pair's separation keeps its relative precision.
+struct WarpMem {
+    float4 *list, *own;
+    uint32_t *stk, *tgt;
+};
+
+__device__ __forceinline__ WarpMem warp_mem(float4 *smem, int warp, uint32_t stk_cap,
+                                            bool with_tgt) {
+    const uint32_t wbytes =
+        group_warp_bytes(stk_cap) + (with_tgt ? kGroupListCap * (uint32_t)sizeof(uint32_t) : 0u);
+    WarpMem w;
+    w.list = reinterpret_cast<float4 *>(reinterpret_cast<char *>(smem) + warp * wbytes);
+    w.own = w.list + kGroupListCap;
+    w.stk = reinterpret_cast<uint32_t *>(w.own + 64);
+    w.tgt = w.stk + stk_cap;
+    return w;
+}
+
+// One lane's view of its group: tree positions, frame origin, own position, the two boxes.
+struct Group {
+    uint32_t g0, g1, s;
+    bool valid;
+    float ohx, ohy, ohz, olx, oly, olz;  // origin: the group's first body, hi + lo
+    float qx, qy, qz;                    // the lane's body in the group frame
+    float4 mh, ml;                       // the lane's body, split absolute position
+    float a[6], b[6];                    // boxes (lo xyz, hi xyz) before / after the split
+};
+
+__device__ __forceinline__ Group make_group(const float4 *__restrict__ thi,
+                                            const float4 *__restrict__ tlo, uint32_t g0,
+                                            uint32_t g1, uint32_t gs, int lane) {
+    Group G;
+    G.g0 = g0;
+    G.g1 = g1;
+    G.valid = lane < (int)(g1 - g0);
+    G.s = G.valid ? g0 + lane : g0;
+    const float4 mh = thi[G.s], ml = tlo[G.s];
+    G.mh = mh;
+    G.ml = ml;
+    G.ohx = __shfl_sync(kFull, mh.x, 0);
+    G.ohy = __shfl_sync(kFull, mh.y, 0);
+    G.ohz = __shfl_sync(kFull, mh.z, 0);
+    G.olx = __shfl_sync(kFull, ml.x, 0);
+    G.oly = __shfl_sync(kFull, ml.y, 0);
+    G.olz = __shfl_sync(kFull, ml.z, 0);
+    G.qx = (mh.x - G.ohx) + (ml.x - G.olx);
+    G.qy = (mh.y - G.ohy) + (ml.y - G.oly);
+    G.qz = (mh.z - G.ohz) + (ml.z - G.olz);
+    const bool inA = G.valid && G.s < gs, inB = G.valid && G.s >= gs;
+    const float q[3] = {G.qx, G.qy, G.qz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        G.a[d] = warp_min(inA ? q[d] : INFINITY);
+        G.a[d + 3] = warp_max(inA ? q[d] : -INFINITY);
+        G.b[d] = warp_min(inB ? q[d] : INFINITY);
+        G.b[d + 3] = warp_max(inB ? q[d] : -INFINITY);
+    }
+    return G;
+}
+
+// Walk of one group.  Accepted nodes and far leaves' bodies are appended to W.list (with
+// their source targets when kTgt); the group's own leaves go to W.own.  flush(nl) is
+// called whenever the list holds kGroupFlush entries or more, and at the end.
+template <bool kTgt, bool kCount, typename Flush>
+__device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
+                                         const float4 *__restrict__ trel,
+                                         const float4 *__restrict__ thi,
+                                         const float4 *__restrict__ tlo, const Group &G,
+                                         const WarpMem &W, uint32_t stk_cap, float theta2,
+                                         int lane, uint32_t *err, uint32_t &nown,
+                                         unsigned long long (&cnt)[3], Flush &&flush) {
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t nl = 0, top = 1;
+    nown = 0;
+    if (lane == 0) W.stk[0] = 0u;
+    __syncwarp();
+    while (top > 0) {
+        const uint32_t take = min(top, 32u);
+        const bool has = (uint32_t)lane < take;
+        const uint32_t node = has ? W.stk[top - 1 - lane] : 0u;
+        top -= take;
+        __syncwarp();
+        if (kCount) cnt[2] += take;
+        float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
+        uint2 ab = make_uint2(0u, 0u);
+        if (has) {
+            h = __ldg(&rec[node].hi);
+            l = __ldg(&rec[node].lo);
+            ab = __ldg(reinterpret_cast<const uint2 *>(&rec[node].a));
+        }
+        const bool leaf = ab.y != 0u;
+        // centre of mass (leaf: its first body) in the group frame
+        const float cx = (h.x - G.ohx) + (l.x - G.olx);
+        const float cy = (h.y - G.ohy) + (l.y - G.oly);
+        const float cz = (h.z - G.ohz) + (l.z - G.olz);
+        const float ex = fmaxf(fmaxf(G.a[0] - cx, cx - G.a[3]), 0.f);
+        const float ey = fmaxf(fmaxf(G.a[1] - cy, cy - G.a[4]), 0.f);
+        const float ez = fmaxf(fmaxf(G.a[2] - cz, cz - G.a[5]), 0.f);
+        const float fx = fmaxf(fmaxf(G.b[0] - cx, cx - G.b[3]), 0.f);
+        const float fy = fmaxf(fmaxf(G.b[1] - cy, cy - G.b[4]), 0.f);
+        const float fz = fmaxf(fmaxf(G.b[2] - cz, cz - G.b[5]), 0.f);
+        const float dmin2 = fminf(fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
+                                  fmaf(fx, fx, fmaf(fy, fy, fz * fz)));
+        const bool take_m = has && !leaf && h.w < theta2 * dmin2;
+        const bool open = has && !leaf && !take_m;
+        const bool mine = has && leaf && ab.x >= G.g0 && ab.x < G.g1;
+        const bool far = has && leaf && !mine;
+
+        // accepted nodes: one entry each
+        const uint32_t am = __ballot_sync(kFull, take_m);
+        if (take_m) {
+            const uint32_t k = nl + __popc(am & lt);
+            W.list[k] = make_float4(cx, cy, cz, l.w);
+            if (kTgt) W.tgt[k] = node | kNodeTarget;
+        }
+        nl += __popc(am);
+        if (kCount) cnt[1] += __popc(am);
+        // reached leaves: their bodies, the group's own leaves into their own list
+        const uint32_t fc = far ? ab.y : 0u, oc = mine ? ab.y : 0u;
+        const uint32_t fi = warp_incl_scan(fc, lane), oi = warp_incl_scan(oc, lane);
+        const uint32_t ft = __shfl_sync(kFull, fi, 31), ot = __shfl_sync(kFull, oi, 31);
+        if (far) {
+            // all member loads of the leaf in flight at once (leaf size <= 8)
+            float4 t[8];
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k)
+                if (k < ab.y) t[k] = __ldg(&trel[ab.x + k]);
+            const uint32_t d0 = nl + fi - fc;
+#pragma unroll
+            for (uint32_t k = 0; k < 8; ++k)
+                if (k < ab.y) {
+                    W.list[d0 + k] = make_float4(cx + t[k].x, cy + t[k].y, cz + t[k].z, t[k].w);
+                    if (kTgt) W.tgt[d0 + k] = ab.x + k;
+                }
+        } else if (mine) {
+            const uint32_t o0 = nown + oi - oc;
+            for (uint32_t k = 0; k < ab.y && o0 + k < 32u; ++k) {
+                const float4 hi = __ldg(&thi[ab.x + k]), lo = __ldg(&tlo[ab.x + k]);
+                W.own[2 * (o0 + k)] = hi;
+                W.own[2 * (o0 + k) + 1] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(ab.x + k));
+            }
+        }
+        nl += ft;
+        nown = min(nown + ot, 32u);
+        if (kCount) cnt[0] += ft;
+        // opened nodes: both children
+        const uint32_t om = __ballot_sync(kFull, open);
+        if (top + 2u * __popc(om) > stk_cap) {
+            if (lane == 0) atomicOr(err, kErrStack);
+            break;
+        }
+        if (open) {
+            const uint32_t slot = top + 2u * __popc(om & lt);
+            W.stk[slot] = ab.x;          // right child
+            W.stk[slot + 1] = node + 1u;  // left child
+        }
+        top += 2u * __popc(om);
+        __syncwarp();
+        if (nl >= (uint32_t)kGroupFlush) {
+            flush(nl);
+            nl = 0;
+            __syncwarp();
+        }
+    }
+    __syncwarp();
+    if (nl) flush(nl);
+    __syncwarp();
+}
+
+// Sum of the entries [0, nl) on the lane's body: plain FP32 partial sums over 32 entries,
+// each folded into the compensated sums.
 template <bool kPot>
 __device__ __forceinline__ void sum_list(const float4 *list, uint32_t nl, float qx, float qy,
                                          float qz, float (&s)[4], float (&c)[4]) {
@@ -94,6 +276,51 @@ __device__ __forceinline__ void sum_list(const float4 *list, uint32_t nl, float 
     }
 }
 
+// w = |d|^-3 (mu - 3 (d . mu) |d|^-2 d), d = sink - source: the tidal tensor times mu.
+__device__ __forceinline__ void tidal_w(float dx, float dy, float dz, float mx, float my,
+                                        float mz, float &wx, float &wy, float &wz) {
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float inv = rsqrt_ftz(d2);
+    const float inv2 = inv * inv, inv3 = inv2 * inv;
+    const float dm = fmaf(dx, mx, fmaf(dy, my, dz * mz));
+    const float c3 = 3.0f * dm * inv2;
+    wx = inv3 * fmaf(-c3, dx, mx);
+    wy = inv3 * fmaf(-c3, dy, my);
+    wz = inv3 * fmaf(-c3, dz, mz);
+}
+
+// Adjoint terms of 32 sources (padding sources far away with zero mass) against the warp's
+// 32 sinks by rotation: the sink terms -m w into the compensated sums (sum, comp), folded
+// every 8 pairs, and lane l returns the sum over the sinks of w for source l.
+// `pair(slot, dx, dy, dz)` gives the separation sink - source and returns the source mass.
+template <typename Pair>
+__device__ __forceinline__ void rotate32(int lane, float mx, float my, float mz,
+                                         float (&sum)[3], float (&comp)[3], float &ax,
+                                         float &ay, float &az, Pair &&pair) {
+    ax = ay = az = 0.f;
+    const int up = (lane + 1) & 31;
+#pragma unroll 1
+    for (int k0 = 0; k0 < 32; k0 += 8) {
+        float px = 0.f, py = 0.f, pz = 0.f;
+#pragma unroll
+        for (int k = k0; k < k0 + 8; ++k) {
+            float dx, dy, dz;
+            const float m = pair((lane + k) & 31, dx, dy, dz);
+            float wx, wy, wz;
+            tidal_w(dx, dy, dz, mx, my, mz, wx, wy, wz);
+            px = fmaf(-m, wx, px);
+            py = fmaf(-m, wy, py);
+            pz = fmaf(-m, wz, pz);
+            ax = __shfl_sync(kFull, ax + wx, up);
+            ay = __shfl_sync(kFull, ay + wy, up);
+            az = __shfl_sync(kFull, az + wz, up);
+        }
+        kahan(sum[0], comp[0], px);
+        kahan(sum[1], comp[1], py);
+        kahan(sum[2], comp[2], pz);
+    }
+}
+
 }  // namespace
 
 template <bool kCount, bool kPot>
@@ -101,9 +328,9 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
     const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
     const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,
-    const uint32_t *__restrict__ gsplit, uint32_t n_groups, uint32_t stk_cap, float theta2, Bodies b, const uint32_t *__restrict__ heavy_ids,
-    int n_heavy, double *__restrict__ acc, double *__restrict__ phi, uint32_t *err,
-    unsigned long long *counts) {
+    const uint32_t *__restrict__ gsplit, uint32_t n_groups, uint32_t stk_cap, float theta2,
+    Bodies b, const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
+    double *__restrict__ phi, uint32_t *err, unsigned long long *counts) {
     extern __shared__ float4 smem[];
     __shared__ Heavy heavy[kMaxHeavy];
     if (threadIdx.x < n_heavy) {
@@ -114,136 +341,30 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t g = blockIdx.x * kGroupWarps + warp;
     if (g >= n_groups) return;  // no block-wide barrier follows
-    const uint32_t wbytes = group_warp_bytes(stk_cap);
-    float4 *list = reinterpret_cast<float4 *>(reinterpret_cast<char *>(smem) + warp * wbytes);
-    float4 *own = list + kGroupListCap;
-    uint32_t *own_pos = reinterpret_cast<uint32_t *>(own + 32);
-    uint32_t *stk = own_pos + 32;
-    const uint32_t lt = (1u << lane) - 1u;
-
-    const uint32_t g0 = gstart[g], g1 = gstart[g + 1], gs = gsplit[g];
-    const bool valid = lane < (int)(g1 - g0);
-    const uint32_t s = valid ? g0 + lane : g0;
-    const float4 mh = thi[s], ml = tlo[s];
-    // the group's frame: origin at its first body, split precision
-    const float ohx = __shfl_sync(kFull, mh.x, 0), ohy = __shfl_sync(kFull, mh.y, 0),
-                ohz = __shfl_sync(kFull, mh.z, 0);
-    const float olx = __shfl_sync(kFull, ml.x, 0), oly = __shfl_sync(kFull, ml.y, 0),
-                olz = __shfl_sync(kFull, ml.z, 0);
-    const float qx = (mh.x - ohx) + (ml.x - olx);
-    const float qy = (mh.y - ohy) + (ml.y - oly);
-    const float qz = (mh.z - ohz) + (ml.z - olz);
-    // two boxes: the group's bodies before and after the split of the deepest node holding
-    // the whole group (an empty box gives an infinite distance)
-    const bool inA = valid && s < gs, inB = valid && s >= gs;
-    const float alx = warp_min(inA ? qx : INFINITY), ahx = warp_max(inA ? qx : -INFINITY);
-    const float aly = warp_min(inA ? qy : INFINITY), ahy = warp_max(inA ? qy : -INFINITY);
-    const float alz = warp_min(inA ? qz : INFINITY), ahz = warp_max(inA ? qz : -INFINITY);
-    const float blx = warp_min(inB ? qx : INFINITY), bhx = warp_max(inB ? qx : -INFINITY);
-    const float bly = warp_min(inB ? qy : INFINITY), bhy = warp_max(inB ? qy : -INFINITY);
-    const float blz = warp_min(inB ? qz : INFINITY), bhz = warp_max(inB ? qz : -INFINITY);
+    const WarpMem W = warp_mem(smem, warp, stk_cap, false);
+    const Group G = make_group(thi, tlo, gstart[g], gstart[g + 1], gsplit[g], lane);
+    const uint32_t s = G.s;
 
     float sum[4] = {0.f, 0.f, 0.f, 0.f}, comp[4] = {0.f, 0.f, 0.f, 0.f};
-    uint32_t nl = 0, nown = 0, top = 1;
-    unsigned long long n_m2p = 0, n_p2p = 0, n_test = 0;
-    if (lane == 0) stk[0] = 0u;
-    __syncwarp();
-    while (top > 0) {
-        const uint32_t take = min(top, 32u);
-        const bool has = (uint32_t)lane < take;
-        const uint32_t node = has ? stk[top - 1 - lane] : 0u;
-        top -= take;
-        __syncwarp();
-        if (kCount) n_test += take;
-        float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
-        uint2 ab = make_uint2(0u, 0u);
-        if (has) {
-            h = __ldg(&rec[node].hi);
-            l = __ldg(&rec[node].lo);
-            ab = __ldg(reinterpret_cast<const uint2 *>(&rec[node].a));
-        }
-        const bool leaf = ab.y != 0u;
-        // centre of mass (leaf: its first body) in the group frame
-        const float cx = (h.x - ohx) + (l.x - olx);
-        const float cy = (h.y - ohy) + (l.y - oly);
-        const float cz = (h.z - ohz) + (l.z - olz);
-        const float ex = fmaxf(fmaxf(alx - cx, cx - ahx), 0.f);
-        const float ey = fmaxf(fmaxf(aly - cy, cy - ahy), 0.f);
-        const float ez = fmaxf(fmaxf(alz - cz, cz - ahz), 0.f);
-        const float fx = fmaxf(fmaxf(blx - cx, cx - bhx), 0.f);
-        const float fy = fmaxf(fmaxf(bly - cy, cy - bhy), 0.f);
-        const float fz = fmaxf(fmaxf(blz - cz, cz - bhz), 0.f);
-        const float dmin2 = fminf(fmaf(ex, ex, fmaf(ey, ey, ez * ez)),
-                                  fmaf(fx, fx, fmaf(fy, fy, fz * fz)));
-        const bool take_m = has && !leaf && h.w < theta2 * dmin2;
-        const bool open = has && !leaf && !take_m;
-        const bool mine = has && leaf && ab.x >= g0 && ab.x < g1;
-        const bool far = has && leaf && !mine;
-
-        // accepted nodes: one entry each
-        const uint32_t am = __ballot_sync(kFull, take_m);
-        if (take_m) list[nl + __popc(am & lt)] = make_float4(cx, cy, cz, l.w);
-        nl += __popc(am);
-        if (kCount) n_m2p += __popc(am);
-        // reached leaves: their bodies, the group's own leaves into their own list
-        const uint32_t fc = far ? ab.y : 0u, oc = mine ? ab.y : 0u;
-        const uint32_t fi = warp_incl_scan(fc, lane), oi = warp_incl_scan(oc, lane);
-        const uint32_t ft = __shfl_sync(kFull, fi, 31), ot = __shfl_sync(kFull, oi, 31);
-        if (leaf && has) {
-            // all member loads of the leaf in flight at once (leaf size <= 8)
-            float4 t[8];
-#pragma unroll
-            for (uint32_t k = 0; k < 8; ++k)
-                if (k < ab.y) t[k] = __ldg(&trel[ab.x + k]);
-            if (far) {
-                float4 *dst = list + nl + fi - fc;
-#pragma unroll
-                for (uint32_t k = 0; k < 8; ++k)
-                    if (k < ab.y) dst[k] = make_float4(cx + t[k].x, cy + t[k].y, cz + t[k].z, t[k].w);
-            } else {
-                const uint32_t o0 = nown + oi - oc;
-#pragma unroll
-                for (uint32_t k = 0; k < 8; ++k)
-                    if (k < ab.y && o0 + k < 32u) {
-                        own[o0 + k] = make_float4(cx + t[k].x, cy + t[k].y, cz + t[k].z, t[k].w);
-                        own_pos[o0 + k] = ab.x + k;
-                    }
-            }
-        }
-        nl += ft;
-        nown = min(nown + ot, 32u);
-        if (kCount) n_p2p += ft;
-        // opened nodes: both children
-        const uint32_t om = __ballot_sync(kFull, open);
-        if (top + 2u * __popc(om) > stk_cap) {
-            if (lane == 0) atomicOr(err, kErrStack);
-            break;
-        }
-        if (open) {
-            const uint32_t slot = top + 2u * __popc(om & lt);
-            stk[slot] = ab.x;      // right child
-            stk[slot + 1] = node + 1u;  // left child
-        }
-        top += 2u * __popc(om);
-        __syncwarp();
-        if (nl >= (uint32_t)kGroupFlush) {
-            sum_list<kPot>(list, nl, qx, qy, qz, sum, comp);
-            nl = 0;
-            __syncwarp();
-        }
-    }
-    __syncwarp();
-    if (nl) sum_list<kPot>(list, nl, qx, qy, qz, sum, comp);
-    // the group's own leaves, self excluded by tree position
+    uint32_t nown = 0;
+    unsigned long long cnt[3] = {0, 0, 0};  // pair entries, node entries, node tests
+    traverse<false, kCount>(rec, trel, thi, tlo, G, W, stk_cap, theta2, lane, err, nown, cnt,
+                            [&](uint32_t nl) {
+                                sum_list<kPot>(W.list, nl, G.qx, G.qy, G.qz, sum, comp);
+                            });
+    // the group's own leaves, self excluded by tree position, separations from the split
+    // absolute positions
     {
         float px = 0.f, py = 0.f, pz = 0.f, pp = 0.f;
         for (uint32_t k = 0; k < nown; ++k) {
-            if (own_pos[k] == s) continue;
-            const float4 e = own[k];
-            const float dx = e.x - qx, dy = e.y - qy, dz = e.z - qz;
+            const float4 eh = W.own[2 * k], el = W.own[2 * k + 1];
+            if (__float_as_uint(el.w) == s) continue;
+            const float dx = (eh.x - G.mh.x) + (el.x - G.ml.x);
+            const float dy = (eh.y - G.mh.y) + (el.y - G.ml.y);
+            const float dz = (eh.z - G.mh.z) + (el.z - G.ml.z);
             const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const float inv = rsqrt_ftz(d2);
-            const float mi = e.w * inv;
+            const float mi = eh.w * inv;
             const float f = mi * (inv * inv);
             px = fmaf(f, dx, px);
             py = fmaf(f, dy, py);
@@ -255,7 +376,7 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
         kahan(sum[2], comp[2], pz);
         if (kPot) kahan(sum[3], comp[3], -pp);
     }
-    if (valid) {
+    if (G.valid) {
         const uint32_t o = tid[s];
         double ax = (double)sum[0] - (double)comp[0];
         double ay = (double)sum[1] - (double)comp[1];
@@ -281,21 +402,174 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
         if (kPot) phi[o] = ph;
     }
     if (kCount && lane == 0) {
-        const unsigned long long nv = g1 - g0;
+        const unsigned long long nv = G.g1 - G.g0;
         // the own leaves hold every body of the group (each reached once)
         const unsigned long long own_pairs = nown >= nv ? nv * (nown - 1) : nv * nown;
-        atomicAdd(&counts[0], nv * n_p2p + own_pairs);
-        atomicAdd(&counts[1], n_test);
-        atomicAdd(&counts[2], nv * n_m2p);
-        atomicAdd(&counts[3], nv * n_test);
+        atomicAdd(&counts[0], nv * cnt[0] + own_pairs);
+        atomicAdd(&counts[1], cnt[2]);
+        atomicAdd(&counts[2], nv * cnt[1]);
+        atomicAdd(&counts[3], nv * cnt[2]);
+    }
+}
+
+// Transpose-Jacobian product of one step over the grouped interaction set.  Per sink s:
+// ysink_s (tree order) = -sum m w + the FP64 heavy-body terms; per list entry the sum over
+// the group's sinks of w goes to U (a body, tree order) or G (a node); the heavy bodies'
+// source sums go to yheavy.
+__global__ __launch_bounds__(kGroupWarps * 32, 4) void k_adj_group(
+    const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
+    const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
+    const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,
+    const uint32_t *__restrict__ gsplit, uint32_t n_groups, uint32_t stk_cap, float theta2,
+    Bodies b, const uint32_t *__restrict__ heavy_ids, int n_heavy,
+    const double *__restrict__ mu, double *__restrict__ ysink, double *__restrict__ U,
+    double *__restrict__ Gn, double *__restrict__ yheavy, uint32_t *err) {
+    extern __shared__ float4 smem[];
+    __shared__ Heavy heavy[kMaxHeavy];
+    __shared__ double hred[kGroupWarps][kMaxHeavy][3];
+    if (threadIdx.x < n_heavy) {
+        const uint32_t h = heavy_ids[threadIdx.x];
+        heavy[threadIdx.x] = Heavy{b.x[h], b.y[h], b.z[h], b.m[h]};
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t g = blockIdx.x * kGroupWarps + warp;
+    double hx[kMaxHeavy][3];
+#pragma unroll
+    for (int h = 0; h < kMaxHeavy; ++h) hx[h][0] = hx[h][1] = hx[h][2] = 0.0;
+    if (g < n_groups) {  // warp-uniform; the block barrier below is reached by every warp
+        const WarpMem W = warp_mem(smem, warp, stk_cap, true);
+        const Group G = make_group(thi, tlo, gstart[g], gstart[g + 1], gsplit[g], lane);
+        const uint32_t s = G.s;
+        const uint32_t o = G.valid ? tid[s] : 0u;
+        double mux = 0.0, muy = 0.0, muz = 0.0;
+        if (G.valid) {
+            mux = mu[3 * (size_t)o];
+            muy = mu[3 * (size_t)o + 1];
+            muz = mu[3 * (size_t)o + 2];
+        }
+        const float mx = (float)mux, my = (float)muy, mz = (float)muz;
+        // lanes without a body sit far away with mu = 0: every term they make is zero
+        const float qx = G.valid ? G.qx : -kFar, qy = G.valid ? G.qy : -kFar,
+                    qz = G.valid ? G.qz : -kFar;
+        float sum[3] = {0.f, 0.f, 0.f}, comp[3] = {0.f, 0.f, 0.f};
+        uint32_t nown = 0;
+        unsigned long long cnt[3] = {0, 0, 0};
+        traverse<true, false>(
+            rec, trel, thi, tlo, G, W, stk_cap, theta2, lane, err, nown, cnt, [&](uint32_t nl) {
+                const uint32_t nr = (nl + 31u) & ~31u;
+                if ((uint32_t)lane < nr - nl) {
+                    W.list[nl + lane] = make_float4(kFar, kFar, kFar, 0.f);
+                    W.tgt[nl + lane] = kNoTarget;
+                }
+                __syncwarp();
+                for (uint32_t k0 = 0; k0 < nr; k0 += 32) {
+                    float ax, ay, az;
+                    const float4 *e = W.list + k0;
+                    rotate32(lane, mx, my, mz, sum, comp, ax, ay, az,
+                             [&](int slot, float &dx, float &dy, float &dz) {
+                                 const float4 c = e[slot];
+                                 dx = qx - c.x;
+                                 dy = qy - c.y;
+                                 dz = qz - c.z;
+                                 return c.w;
+                             });
+                    const uint32_t t = W.tgt[k0 + lane];
+                    if (t != kNoTarget) {
+                        double *dst = (t & kNodeTarget) ? Gn + 3 * (size_t)(t & ~kNodeTarget)
+                                                        : U + 3 * (size_t)t;
+                        atomicAdd(dst, (double)ax);
+                        atomicAdd(dst + 1, (double)ay);
+                        atomicAdd(dst + 2, (double)az);
+                    }
+                }
+            });
+        // the group's own leaves: pairs among the group's bodies, self excluded, separations
+        // from the split absolute positions
+        {
+            if ((uint32_t)lane >= nown) {
+                W.own[2 * lane] = make_float4(kFar, kFar, kFar, 0.f);
+                W.own[2 * lane + 1] = make_float4(0.f, 0.f, 0.f, __uint_as_float(kNoTarget));
+            }
+            __syncwarp();
+            // lanes without a body sit far away on the other side: no pair reaches zero
+            const float4 mh = G.valid ? G.mh : make_float4(-kFar, -kFar, -kFar, 0.f);
+            const float4 ml = G.valid ? G.ml : make_float4(0.f, 0.f, 0.f, 0.f);
+            float ax, ay, az;
+            rotate32(lane, mx, my, mz, sum, comp, ax, ay, az,
+                     [&](int slot, float &dx, float &dy, float &dz) {
+                         const float4 eh = W.own[2 * slot], el = W.own[2 * slot + 1];
+                         if (__float_as_uint(el.w) == s && G.valid) {
+                             dx = dy = dz = kFar;
+                             return 0.f;
+                         }
+                         dx = (mh.x - eh.x) + (ml.x - el.x);
+                         dy = (mh.y - eh.y) + (ml.y - el.y);
+                         dz = (mh.z - eh.z) + (ml.z - el.z);
+                         return eh.w;
+                     });
+            const uint32_t t = __float_as_uint(W.own[2 * lane + 1].w);
+            if (t != kNoTarget) {
+                atomicAdd(&U[3 * (size_t)t], (double)ax);
+                atomicAdd(&U[3 * (size_t)t + 1], (double)ay);
+                atomicAdd(&U[3 * (size_t)t + 2], (double)az);
+            }
+        }
+        if (G.valid) {
+            double ysx = (double)sum[0] - (double)comp[0];
+            double ysy = (double)sum[1] - (double)comp[1];
+            double ysz = (double)sum[2] - (double)comp[2];
+            // heavy bodies in FP64: sink side here, source side reduced over the block
+            const double X = b.x[o], Y = b.y[o], Z = b.z[o];
+#pragma unroll
+            for (int h = 0; h < kMaxHeavy; ++h) {
+                if (h >= n_heavy || heavy_ids[h] == o) continue;
+                const Heavy q = heavy[h];
+                const double dx = X - q.x, dy = Y - q.y, dz = Z - q.z;
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                const double inv2 = 1.0 / d2;
+                const double inv3 = inv2 * sqrt(inv2);
+                const double dm = dx * mux + dy * muy + dz * muz;
+                const double c3 = 3.0 * dm * inv2;
+                const double wx = inv3 * (mux - c3 * dx), wy = inv3 * (muy - c3 * dy),
+                             wz = inv3 * (muz - c3 * dz);
+                ysx -= q.m * wx;
+                ysy -= q.m * wy;
+                ysz -= q.m * wz;
+                hx[h][0] = q.m * wx;
+                hx[h][1] = q.m * wy;
+                hx[h][2] = q.m * wz;
+            }
+            ysink[3 * (size_t)s] = ysx;
+            ysink[3 * (size_t)s + 1] = ysy;
+            ysink[3 * (size_t)s + 2] = ysz;
+        }
+    }
+    if (n_heavy > 0) {
+#pragma unroll
+        for (int h = 0; h < kMaxHeavy; ++h)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                double val = hx[h][d];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) val += __shfl_xor_sync(kFull, val, off);
+                if (lane == 0) hred[warp][h][d] = val;
+            }
+        __syncthreads();
+        if (threadIdx.x < (unsigned)(3 * n_heavy)) {
+            const int h = threadIdx.x / 3, d = threadIdx.x % 3;
+            double val = 0.0;
+            for (int w = 0; w < kGroupWarps; ++w) val += hred[w][h][d];
+            atomicAdd(&yheavy[3 * h + d], val);
+        }
     }
 }
 
 void launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
                        const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
-                       const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta, const Bodies &b,
-                       const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
-                       unsigned long long *counts, cudaStream_t st, double *phi) {
+                       const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta,
+                       const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
+                       uint32_t *err, unsigned long long *counts, cudaStream_t st, double *phi) {
     const uint32_t threads = kGroupWarps * 32;
     const uint32_t blocks = (n_groups + kGroupWarps - 1) / kGroupWarps;
     const size_t smem = (size_t)kGroupWarps * group_warp_bytes(stk_cap);
@@ -303,19 +577,34 @@ void launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
     if (phi) {
         auto k = k_walk_group<false, true>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups, stk_cap,
-                                         theta2, b, heavy_ids, n_heavy, acc, phi, err, nullptr);
+        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups,
+                                         stk_cap, theta2, b, heavy_ids, n_heavy, acc, phi, err,
+                                         nullptr);
     } else if (counts) {
         auto k = k_walk_group<true, false>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups, stk_cap,
-                                         theta2, b, heavy_ids, n_heavy, acc, nullptr, err, counts);
+        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups,
+                                         stk_cap, theta2, b, heavy_ids, n_heavy, acc, nullptr,
+                                         err, counts);
     } else {
         auto k = k_walk_group<false, false>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups, stk_cap,
-                                         theta2, b, heavy_ids, n_heavy, acc, nullptr, err, nullptr);
+        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups,
+                                         stk_cap, theta2, b, heavy_ids, n_heavy, acc, nullptr,
+                                         err, nullptr);
     }
+}
+
+void launch_adj_group(const AdjArgs &a, cudaStream_t st) {
+    const uint32_t threads = kGroupWarps * 32;
+    const uint32_t blocks = (a.n_groups + kGroupWarps - 1) / kGroupWarps;
+    const size_t smem = (size_t)kGroupWarps *
+                        (group_warp_bytes(a.stk_cap) + kGroupListCap * sizeof(uint32_t));
+    cudaFuncSetAttribute(k_adj_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_adj_group<<<blocks, threads, smem, st>>>(
+        a.recf, a.thi, a.tlo, a.trel, a.tid, a.gstart, a.gsplit, a.n_groups, a.stk_cap,
+        (float)(a.theta * a.theta), a.bodies, a.heavy, a.n_heavy, a.mu, a.ysink, a.U, a.G,
+        a.yheavy, a.err);
 }
 
 }  // namespace kd

@@ -219,22 +219,16 @@ void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, u
 constexpr int kGroupWarps = 4;
 constexpr int kGroupFlush = 256;
 constexpr int kGroupListCap = kGroupFlush + 32 * 8;
-// shared memory of one warp: interaction list, own-leaf list and positions, stack
+// shared memory of one warp: interaction list, own-leaf list (split positions), stack
 __host__ __device__ inline uint32_t group_warp_bytes(uint32_t stk_cap) {
-    return (uint32_t)((kGroupListCap + 32) * sizeof(float4) + 32 * sizeof(uint32_t) +
-                      stk_cap * sizeof(uint32_t));
+    return (uint32_t)((kGroupListCap + 64) * sizeof(float4) + stk_cap * sizeof(uint32_t));
 }
 void launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
                        const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
                        const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta, const Bodies &b,
                        const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
                        unsigned long long *counts, cudaStream_t st, double *phi = nullptr);
-// phi (optional): also the potential of every body (original order)
-void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
-                       const float4 *trel, const uint32_t *tid, uint32_t n, double theta,
-                       const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
-                       uint32_t *err, unsigned long long *counts, cudaStream_t st,
-                       double *phi = nullptr);
+
 // per-block sums (kinetic, potential) of 0.5 m v^2 and 0.5 m phi into part[2*blocks]
 void launch_energy_partial(const Bodies &b, const double *phi, uint32_t n, double *part,
                            int blocks, cudaStream_t st);
@@ -270,10 +264,14 @@ struct AdjArgs {
     double *mu, *y;         // 3n scratch
     double *ysink;          // 3n, tree order
     double *yheavy;         // 3 * kMaxHeavy
-    float *U;               // 3n, tree order: pair-source sums
-    float *G;               // 3 * n_nodes: node-source sums
+    double *U;              // 3n, tree order: pair-source sums
+    double *G;              // 3 * n_nodes: node-source sums
     uint32_t *err;
+    const uint32_t *gstart, *gsplit;  // sink groups of the grouped walk
+    uint32_t n_groups, stk_cap;
 };
+// The transpose-Jacobian walk over the grouped interaction set (kd_group.cu).
+void launch_adj_group(const AdjArgs &a, cudaStream_t st);
 // One backward step over the tree currently built (mixed records).  Returns kernels launched.
 int launch_adjoint_step(const AdjArgs &a, cudaStream_t st);
 

@@ -7,9 +7,7 @@
 // reference's IEEE operation order (array_kd_tree.rs:601-609, array_particle.rs:67-76),
 // written with explicit round-to-nearest intrinsics so no multiply-add is fused.
 //
-// Mixed path: the same traversal in FP32 on split (hi + lo) coordinates, compensated
-// (Kahan) per-body sums, and the heavy bodies (the central mass of a ring) summed directly
-// in FP64 and left out of the FP32 node masses.
+// The mixed-precision path walks the tree per group of sinks (kd_group.cu).
 #include "kd_internal.cuh"
 
 namespace kd {
@@ -148,245 +146,6 @@ void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, u
     else
         k_walk_fp64<false><<<blocks, threads, 0, st>>>(rec, tpos, tid, n, theta2, acc, err,
                                                        nullptr);
-}
-
-// ------------------------------------------------------------------ mixed walk
-
-__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
-    const float y = x - comp;
-    const float t = sum + y;
-    comp = (t - sum) - y;
-    sum = t;
-}
-
-struct HeavyBody {
-    double x, y, z, m;
-};
-
-// Interactions of the lanes in `mask` with one child node of an opened node: the pair sums
-// of a leaf (folded into the compensated sum), or the opening test and, where accepted, the
-// multipole term (into the partial p).  Returns the lanes that open the node.
-template <bool kCount, bool kPot>
-__device__ __forceinline__ uint32_t visit_mixed(
-    const NodeF *__restrict__ rec, const float4 *__restrict__ trel, uint32_t node,
-    const float4 &nh, const uint2 &ab, uint32_t mask, uint32_t bit, uint32_t s,
-    const float4 &mh, const float4 &ml, float theta2, float &px, float &py, float &pz,
-    float &sx, float &sy, float &sz, float &cx, float &cy, float &cz, float &pp, float &sp,
-    float &cp, unsigned long long &c_p2p, unsigned long long &c_open,
-    unsigned long long &c_m2p, unsigned long long &c_vis) {
-    const bool act = (mask & bit) != 0;
-    if (kCount) c_vis += act ? 1 : 0;
-    if (ab.y != 0u) {
-        if (act) {
-            // sink position relative to the leaf origin, in split precision
-            const float4 ol = __ldg(&rec[node].lo);
-            const float qx = (mh.x - nh.x) + (ml.x - ol.x);
-            const float qy = (mh.y - nh.y) + (ml.y - ol.y);
-            const float qz = (mh.z - nh.z) + (ml.z - ol.z);
-            for (uint32_t k = 0; k < ab.y; ++k) {
-                const uint32_t j = ab.x + k;
-                if (j == s) continue;
-                const float4 r = __ldg(&trel[j]);
-                const float dx = qx - r.x, dy = qy - r.y, dz = qz - r.z;
-                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const float inv = rsqrtf(d2);
-                const float f = -r.w * (inv * inv * inv);
-                px = fmaf(f, dx, px);
-                py = fmaf(f, dy, py);
-                pz = fmaf(f, dz, pz);
-                if (kPot) pp = fmaf(-r.w, inv, pp);
-                if (kCount) ++c_p2p;
-            }
-            kahan_add(sx, cx, px);
-            kahan_add(sy, cy, py);
-            kahan_add(sz, cz, pz);
-            px = py = pz = 0.f;
-            if (kPot) {
-                kahan_add(sp, cp, pp);
-                pp = 0.f;
-            }
-        }
-        return 0u;
-    }
-    // opening test on the high parts: an approximate decision suffices here
-    const float ex = mh.x - nh.x, ey = mh.y - nh.y, ez = mh.z - nh.z;
-    const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-    const bool take = act && nh.w < theta2 * e2;
-    if (kCount) c_open += act ? 1 : 0;
-    const uint32_t tk = __ballot_sync(kFull, take);
-    if (tk) {
-        const float4 nl = __ldg(&rec[node].lo);
-        if (take) {
-            // force on the split coordinates
-            const float dx = ex + (ml.x - nl.x);
-            const float dy = ey + (ml.y - nl.y);
-            const float dz = ez + (ml.z - nl.z);
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float inv = rsqrtf(d2);
-            const float f = -nl.w * (inv * inv * inv);
-            px = fmaf(f, dx, px);
-            py = fmaf(f, dy, py);
-            pz = fmaf(f, dz, pz);
-            if (kPot) pp = fmaf(-nl.w, inv, pp);
-            if (kCount) ++c_m2p;
-        }
-    }
-    return mask & ~tk;
-}
-
-// The traversal handles both children of an opened node per iteration: their two records
-// are loaded together and tested together, and the stack keeps (node, right child, lanes)
-// of opened nodes whose children are still to be visited.  Every lane's decisions are the
-// same as in a one-node-at-a-time walk; only the order of the terms differs.
-template <bool kCount, bool kPot>
-__global__ __launch_bounds__(kWalkWarps * 32) void k_walk_mixed(
-    const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
-    const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
-    const uint32_t *__restrict__ tid, uint32_t n, float theta2, Bodies b,
-    const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
-    double *__restrict__ phi, uint32_t *err, unsigned long long *counts) {
-    __shared__ HeavyBody heavy[kMaxHeavy];
-    if (threadIdx.x < n_heavy) {
-        const uint32_t h = heavy_ids[threadIdx.x];
-        heavy[threadIdx.x] = HeavyBody{b.x[h], b.y[h], b.z[h], b.m[h]};
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t s = (blockIdx.x * kWalkWarps + warp) * 32 + lane;
-    const bool valid = s < n;
-    uint32_t mask = __ballot_sync(kFull, valid);
-    if (mask == 0) return;
-    const uint32_t bit = 1u << lane;
-    const float4 mh = valid ? thi[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 ml = valid ? tlo[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-    // compensated body sum (s, c); multipole terms gather in the plain partial p, which is
-    // folded into the compensated sum at every leaf
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    float px = 0.f, py = 0.f, pz = 0.f;
-    float pp = 0.f, sp_ = 0.f, cp = 0.f;  // potential: partial, compensated sum
-    unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
-    // lane k holds stack entry k: an opened node (its right child) and the lanes that opened it
-    uint32_t st_node = 0, st_right = 0, st_mask = 0;
-    int sp = 0;
-    // the root alone
-    uint32_t cur, cur_right;
-    {
-        const float4 nh = __ldg(&rec[0].hi);
-        const uint2 ab = __ldg(reinterpret_cast<const uint2 *>(&rec[0].a));
-        mask = visit_mixed<kCount, kPot>(rec, trel, 0u, nh, ab, mask, bit, s, mh, ml, theta2, px,
-                                         py, pz, sx, sy, sz, cx, cy, cz, pp, sp_, cp, c_p2p,
-                                         c_open, c_m2p, c_vis);
-        cur = 0u;
-        cur_right = ab.x;
-    }
-    while (mask) {
-        const uint32_t L = cur + 1, R = cur_right;
-        const float4 hL = __ldg(&rec[L].hi);
-        const uint2 aL = __ldg(reinterpret_cast<const uint2 *>(&rec[L].a));
-        const float4 hR = __ldg(&rec[R].hi);
-        const uint2 aR = __ldg(reinterpret_cast<const uint2 *>(&rec[R].a));
-        const uint32_t oL = visit_mixed<kCount, kPot>(rec, trel, L, hL, aL, mask, bit, s, mh,
-                                                      ml, theta2, px, py, pz, sx, sy, sz, cx,
-                                                      cy, cz, pp, sp_, cp, c_p2p, c_open, c_m2p,
-                                                      c_vis);
-        const uint32_t oR = visit_mixed<kCount, kPot>(rec, trel, R, hR, aR, mask, bit, s, mh,
-                                                      ml, theta2, px, py, pz, sx, sy, sz, cx,
-                                                      cy, cz, pp, sp_, cp, c_p2p, c_open, c_m2p,
-                                                      c_vis);
-        if (oL) {
-            if (oR) {
-                if (sp >= kStackMax) {
-                    if (lane == 0) atomicOr(err, kErrStack);
-                    break;
-                }
-                if (lane == sp) {
-                    st_node = R;
-                    st_right = aR.x;
-                    st_mask = oR;
-                }
-                ++sp;
-            }
-            cur = L;
-            cur_right = aL.x;
-            mask = oL;
-        } else if (oR) {
-            cur = R;
-            cur_right = aR.x;
-            mask = oR;
-        } else {
-            if (sp == 0) break;
-            --sp;
-            cur = __shfl_sync(kFull, st_node, sp);
-            cur_right = __shfl_sync(kFull, st_right, sp);
-            mask = __shfl_sync(kFull, st_mask, sp);
-        }
-    }
-    kahan_add(sx, cx, px);
-    kahan_add(sy, cy, py);
-    kahan_add(sz, cz, pz);
-    if (kPot) kahan_add(sp_, cp, pp);
-    if (valid) {
-        const uint32_t o = tid[s];
-        double ax = (double)sx - (double)cx;
-        double ay = (double)sy - (double)cy;
-        double az = (double)sz - (double)cz;
-        double ph = (double)sp_ - (double)cp;
-        // heavy bodies in FP64, pair kernel of array_particle.rs:67-76
-        const double px64 = b.x[o], py64 = b.y[o], pz64 = b.z[o];
-        for (int h = 0; h < n_heavy; ++h) {
-            if (heavy_ids[h] == o) continue;
-            const HeavyBody q = heavy[h];
-            const double dx = px64 - q.x, dy = py64 - q.y, dz = pz64 - q.z;
-            const double dp2 = dx * dx + dy * dy + dz * dz;
-            const double dist = sqrt(dp2);
-            const double magi = -q.m / (dist * dist * dist);
-            ax += magi * dx;
-            ay += magi * dy;
-            az += magi * dz;
-            if (kPot) ph -= q.m / dist;
-        }
-        acc[3 * (size_t)o] = ax;
-        acc[3 * (size_t)o + 1] = ay;
-        acc[3 * (size_t)o + 2] = az;
-        if (kPot) phi[o] = ph;
-    }
-    if (kCount) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            c_p2p += __shfl_xor_sync(kFull, c_p2p, o);
-            c_open += __shfl_xor_sync(kFull, c_open, o);
-            c_m2p += __shfl_xor_sync(kFull, c_m2p, o);
-            c_vis += __shfl_xor_sync(kFull, c_vis, o);
-        }
-        if (lane == 0) {
-            atomicAdd(&counts[0], c_p2p);
-            atomicAdd(&counts[1], c_open);
-            atomicAdd(&counts[2], c_m2p);
-            atomicAdd(&counts[3], c_vis);
-        }
-    }
-}
-
-void launch_walk_mixed(const NodeF *rec, const float4 *thi, const float4 *tlo,
-                       const float4 *trel, const uint32_t *tid, uint32_t n, double theta,
-                       const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
-                       uint32_t *err, unsigned long long *counts, cudaStream_t st,
-                       double *phi) {
-    const uint32_t threads = kWalkWarps * 32;
-    const uint32_t blocks = (n + threads - 1) / threads;
-    const float theta2 = (float)(theta * theta);
-    if (phi)
-        k_walk_mixed<false, true><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n, theta2,
-                                                              b, heavy_ids, n_heavy, acc, phi,
-                                                              err, nullptr);
-    else if (counts)
-        k_walk_mixed<true, false><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n, theta2,
-                                                              b, heavy_ids, n_heavy, acc, nullptr,
-                                                              err, counts);
-    else
-        k_walk_mixed<false, false><<<blocks, threads, 0, st>>>(rec, thi, tlo, trel, tid, n,
-                                                               theta2, b, heavy_ids, n_heavy, acc,
-                                                               nullptr, err, nullptr);
 }
 
 // 0.5 m v^2 and 0.5 m phi summed per block in a fixed order (then on the host, in order).

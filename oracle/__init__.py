@@ -65,6 +65,8 @@ class Oracle:
             "orc_adjoint_direct": (C.c_int, [_vp, C.c_size_t, C.c_double, C.c_int64, _vp, _vp,
                                              _vp, _vp, _vp, _vp, _vp]),
             "orc_tree_jt": (C.c_int, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_double, _vp, _vp]),
+            "orc_tree_jt_group": (C.c_int, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_double, _vp,
+                                            _vp]),
             "orc_calc_accel_group": (C.c_int, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_double, _vp,
                                                _vp]),
             "orc_omp_threads": (C.c_int, []),
@@ -212,6 +214,17 @@ class Oracle:
         y = np.zeros((len(b), 3))
         if self.lib.orc_tree_jt(_p(b), len(b), _p(nodes), len(nodes), theta, _p(mu), _p(y)):
             raise RuntimeError("orc_tree_jt failed")
+        return y
+
+    def tree_jt_group(self, bodies, nodes, mu, theta: float = 0.3) -> np.ndarray:
+        """y = J^T mu over the grouped interaction set of the mixed path (FP64)."""
+        b = self._bodies(bodies)
+        nodes = np.ascontiguousarray(nodes, dtype=NODE)
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        y = np.zeros((len(b), 3))
+        if self.lib.orc_tree_jt_group(_p(b), len(b), _p(nodes), len(nodes), theta, _p(mu),
+                                      _p(y)):
+            raise RuntimeError("orc_tree_jt_group failed")
         return y
 
     def energy(self, bodies):

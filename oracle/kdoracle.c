@@ -803,6 +803,101 @@ int orc_tree_jt(const orc_particle *P, size_t n, const orc_node *nodes, size_t n
     return 0;
 }
 
+/* J^T mu over the grouped interaction set of the mixed path (the decisions of group_recur):
+ * per sink s and source c of mass m, w = T(x_s - c) mu_s; the sink gets -m w, a pair source
+ * j gets +m_j w, an accepted node's bodies get m_i w through Gn and jt_down. */
+static void jt_group_recur(size_t cur, const orc_particle *P, const orc_node *nodes,
+                           const uint64_t *sinks, size_t ns, const double lo[2][3],
+                           const double hi[2][3], double theta2, const double *mu, double *ys,
+                           double *y, double *Gn) {
+    const orc_node *nd = &nodes[cur];
+    if (nd->num_parts > 0) {
+        for (size_t k = 0; k < ns; ++k) {
+            const size_t p = (size_t)sinks[k];
+            for (uint64_t i = 0; i < nd->num_parts; ++i) {
+                const size_t j = (size_t)nd->particles[i];
+                if (j == p) continue;
+                double d[3] = {P[p].p[0] - P[j].p[0], P[p].p[1] - P[j].p[1],
+                               P[p].p[2] - P[j].p[2]};
+                double w[3];
+                tidal_w(d, &mu[3 * p], w);
+                for (int q = 0; q < 3; ++q) {
+                    ys[3 * k + q] -= P[j].m * w[q];
+#pragma omp atomic
+                    y[3 * j + q] += P[j].m * w[q];
+                }
+            }
+        }
+        return;
+    }
+    double e2 = box_dist2(nd->cm, lo[0], hi[0]);
+    const double f2 = box_dist2(nd->cm, lo[1], hi[1]);
+    if (f2 < e2) e2 = f2;
+    if (nd->size * nd->size < theta2 * e2) {
+        for (size_t k = 0; k < ns; ++k) {
+            const size_t p = (size_t)sinks[k];
+            double d[3] = {P[p].p[0] - nd->cm[0], P[p].p[1] - nd->cm[1], P[p].p[2] - nd->cm[2]};
+            double w[3];
+            tidal_w(d, &mu[3 * p], w);
+            for (int q = 0; q < 3; ++q) {
+                ys[3 * k + q] -= nd->m * w[q];
+#pragma omp atomic
+                Gn[3 * cur + q] += w[q];
+            }
+        }
+        return;
+    }
+    jt_group_recur(nd->left, P, nodes, sinks, ns, lo, hi, theta2, mu, ys, y, Gn);
+    jt_group_recur(nd->right, P, nodes, sinks, ns, lo, hi, theta2, mu, ys, y, Gn);
+}
+
+int orc_tree_jt_group(const orc_particle *P, size_t n, const orc_node *nodes, size_t n_nodes,
+                      double theta, const double *mu, double *y) {
+    double *Gn = (double *)calloc(3 * n_nodes, sizeof(double));
+    uint64_t *order = (uint64_t *)malloc(sizeof(uint64_t) * n);
+    size_t *gstart = (size_t *)malloc(sizeof(size_t) * (n + 1));
+    if (!Gn || !order || !gstart) {
+        free(Gn);
+        free(order);
+        free(gstart);
+        return -2;
+    }
+    memset(y, 0, 3 * n * sizeof(double));
+    const size_t ng = make_groups(nodes, n_nodes, order, gstart);
+    const double theta2 = theta * theta;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (size_t g = 0; g < ng; ++g) {
+        const uint64_t *sk = order + gstart[g];
+        const size_t ns = gstart[g + 1] - gstart[g];
+        const size_t sp = group_split(nodes, n, gstart[g], gstart[g + 1]) - gstart[g];
+        double lo[2][3], hi[2][3], ys[3 * 32];
+        for (int h = 0; h < 2; ++h)
+            for (int d = 0; d < 3; ++d) {
+                lo[h][d] = INFINITY;
+                hi[h][d] = -INFINITY;
+            }
+        for (size_t k = 0; k < ns; ++k) {
+            const int h = k < sp ? 0 : 1;
+            for (int d = 0; d < 3; ++d) {
+                if (P[sk[k]].p[d] < lo[h][d]) lo[h][d] = P[sk[k]].p[d];
+                if (P[sk[k]].p[d] > hi[h][d]) hi[h][d] = P[sk[k]].p[d];
+            }
+        }
+        for (size_t k = 0; k < 3 * ns; ++k) ys[k] = 0.0;
+        jt_group_recur(0, P, nodes, sk, ns, lo, hi, theta2, mu, ys, y, Gn);
+        for (size_t k = 0; k < ns; ++k)
+            for (int q = 0; q < 3; ++q) {
+#pragma omp atomic
+                y[3 * sk[k] + q] += ys[3 * k + q];
+            }
+    }
+    jt_down(0, P, nodes, Gn, 0.0, 0.0, 0.0, y);
+    free(Gn);
+    free(order);
+    free(gstart);
+    return 0;
+}
+
 int orc_omp_threads(void) { return max_threads(); }
 
 void orc_set_threads(int n) {

@@ -2,8 +2,8 @@
 
 * The transpose-Jacobian product of one step: with steps=1, dt=1 and dL/dv=0, the backward
   sweep returns g_x0 = r + J(x0)^T r for dL/dx = r, which is compared with the oracle's FP64
-  J^T r over the Barnes-Hut interaction set of the reference walk (its own exactness is
-  pinned at theta=0 against the direct-sum adjoint in tests/test_oracle_adjoint.py).
+  J^T r over the grouped interaction set of the mixed walk (the oracle's J^T is pinned at
+  theta=0 against the direct-sum adjoint in tests/test_oracle_adjoint.py).
 * Whole sweeps: against the oracle's FP64 direct-sum adjoint, and against central finite
   differences (h = 1e-6) of the GPU forward on seeded coordinates of v0.
 """
@@ -55,9 +55,9 @@ def test_one_step_jt_matches_oracle_tree(kd, oracle, theta):
     assert np.array_equal(gv, r)
     jt = gx - r
     nodes, _ = oracle.build_tree_dfs(b, leaf=7)
-    ref = oracle.tree_jt(b, nodes, r, theta)
+    ref = oracle.tree_jt_group(b, nodes, r, theta)
     e = rel_rows(jt, ref)
-    # FP32 arithmetic, and the rare node whose FP32 opening decision differs from FP64
+    # FP32 arithmetic, and the rare node whose FP32 group test differs from FP64
     assert np.sqrt(np.mean(e ** 2)) <= 1e-4, np.sqrt(np.mean(e ** 2))
     assert np.median(e) <= 1e-5, np.median(e)
 

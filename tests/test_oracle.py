@@ -158,3 +158,32 @@ def test_theta_zero_is_direct_sum(oracle):
     sinks = np.arange(len(b))
     direct = oracle.direct_accel(b, sinks)
     assert rel_err(acc, direct).max() <= 1e-12
+
+
+# ------------------------------------------------------------------ grouped walk (mixed path)
+
+def test_grouped_walk_theta_zero_is_direct_sum(oracle):
+    b = plummer(2000, seed=21)
+    nodes, _ = oracle.build_tree_dfs(b, leaf=7)
+    acc, cnt = oracle.calc_accel_group(b, nodes, 0.0)
+    ref = oracle.direct_accel(b, np.arange(len(b)))
+    assert rel_err(acc, ref).max() <= 1e-12
+    assert cnt["m2p"] == 0 and cnt["p2p"] == len(b) * (len(b) - 1)
+
+
+@pytest.mark.parametrize("gen,theta", [("ring", 0.3), ("plummer", 0.5)])
+def test_grouped_walk_refines_reference_walk(oracle, gen, theta):
+    """Every node the group test accepts passes the per-body test of every sink in the
+    group, so the grouped set holds at least as many terms per body and no larger overall
+    truncation error than the reference walk."""
+    n = 20_000
+    b = ring(n, seed=22) if gen == "ring" else plummer(n, seed=22)
+    nodes, _ = oracle.build_tree_dfs(b, leaf=7)
+    ag, cg = oracle.calc_accel_group(b, nodes, theta)
+    ab = oracle.calc_accel(b, nodes, theta)
+    sinks = np.arange(1, n, 7)
+    ref = oracle.direct_accel(b, sinks)
+    eg, eb = rel_err(ag[sinks], ref), rel_err(ab[sinks], ref)
+    assert np.sqrt(np.mean(eg ** 2)) <= np.sqrt(np.mean(eb ** 2))
+    pb = oracle.walk_counts(b, nodes, np.arange(n), theta)
+    assert cg["p2p"] + cg["m2p"] >= pb["p2p"] + pb["m2p"]
