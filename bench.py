@@ -226,8 +226,9 @@ def adjoint_timing(kd, bodies, a, dev):
     return {"steps": a.adjoint_steps, "forward_ms_per_step": fwd_ms / a.adjoint_steps,
             "backward_ms_per_step": bwd_ms / a.adjoint_steps,
             "adjoint_over_forward": bwd_ms / fwd_ms,
-            "note": "backward = recompute of the checkpoint segment + rebuild + "
-                    "transpose-Jacobian walk per step; loss = mean |x_T - R_z(1) x_0|^2"}
+            "note": "backward = recompute of each checkpoint segment but the last (whose "
+                    "positions the forward keeps) + rebuild + transpose-Jacobian walk per "
+                    "step; loss = mean |x_T - R_z(1) x_0|^2"}
 
 
 def pinned_bodies(n):

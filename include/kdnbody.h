@@ -199,10 +199,13 @@ int kd_direct_accel(kd_ctx *ctx, const uint64_t *sinks, size_t ns, double *acc);
  * checkpoint of (x, v) every `ckpt_every` steps in device memory; kd_backward takes the
  * gradient of a loss with respect to the final positions and velocities (host, 3*n each,
  * dL_dv may be NULL for zero) and returns the gradients with respect to the initial ones
- * (host, 3*n each).  Each checkpoint segment is recomputed forward, then walked back step
- * by step: mu = lv + dt*lx; lv = mu; lx += dt * J(x_n)^T mu, J = da/dx over the interaction
- * set of the forward walk (tidal tensors; node sources pushed down to their bodies with
- * weight m_i/M).  The bodies are left at the final state.  A tape may be consumed by
+ * (host, 3*n each).  Each checkpoint segment is recomputed forward (except the last, whose
+ * positions the forward sweep leaves in the context while no later sweep has replaced them),
+ * then walked back step by step: mu = lv + dt*lx; lv = mu; lx += dt * J(x_n)^T mu,
+ * J = da/dx over the interaction set of the forward walk (tidal tensors; node sources pushed
+ * down to their bodies with weight m_i/M).  Device memory: 48 B per body per checkpoint
+ * plus 24 B per body per step of one segment.  The bodies are left at the final state.  A
+ * tape may be consumed by
  * several kd_backward calls; kd_tape_free releases it.  No counterpart in the reference
  * (which has no derivatives); it differentiates simple_sim (array_kd_tree.rs:623-664). */
 int kd_forward(kd_ctx *ctx, double dt, int64_t steps, int64_t ckpt_every, kd_tape **tape);

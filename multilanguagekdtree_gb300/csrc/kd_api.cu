@@ -235,6 +235,9 @@ struct kd_ctx {
     int64_t adj_every = 0;
     double *lx = nullptr, *lv = nullptr, *amu = nullptr, *ay = nullptr, *ysink = nullptr,
            *yheavy = nullptr, *segbuf = nullptr;
+    // segbuf holds the positions of the last checkpoint segment of tape seg_owner (as the
+    // forward sweep left them), or nothing (0)
+    uint64_t tapes = 0, seg_owner = 0;
     double *aU = nullptr, *aG = nullptr;
 
     int fail(int code, const char *fmt, ...) {
@@ -505,6 +508,7 @@ int accept_bodies(kd_ctx *c) {
 
 struct kd_tape_impl {
     kd_ctx *ctx;
+    uint64_t gen;  // the context's tape number: names the owner of the segment buffer
     double dt;
     int64_t steps, every;
     std::vector<double *> ck;  // per checkpoint: x|y|z|vx|vy|vz (6n)
@@ -543,6 +547,7 @@ int adj_alloc(kd_ctx *c, int64_t every) {
         c->segbuf = nullptr;
     }
     KD_CHECK(c, c->alloc(&c->segbuf, 3 * n * (size_t)every));
+    c->seg_owner = 0;
     c->adj_every = every;
     c->adj_ready = true;
     return KD_OK;
@@ -1065,6 +1070,7 @@ int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape 
     kd_tape_impl *t = new (std::nothrow) kd_tape_impl();
     if (!t) return c->fail(KD_ENOMEM, "out of host memory");
     t->ctx = c;
+    t->gen = ++c->tapes;
     t->dt = dt;
     t->steps = steps;
     t->every = ckpt_every;
@@ -1082,11 +1088,23 @@ int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape 
         return c->cuda_fail(e, "checkpoint allocation");
     }
     c->launches = 0;
+    // the last segment's positions stay in segbuf, so the backward sweep need not recompute
+    // that segment (the forward is deterministic: they are the positions it would recompute)
+    const int64_t last0 = ((steps - 1) / ckpt_every) * ckpt_every;
+    const size_t n = c->n;
+    double *pos[3] = {c->bodies.x, c->bodies.y, c->bodies.z};
+    c->seg_owner = 0;
     KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
     for (int64_t s = 0; s < steps; ++s) {
         if (s % ckpt_every == 0) {
             rc = copy_state(c, t->ck[(size_t)(s / ckpt_every)], true);
             if (rc) break;
+        }
+        if (s >= last0) {
+            double *dst = c->segbuf + 3 * n * (size_t)(s - last0);
+            for (int k = 0; k < 3; ++k)
+                KD_CHECK(c, cudaMemcpyAsync(dst + k * n, pos[k], n * sizeof(double),
+                                            cudaMemcpyDeviceToDevice, c->st));
         }
         enqueue_step(c, dt);
     }
@@ -1098,6 +1116,7 @@ int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape 
         return rc;
     }
     c->has_tree = false;
+    c->seg_owner = t->gen;
     c->stats = kd_stats{};
     c->stats.total_ms = elapsed(c->ev[0], c->ev[1]);
     c->stats.steps = (uint64_t)steps;
@@ -1157,10 +1176,14 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
     double *pos[3] = {c->bodies.x, c->bodies.y, c->bodies.z};
     for (int64_t seg = nseg - 1; seg >= 0 && !rc; --seg) {
         const int64_t n0 = seg * t->every, n1 = std::min(t->steps, n0 + t->every);
-        rc = copy_state(c, t->ck[(size_t)seg], false);
-        if (rc) break;
+        const bool kept = seg == nseg - 1 && c->seg_owner == t->gen;
+        if (!kept) {
+            c->seg_owner = 0;
+            rc = copy_state(c, t->ck[(size_t)seg], false);
+            if (rc) break;
+        }
         // recompute the segment forward, keeping the positions at the start of every step
-        for (int64_t s = n0; s < n1; ++s) {
+        for (int64_t s = n0; s < n1 && !kept; ++s) {
             double *dst = c->segbuf + 3 * n * (size_t)(s - n0);
             for (int k = 0; k < 3; ++k)
                 KD_CHECK(c, cudaMemcpyAsync(dst + k * n, pos[k], n * sizeof(double),

@@ -276,17 +276,20 @@ __device__ __forceinline__ void sum_list(const float4 *list, uint32_t nl, float 
     }
 }
 
-// w = |d|^-3 (mu - 3 (d . mu) |d|^-2 d), d = sink - source: the tidal tensor times mu.
-__device__ __forceinline__ void tidal_w(float dx, float dy, float dz, float mx, float my,
-                                        float mz, float &wx, float &wy, float &wz) {
+// w = |d|^-3 (mu - 3 (d . mu) |d|^-2 d), d = sink - source: the tidal tensor times mu,
+// returned as the factor inv3 = |d|^-3 and the vector v = w / inv3.
+__device__ __forceinline__ void tidal_v(float dx, float dy, float dz, float mx, float my,
+                                        float mz, float &inv3, float &vx, float &vy,
+                                        float &vz) {
     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float inv = rsqrt_ftz(d2);
-    const float inv2 = inv * inv, inv3 = inv2 * inv;
+    const float inv2 = inv * inv;
+    inv3 = inv2 * inv;
     const float dm = fmaf(dx, mx, fmaf(dy, my, dz * mz));
     const float c3 = 3.0f * dm * inv2;
-    wx = inv3 * fmaf(-c3, dx, mx);
-    wy = inv3 * fmaf(-c3, dy, my);
-    wz = inv3 * fmaf(-c3, dz, mz);
+    vx = fmaf(-c3, dx, mx);
+    vy = fmaf(-c3, dy, my);
+    vz = fmaf(-c3, dz, mz);
 }
 
 // Adjoint terms of 32 sources (padding sources far away with zero mass) against the warp's
@@ -306,14 +309,15 @@ __device__ __forceinline__ void rotate32(int lane, float mx, float my, float mz,
         for (int k = k0; k < k0 + 8; ++k) {
             float dx, dy, dz;
             const float m = pair((lane + k) & 31, dx, dy, dz);
-            float wx, wy, wz;
-            tidal_w(dx, dy, dz, mx, my, mz, wx, wy, wz);
-            px = fmaf(-m, wx, px);
-            py = fmaf(-m, wy, py);
-            pz = fmaf(-m, wz, pz);
-            ax = __shfl_sync(kFull, ax + wx, up);
-            ay = __shfl_sync(kFull, ay + wy, up);
-            az = __shfl_sync(kFull, az + wz, up);
+            float inv3, vx, vy, vz;
+            tidal_v(dx, dy, dz, mx, my, mz, inv3, vx, vy, vz);
+            const float sm = -m * inv3;
+            px = fmaf(sm, vx, px);
+            py = fmaf(sm, vy, py);
+            pz = fmaf(sm, vz, pz);
+            ax = __shfl_sync(kFull, fmaf(inv3, vx, ax), up);
+            ay = __shfl_sync(kFull, fmaf(inv3, vy, ay), up);
+            az = __shfl_sync(kFull, fmaf(inv3, vz, az), up);
         }
         kahan(sum[0], comp[0], px);
         kahan(sum[1], comp[1], py);

@@ -130,3 +130,20 @@ def test_adjoint_needs_mixed_precision(kd):
         s.set_bodies(b)
         with pytest.raises(kd.KDError):
             s.forward(1e-3, 2, 1)
+
+
+def test_kept_last_segment_matches_recompute(kd):
+    """The forward sweep leaves its last segment's positions for the backward sweep; once
+    another sweep has replaced them the segment is recomputed, with the same gradients."""
+    n = 3000
+    b = kd.plummer(n, seed=12)
+    r = np.random.default_rng(3).normal(size=(n, 3))
+    with kd.KDTreeSim(n, leaf_size=7, precision="mixed", theta=0.5) as s:
+        s.set_bodies(b)
+        with s.forward(1e-3, 10, 32) as ta:
+            gx1, gv1 = ta.backward(r)           # last segment kept from the forward
+            with s.forward(1e-3, 10, 32):       # replaces the kept positions
+                pass
+            gx2, gv2 = ta.backward(r)           # recomputed from the checkpoint
+    assert np.allclose(gx1, gx2, rtol=1e-9, atol=1e-12 * np.abs(gx1).max())
+    assert np.allclose(gv1, gv2, rtol=1e-9, atol=1e-12 * np.abs(gv1).max())
