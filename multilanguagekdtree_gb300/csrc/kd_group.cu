@@ -197,9 +197,12 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
         nl += __popc(am);
         if (kCount) cnt[1] += __popc(am);
         // reached leaves: their bodies, the group's own leaves into their own list
+        // one scan for both counts: far-leaf bodies in the low half, own in the high half
+        // (each total is at most 32 * 8)
         const uint32_t fc = far ? ab.y : 0u, oc = mine ? ab.y : 0u;
-        const uint32_t fi = warp_incl_scan(fc, lane), oi = warp_incl_scan(oc, lane);
-        const uint32_t ft = __shfl_sync(kFull, fi, 31), ot = __shfl_sync(kFull, oi, 31);
+        const uint32_t pi = warp_incl_scan(fc | (oc << 16), lane);
+        const uint32_t pt = __shfl_sync(kFull, pi, 31);
+        const uint32_t fi = pi & 0xffffu, oi = pi >> 16, ft = pt & 0xffffu, ot = pt >> 16;
         if (far) {
             // all member loads of the leaf in flight at once (leaf size <= 8)
             float4 t[8];
@@ -328,7 +331,7 @@ __device__ __forceinline__ void rotate32(int lane, float mx, float my, float mz,
 }  // namespace
 
 template <bool kCount, bool kPot>
-__global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
+__global__ __launch_bounds__(kGroupWarps * 32, 5) void k_walk_group(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
     const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
     const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,

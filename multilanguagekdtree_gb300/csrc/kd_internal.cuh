@@ -217,7 +217,7 @@ void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, u
 // order, boxed in two parts split at gsplit[g]; stk_cap = per-warp stack entries (a multiple
 // of 32).
 constexpr int kGroupWarps = 4;
-constexpr int kGroupFlush = 256;
+constexpr int kGroupFlush = 128;
 constexpr int kGroupListCap = kGroupFlush + 32 * 8;
 // shared memory of one warp: interaction list, own-leaf list (split positions), stack
 __host__ __device__ inline uint32_t group_warp_bytes(uint32_t stk_cap) {
