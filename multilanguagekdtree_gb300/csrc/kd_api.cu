@@ -371,6 +371,14 @@ int setup(kd_ctx *c) {
     KD_CHECK(c, c->alloc(&c->d_total, 1));
     KD_CHECK(c, c->alloc(&c->gen_scratch, 6 * 256));
     KD_CHECK(c, cudaMemset(c->dev_err, 0, sizeof(uint32_t)));
+    // the build's ping-pong buffers start as valid bodies (id 0 at the origin), so a slot a
+    // failed select leaves unwritten never holds an out-of-range id
+    for (int k = 0; k < 2; ++k) {
+        KD_CHECK(c, cudaMemset(c->work.x[k], 0, n * sizeof(double)));
+        KD_CHECK(c, cudaMemset(c->work.y[k], 0, n * sizeof(double)));
+        KD_CHECK(c, cudaMemset(c->work.z[k], 0, n * sizeof(double)));
+        KD_CHECK(c, cudaMemset(c->work.id[k], 0, n * sizeof(uint32_t)));
+    }
     KD_CHECK(c, cudaMemset(c->nout.split_dim, 0, nn));
     KD_CHECK(c, cudaMemset(c->nout.split_val, 0, nn * sizeof(double)));
     KD_CHECK(c, cudaMemset(c->nout.size, 0, nn * sizeof(double)));

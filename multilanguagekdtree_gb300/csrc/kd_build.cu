@@ -783,7 +783,7 @@ struct LocalSmem {
     uint32_t cid[kLocalWarps][32];
     // internal sub-segments of every level, appended level after level
     uint32_t tab_id[kLocalMax];
-    uint16_t tab_st[kLocalMax], tab_cn[kLocalMax];
+    uint16_t tab_st[kLocalMax], tab_cn[kLocalMax], tab_pcn[kLocalMax];
     uint16_t perm[kLocalMax], perm2[kLocalMax];
     uint16_t clid[kLocalWarps][32];
     uint32_t lvl_off[kLocalLevels + 1];
@@ -883,6 +883,98 @@ __device__ __forceinline__ void load_moments(const Moments &mo, uint32_t id, dou
     v[3] = mo.S[3 * (size_t)id + 2];
 }
 
+// Whole subtree of a node of cn <= 32 bodies (tree positions [st, st+cn) of the block) in
+// one warp: lane k holds one body; its rank among the cn bodies in each dimension, by
+// (ordered key, id) as the exact select orders them, is counted once.  Then every internal
+// node of the subtree takes O(1) warp instructions: bounding box from the lanes of minimum
+// and maximum rank, split by choose_split, median = the member of rank-order position c/2
+// (the (c/2+1)-th set bit of the members' rank mask), and the new tree positions are the
+// members' positions in rank order of the split dimension (the left half below the median,
+// as the exact select and partition of the larger nodes give).  Writes split_dim, size,
+// split_val of the internal nodes and the subtree's final order into perm.
+__device__ __forceinline__ void small_subtree(LocalSmem &S, const Topology &t, const NodeOut &no,
+                                           uint32_t st, uint32_t cn, uint32_t nid,
+                                           uint32_t leaf, int lane, uint32_t *err) {
+    const bool valid = (uint32_t)lane < cn;
+    const uint32_t l = valid ? S.perm[st + lane] : 0u;
+    const double c[3] = {S.x[l], S.y[l], S.z[l]};
+    const unsigned long long k[3] = {ord_key(c[0]), ord_key(c[1]), ord_key(c[2])};
+    const uint32_t id = S.id[l];
+    uint32_t rank[3] = {0u, 0u, 0u};
+    for (uint32_t j = 0; j < cn; ++j) {
+        const uint32_t idj = __shfl_sync(kFull, id, j);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const unsigned long long kj = __shfl_sync(kFull, k[d], j);
+            rank[d] += (kj < k[d] || (kj == k[d] && idj < id)) ? 1u : 0u;
+        }
+    }
+    uint32_t pos = (uint32_t)lane;  // position in the subtree
+    // stack of internal nodes still to split, entry q in lane q: (first position, count, id)
+    uint32_t ss = 0u, sc = cn, si = nid;
+    int sp = cn > leaf ? 1 : 0;
+    while (sp > 0) {
+        --sp;
+        const uint32_t ns = __shfl_sync(kFull, ss, sp), nc = __shfl_sync(kFull, sc, sp),
+                       ni = __shfl_sync(kFull, si, sp);
+        const bool mem = valid && pos >= ns && pos < ns + nc;
+        double mn[3], mx[3];
+        uint32_t sel[3] = {0u, 0u, 0u};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const uint32_t rlo = __reduce_min_sync(kFull, mem ? rank[d] : 0xffffffffu);
+            const uint32_t rhi = __reduce_max_sync(kFull, mem ? rank[d] : 0u);
+            const int llo = __ffs(__ballot_sync(kFull, mem && rank[d] == rlo)) - 1;
+            const int lhi = __ffs(__ballot_sync(kFull, mem && rank[d] == rhi)) - 1;
+            mn[d] = ord_val(__shfl_sync(kFull, k[d], llo));
+            mx[d] = ord_val(__shfl_sync(kFull, k[d], lhi));
+            sel[d] = __reduce_or_sync(kFull, mem ? (1u << rank[d]) : 0u);
+        }
+        uint32_t sd;
+        double size;
+        choose_split(mn, mx, sd, size);
+        const uint32_t B = sd == 0 ? sel[0] : (sd == 1 ? sel[1] : sel[2]);
+        const uint32_t rs = sd == 0 ? rank[0] : (sd == 1 ? rank[1] : rank[2]);
+        const uint32_t half = nc / 2;
+        // rank value of the median: the (half+1)-th smallest rank among the members
+        const uint32_t rmed = __fns(B, 0u, (int)half + 1);
+        const int ml = __ffs(__ballot_sync(kFull, mem && rs == rmed)) - 1;
+        if (ml < 0 || rmed > 31u) {
+            if (lane == 0) atomicOr(err, kErrSelect);
+            break;
+        }
+        const double cs = sd == 0 ? c[0] : (sd == 1 ? c[1] : c[2]);
+        const double sv = __shfl_sync(kFull, cs, ml);
+        if (lane == 0) {
+            no.split_dim[ni] = (uint8_t)sd;
+            no.size[ni] = size;
+            no.split_val[ni] = sv;
+        }
+        // members in rank order of the split dimension: the left half lies below the median
+        if (mem) pos = ns + (uint32_t)__popc(B & ((1u << rs) - 1u));
+        const uint32_t rc = nc - half;
+        if (rc > leaf) {  // at most one pending entry per depth: sp stays below 32
+            if (lane == sp) {
+                ss = ns + half;
+                sc = rc;
+                si = ni + 1u + t.ttab[half];
+            }
+            ++sp;
+        }
+        if (half > leaf) {
+            if (lane == sp) {
+                ss = ns;
+                sc = half;
+                si = ni + 1u;
+            }
+            ++sp;
+        }
+    }
+    __syncwarp();
+    if (valid) S.perm[st + pos] = (uint16_t)l;
+    __syncwarp();
+}
+
 __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint32_t *roots,
                                                          NodeOut no, const double *wx,
                                                          const double *wy, const double *wz,
@@ -909,6 +1001,7 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
         const uint32_t g0 = c0 > leaf ? 1u : 0u;
         S.tab_st[0] = 0;
         S.tab_cn[0] = (uint16_t)c0;
+        S.tab_pcn[0] = 0xffffu;
         S.tab_id[0] = root;
         S.lvl_off[0] = 0;
         S.lvl_off[1] = g0;
@@ -922,6 +1015,12 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
         if (hi == lo) break;
         for (uint32_t i = lo + warp; i < hi; i += kLocalWarps) {
             const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
+            if (cn <= 32u) {
+                // the whole subtree of a node of <= 32 bodies in one warp's registers; its
+                // descendants (parent also <= 32) were done with it
+                if (S.tab_pcn[i] > 32u) small_subtree(S, t, no, st, cn, nid, leaf, lane, err);
+                continue;
+            }
             // ---- 1. bounding box and split
             unsigned long long kmn[3] = {~0ull, ~0ull, ~0ull}, kmx[3] = {0ull, 0ull, 0ull};
             for (uint32_t k = lane; k < cn; k += 32) {
@@ -1068,9 +1167,14 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
                 offL += __popc(bl);
                 offR += __popc(br);
             }
-            if (offL != mid && lane == 0) atomicOr(err, kErrSelect);
+            // an inexact split (a failed select) leaves perm2 partly unwritten: keep perm, a
+            // valid permutation, and report the error
             __syncwarp();
-            for (uint32_t k = lane; k < cn; k += 32) S.perm[st + k] = S.perm2[st + k];
+            if (offL == mid) {
+                for (uint32_t k = lane; k < cn; k += 32) S.perm[st + k] = S.perm2[st + k];
+            } else if (lane == 0) {
+                atomicOr(err, kErrSelect);
+            }
             __syncwarp();
         }
         // ---- children that are still internal, appended as the next level
@@ -1080,10 +1184,11 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
         for (uint32_t base = 0; base < 2 * G; base += blockDim.x) {
             const uint32_t u = base + threadIdx.x;
             bool keep = false;
-            uint32_t cst = 0, ccn = 0, cid = 0;
+            uint32_t cst = 0, ccn = 0, cid = 0, pcn = 0;
             if (u < 2 * G) {
                 const uint32_t i = lo + (u >> 1);
                 const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], id = S.tab_id[i];
+                pcn = cn;
                 const uint32_t lc = cn / 2;
                 if (u & 1) {
                     cst = st + lc;
@@ -1110,6 +1215,7 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
                 if (slot < (uint32_t)kLocalMax) {
                     S.tab_st[slot] = (uint16_t)cst;
                     S.tab_cn[slot] = (uint16_t)ccn;
+                    S.tab_pcn[slot] = (uint16_t)pcn;
                     S.tab_id[slot] = cid;
                 }
             }

@@ -17,9 +17,16 @@ __device__ __forceinline__ dbl4 ldg_dbl4(const dbl4 *p) {
 }
 
 // ---------------------------------------------------------------- tuning constants
-constexpr int kLocalMax = 1024;     // segments this small finish their whole subtree in
-                                    // one thread block, in shared memory
-constexpr int kLocalThreads = 256;
+// Segments of at most kLocalMax bodies finish their whole subtree in one thread block of
+// kLocalThreads threads, in shared memory (tunable at compile time).
+#ifndef KD_LOCAL_MAX
+#define KD_LOCAL_MAX 1024
+#endif
+#ifndef KD_LOCAL_THREADS
+#define KD_LOCAL_THREADS 256
+#endif
+constexpr int kLocalMax = KD_LOCAL_MAX;
+constexpr int kLocalThreads = KD_LOCAL_THREADS;
 constexpr int kTile = 2048;         // elements per block in the multi-block level passes
 constexpr int kTileThreads = 256;
 constexpr int kHistBits = 12;       // radix digit of the median select
