@@ -301,3 +301,31 @@ def test_energy_matches_direct_sum(kd, oracle, gen, theta, tol):
     rke, rpe = oracle.energy(b)
     assert ke == pytest.approx(rke, rel=1e-12)
     assert pe == pytest.approx(rpe, rel=tol)
+
+
+# ------------------------------------------------------------------ 1M-body FP64 run
+
+def test_fp64_1M_ring_100_steps_spot_checks(kd, oracle):
+    """The FP64 GPU path on the 1,000,000-body ring for 100 steps (theta 0.3, leaf 7, dt 1e-3,
+    PAR4 numbering).  At steps 0, 50 and 99 the oracle rebuilds the tree from the GPU's own
+    state: leaf membership bit-exact, accelerations within 1e-12."""
+    n = 1_000_000
+    b = kd.ring(n, seed=13)
+    with kd.KDTreeSim(n, leaf_size=7, layout="par4", precision="fp64", theta=0.3) as s:
+        s.set_bodies(b)
+        done = 0
+        for check in (0, 50, 99):
+            if check > done:
+                s.simple_sim(1e-3, check - done)
+                done = check
+            state = s.get_bodies()
+            s.build_tree()
+            nodes = s.nodes()
+            acc = s.calc_accel()
+            onodes = oracle.build_tree_par4(state, leaf=7)
+            assert set(leaf_sets(nodes).values()) == set(leaf_sets(onodes).values()), check
+            oacc, absum = oracle.calc_accel_abs(state, onodes, 0.3)
+            assert_accel_close(acc, oacc, absum)
+        s.simple_sim(1e-3, 100 - done)
+        final = s.get_bodies()
+    assert np.isfinite(final["p"]).all() and np.isfinite(final["v"]).all()
