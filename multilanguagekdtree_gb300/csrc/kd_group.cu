@@ -155,20 +155,23 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
     nown = 0;
     if (lane == 0) W.stk[0] = 0u;
     __syncwarp();
-    while (top > 0) {
-        const uint32_t take = min(top, 32u);
-        const bool has = (uint32_t)lane < take;
-        const uint32_t node = has ? W.stk[top - 1 - lane] : 0u;
-        top -= take;
-        __syncwarp();
+    // Software-pipelined: a wave's children are pushed as soon as its tests are done, and
+    // the next wave's records are requested before this wave's list entries are written and
+    // the list is flushed, so their latency overlaps that work.  The order of tests and of
+    // list entries is the same as popping and loading at the top of each wave.
+    uint32_t take = 1u;
+    bool has = lane == 0;
+    uint32_t node = 0u;
+    top = 0u;
+    float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
+    uint2 ab = make_uint2(0u, 0u);
+    if (has) {
+        h = __ldg(&rec[0].hi);
+        l = __ldg(&rec[0].lo);
+        ab = __ldg(reinterpret_cast<const uint2 *>(&rec[0].a));
+    }
+    while (take > 0) {
         if (kCount) cnt[2] += take;
-        float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
-        uint2 ab = make_uint2(0u, 0u);
-        if (has) {
-            h = __ldg(&rec[node].hi);
-            l = __ldg(&rec[node].lo);
-            ab = __ldg(reinterpret_cast<const uint2 *>(&rec[node].a));
-        }
         const bool leaf = ab.y != 0u;
         // centre of mass (leaf: its first body) in the group frame
         const float cx = (h.x - G.ohx) + (l.x - G.olx);
@@ -187,6 +190,32 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
         const bool mine = has && leaf && ab.x >= G.g0 && ab.x < G.g1;
         const bool far = has && leaf && !mine;
 
+        // opened nodes: both children, then the next wave's nodes and their records
+        const uint32_t om = __ballot_sync(kFull, open);
+        if (top + 2u * __popc(om) > stk_cap) {
+            if (lane == 0) atomicOr(err, kErrStack);
+            break;
+        }
+        if (open) {
+            const uint32_t slot = top + 2u * __popc(om & lt);
+            W.stk[slot] = ab.x;           // right child
+            W.stk[slot + 1] = node + 1u;  // left child
+        }
+        top += 2u * __popc(om);
+        __syncwarp();
+        const uint32_t ntake = min(top, 32u);
+        const bool nhas = (uint32_t)lane < ntake;
+        const uint32_t nnode = nhas ? W.stk[top - 1 - lane] : 0u;
+        top -= ntake;
+        __syncwarp();
+        float4 nh = make_float4(0.f, 0.f, 0.f, 0.f), nlo = nh;
+        uint2 nab = make_uint2(0u, 0u);
+        if (nhas) {
+            nh = __ldg(&rec[nnode].hi);
+            nlo = __ldg(&rec[nnode].lo);
+            nab = __ldg(reinterpret_cast<const uint2 *>(&rec[nnode].a));
+        }
+
         // accepted nodes: one entry each
         const uint32_t am = __ballot_sync(kFull, take_m);
         if (take_m) {
@@ -196,9 +225,9 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
         }
         nl += __popc(am);
         if (kCount) cnt[1] += __popc(am);
-        // reached leaves: their bodies, the group's own leaves into their own list
-        // one scan for both counts: far-leaf bodies in the low half, own in the high half
-        // (each total is at most 32 * 8)
+        // reached leaves: their bodies, the group's own leaves into their own list.  One
+        // scan for both counts: far-leaf bodies in the low half, own in the high half (each
+        // total is at most 32 * 8)
         const uint32_t fc = far ? ab.y : 0u, oc = mine ? ab.y : 0u;
         const uint32_t pi = warp_incl_scan(fc | (oc << 16), lane);
         const uint32_t pt = __shfl_sync(kFull, pi, 31);
@@ -227,24 +256,18 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
         nl += ft;
         nown = min(nown + ot, 32u);
         if (kCount) cnt[0] += ft;
-        // opened nodes: both children
-        const uint32_t om = __ballot_sync(kFull, open);
-        if (top + 2u * __popc(om) > stk_cap) {
-            if (lane == 0) atomicOr(err, kErrStack);
-            break;
-        }
-        if (open) {
-            const uint32_t slot = top + 2u * __popc(om & lt);
-            W.stk[slot] = ab.x;          // right child
-            W.stk[slot + 1] = node + 1u;  // left child
-        }
-        top += 2u * __popc(om);
         __syncwarp();
         if (nl >= (uint32_t)kGroupFlush) {
             flush(nl);
             nl = 0;
             __syncwarp();
         }
+        take = ntake;
+        has = nhas;
+        node = nnode;
+        h = nh;
+        l = nlo;
+        ab = nab;
     }
     __syncwarp();
     if (nl) flush(nl);
