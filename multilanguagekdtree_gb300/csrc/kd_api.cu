@@ -230,6 +230,13 @@ struct kd_ctx {
 
     std::vector<void *> owned;
 
+    // one step (build, walk, kick) as a CUDA graph: captured on first use, relaunched
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = 0.0;
+    int graph_prec = -1, graph_heavy = -1;
+    uint64_t graph_launches = 0;
+    bool graph_off = false;  // capture failed once: launch directly from then on
+
     // adjoint state, allocated by the first kd_forward
     bool adj_ready = false;
     int64_t adj_every = 0;
@@ -569,6 +576,48 @@ void enqueue_step(kd_ctx *c, double dt) {
     c->launches += 1;
 }
 
+// `steps` steps on the context's stream.  A step is a fixed launch sequence for a given n and
+// precision, so it is captured once into a CUDA graph and relaunched: one host call per step
+// instead of ~100.  The graph is recaptured when dt, the precision or the heavy-body count
+// (kernel arguments) change; counting and timing modes launch directly.
+void enqueue_steps(kd_ctx *c, double dt, int64_t steps) {
+    if (steps <= 0) return;
+    if (c->counting || c->timing || c->graph_off) {
+        for (int64_t s = 0; s < steps; ++s) enqueue_step(c, dt);
+        return;
+    }
+    if (!c->graph || c->graph_dt != dt || c->graph_prec != c->prm.precision ||
+        c->graph_heavy != c->n_heavy) {
+        if (c->graph) cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+        const uint64_t l0 = c->launches;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            enqueue_step(c, dt);
+            e = cudaStreamEndCapture(c->st, &g);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        c->graph_launches = c->launches - l0;
+        c->launches = l0;
+        if (e != cudaSuccess || !c->graph) {
+            cudaGetLastError();  // clear: fall back to direct launches
+            c->graph = nullptr;
+            c->graph_off = true;
+            for (int64_t s = 0; s < steps; ++s) enqueue_step(c, dt);
+            return;
+        }
+        c->graph_dt = dt;
+        c->graph_prec = c->prm.precision;
+        c->graph_heavy = c->n_heavy;
+    }
+    for (int64_t s = 0; s < steps; ++s) {
+        cudaGraphLaunch(c->graph, c->st);
+        c->launches += c->graph_launches;
+    }
+}
+
 namespace kd {
 void set_thread_error(const char *msg) { g_create_error = msg ? msg : ""; }
 }  // namespace kd
@@ -685,6 +734,7 @@ void kd_destroy(kd_ctx *c) {
     if (!c) return;
     cudaSetDevice(c->prm.device);
     if (c->st) cudaStreamSynchronize(c->st);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
     for (void *p : c->owned) cudaFree(p);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -1016,7 +1066,8 @@ int kd_simple_sim(kd_ctx *c, double dt, int64_t steps) {
     }
     c->launches = 0;
     KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
-    for (int64_t s = 0; s < steps; ++s) {
+    if (!c->timing) enqueue_steps(c, dt, steps);
+    for (int64_t s = 0; s < (c->timing ? steps : 0); ++s) {
         cudaEvent_t *e = c->timing ? &c->tev[5 * (size_t)s] : nullptr;
         if (e) KD_CHECK(c, cudaEventRecord(e[0], c->st));
         enqueue_build(c, !mixed, mixed);
@@ -1114,7 +1165,7 @@ int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape 
                 KD_CHECK(c, cudaMemcpyAsync(dst + k * n, pos[k], n * sizeof(double),
                                             cudaMemcpyDeviceToDevice, c->st));
         }
-        enqueue_step(c, dt);
+        enqueue_steps(c, dt, 1);
     }
     if (!rc) rc = copy_state(c, t->final_state, true);
     KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
@@ -1196,7 +1247,7 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
             for (int k = 0; k < 3; ++k)
                 KD_CHECK(c, cudaMemcpyAsync(dst + k * n, pos[k], n * sizeof(double),
                                             cudaMemcpyDeviceToDevice, c->st));
-            if (s + 1 < n1) enqueue_step(c, t->dt);
+            if (s + 1 < n1) enqueue_steps(c, t->dt, 1);
         }
         for (int64_t s = n1 - 1; s >= n0; --s) {
             const double *src = c->segbuf + 3 * n * (size_t)(s - n0);
