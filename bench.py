@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--workload", default="ring", choices=["ring", "plummer", "adjoint-check"],
                     help="ring: the headline line; plummer: the 2e7-body Plummer stress case; "
                          "adjoint-check: the 1e5-body, 1000-step gradient check")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="arithmetic of the headline step (the extras always measure both)")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="only one forward + reverse sweep of --adjoint-steps steps (profiling)")
     return ap.parse_args()
@@ -253,9 +255,9 @@ def run_ours(a, ws, rank, local):
         print(json.dumps(line))
         return
 
-    # ---- headline: mixed precision, bodies resident
-    sim = kd.KDTreeSim(n, leaf_size=a.leaf, layout="dfs", precision="mixed", theta=a.theta,
-                       dt=a.dt, device=dev)
+    # ---- headline: mixed precision (or --precision fp64), bodies resident
+    sim = kd.KDTreeSim(n, leaf_size=a.leaf, layout="dfs", precision=a.precision,
+                       theta=a.theta, dt=a.dt, device=dev)
     sim.set_bodies(bodies)
     sim.simple_sim(a.dt, a.warmup)
     clocks = ClockSampler(dev)
@@ -276,10 +278,12 @@ def run_ours(a, ws, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * t_max / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 (mixed)", "data": "synthetic",
-        "config": {"workload": f"ring N={n} theta={a.theta} leaf={a.leaf} dt={a.dt} mixed",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 (mixed)" if a.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": f"ring N={n} theta={a.theta} leaf={a.leaf} dt={a.dt} "
+                               f"{a.precision}",
                    "n_bodies": n, "leaf_size": a.leaf, "theta": a.theta, "dt": a.dt,
-                   "precision": "mixed", "parallelism": f"replicas x{ws}",
+                   "precision": a.precision, "parallelism": f"replicas x{ws}",
                    "l2": "inputs (640 MB of bodies, 1.1 GB with the tree) exceed the 129 MB "
                          "L2; no flush"},
         "gpu_launches": launches, "clocks": clk, "host_wall_s": host_s,
