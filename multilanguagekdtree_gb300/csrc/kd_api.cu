@@ -206,6 +206,7 @@ struct kd_ctx {
     NodeOut nout{};
     Moments mom{}, momf{};  // FP64 and light (mixed) moments
     NodeD *recd = nullptr;
+    NodeP *recp = nullptr;
     NodeF *recf = nullptr;
     dbl4 *tpos = nullptr;
     uint32_t *tid = nullptr;
@@ -366,6 +367,7 @@ int setup(kd_ctx *c) {
     KD_CHECK(c, c->alloc(&c->momf.S, 3 * nn));
     c->momf.counter = c->mom.counter;
     KD_CHECK(c, c->alloc(&c->recd, nn));
+    KD_CHECK(c, c->alloc(&c->recp, nn));
     KD_CHECK(c, c->alloc(&c->recf, nn));
     KD_CHECK(c, c->alloc(&c->tpos, n));
     KD_CHECK(c, c->alloc(&c->tid, n));
@@ -439,6 +441,7 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     o.mo = c->mom;
     o.mof = c->momf;
     o.recd = want_d ? c->recd : nullptr;
+    o.recp = c->recp;
     o.recf = want_f ? c->recf : nullptr;
     o.heavy = c->d_heavy;
     o.n_heavy = c->n_heavy;
@@ -456,7 +459,8 @@ void enqueue_walk(kd_ctx *c) {
                           c->n_groups, c->group_stack, c->prm.theta, c->bodies, c->d_heavy,
                           c->n_heavy, c->acc, c->dev_err, cnt, c->st);
     else
-        launch_walk_fp64(c->recd, c->tpos, c->tid, (uint32_t)c->n, c->prm.theta, c->acc,
+        launch_walk_fp64(c->recd, c->recp, c->thi, c->tlo, c->tpos, c->tid, (uint32_t)c->n,
+                         c->prm.theta, c->acc,
                          c->dev_err, cnt, c->st);
 }
 

@@ -1283,7 +1283,9 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
             const uint32_t right = nid + 1 + t.ttab[lc];
             if (want_d) {
                 store_moments(o.mo, nid, fs);
-                o.recd[nid] = make_noded(fs[0], fs[1], fs[2], fs[3], size, right, 0u);
+                const NodeD q = make_noded(fs[0], fs[1], fs[2], fs[3], size, right, 0u);
+                o.recd[nid] = q;
+                o.recp[nid] = make_nodep(q);
             }
             if (want_f) {
                 store_moments(o.mof, nid, gs);
@@ -1300,7 +1302,7 @@ __global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint3
         const double x = S.x[l], y = S.y[l], z = S.z[l], mm = S.m[l];
         o.tpos[s0 + k] = make_double4_32a(x, y, z, mm);
         o.tid[s0 + k] = id;
-        if (want_f) {
+        {
             const float hx = (float)x, hy = (float)y, hz = (float)z;
             const float fm = is_heavy(id, o.heavy, o.n_heavy) ? 0.0f : (float)mm;
             o.thi[s0 + k] = make_float4(hx, hy, hz, fm);
@@ -1347,7 +1349,9 @@ __global__ void k_moments_top(Topology t, const uint32_t *roots, uint32_t n_root
                 v[1 + d] = __dadd_rn(__ldcg(&o.mo.S[3 * (size_t)L + d]),
                                      __ldcg(&o.mo.S[3 * (size_t)R + d]));
             store_moments(o.mo, node, v);
-            o.recd[node] = make_noded(v[0], v[1], v[2], v[3], size, R, 0u);
+            const NodeD q = make_noded(v[0], v[1], v[2], v[3], size, R, 0u);
+            o.recd[node] = q;
+            o.recp[node] = make_nodep(q);
         }
         if (want_f) {
             double v[4];

@@ -57,6 +57,12 @@ struct __align__(16) NodeD {
 };
 static_assert(sizeof(NodeD) == 56 || sizeof(NodeD) == 64, "NodeD layout");
 
+// FP32 split of an internal node's FP64 centre of mass and size^2 (hi.w), for the FP64
+// walk's FP32 pre-test of the opening decision.
+struct __align__(16) NodeP {
+    float4 hi, lo;
+};
+
 // Walk record of the mixed path: centre of mass as hi+lo floats, size^2, light mass.  The
 // opening test reads only `hi` and `a, b`; an accepted node also reads `lo`.  A leaf record
 // holds instead its origin o (the position of its first body) as hi+lo floats; the bodies of
@@ -145,11 +151,12 @@ struct LocalOut {
     const double *mass;          // master masses, original order
     dbl4 *tpos;                  // bodies in tree order (x, y, z, m)
     uint32_t *tid;               // body index of every tree position
-    float4 *thi, *tlo;           // split coordinates, tree order (mixed records only)
+    float4 *thi, *tlo;           // split coordinates (hi.w: light mass), tree order
     float4 *trel;                // offset from the leaf origin, light mass (mixed only)
     Moments mo;                  // full-mass moments (FP64 records)
     Moments mof;                 // light-mass moments (mixed records)
     NodeD *recd;                 // FP64 walk records, or nullptr
+    NodeP *recp;                 // FP32 pre-test data of the FP64 records (with recd)
     NodeF *recf;                 // mixed walk records, or nullptr
     const uint32_t *heavy;       // bodies left out of the FP32 masses
     int n_heavy;
@@ -195,6 +202,15 @@ __device__ __forceinline__ NodeF make_nodef(double m, double sx, double sy, doub
     return r;
 }
 
+__device__ __forceinline__ NodeP make_nodep(const NodeD &q) {
+    NodeP p;
+    const float hx = (float)q.cmx, hy = (float)q.cmy, hz = (float)q.cmz;
+    p.hi = make_float4(hx, hy, hz, (float)q.size2);
+    p.lo = make_float4((float)(q.cmx - (double)hx), (float)(q.cmy - (double)hy),
+                       (float)(q.cmz - (double)hz), 0.0f);
+    return p;
+}
+
 void launch_init_work(const Bodies &b, Work &w, uint32_t n, cudaStream_t st);
 // quickselect set-up: key[i] = vals[idx[i]], id[i] = idx[i]; flags an index >= n_vals
 void launch_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx, uint32_t n,
@@ -217,7 +233,8 @@ void launch_moments_top(const Topology &t, const uint32_t *roots, uint32_t n_roo
                         const NodeOut &no, const LocalOut &out, cudaStream_t st);
 
 // ---------------------------------------------------------------- launchers (kd_walk.cu)
-void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
+void launch_walk_fp64(const NodeD *rec, const NodeP *recp, const float4 *thi,
+                      const float4 *tlo, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
                       double theta, double *acc, uint32_t *err,
                       unsigned long long *counts, cudaStream_t st);
 // Grouped mixed walk: groups of whole leaves, <= 32 bodies, gstart[g]..gstart[g+1] in tree

@@ -27,11 +27,56 @@ __device__ __forceinline__ void load_noded(const NodeD *rec, uint32_t node, doub
     b = ab.y;
 }
 
+// 1/sqrt(x) for x in [1e-30, 1e30]: the FP32 hardware estimate, then two Newton steps in
+// FP64 (quadratic convergence from ~2^-23 to a few ulp), in place of the reference's
+// sqrt and division: the interaction magnitude m / (d^2 sqrt(d^2)) = m r^3 differs from the
+// IEEE-rounded one by a few ulp.
+__device__ __forceinline__ double rsqrt64(double x) {
+    float f;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"((float)x));
+    const double h = 0.5 * x;
+    double y = (double)f;
+    y = y * fma(-h * y, y, 1.5);
+    y = y * fma(-h * y, y, 1.5);
+    return y;
+}
+
+// m / |d|^3 as the reference forms it (array_kd_tree.rs:607, array_particle.rs:72-73), or
+// by rsqrt64 when d2 is in its range; d2 = 0 keeps the reference's inf.
+__device__ __forceinline__ double inv_cube(double d2) {
+    if (d2 >= 1e-30 && d2 <= 1e30) {
+        const double r = rsqrt64(d2);
+        return (r * r) * r;
+    }
+    return __ddiv_rn(1.0, __dmul_rn(d2, __dsqrt_rn(d2)));
+}
+
+// FP32 pre-test of the opening decision size^2 < theta^2 d^2 (array_kd_tree.rs:606): on the
+// split (hi + lo) coordinates d^2 carries a relative error below 1e-6 once |d| exceeds
+// 1e-5 of the coordinates' magnitude, so a decision outside a 4e-6 relative margin is the
+// FP64 decision.  Returns 1 (accept), 0 (open) or -1 (undecided: test in FP64).
+__device__ __forceinline__ int pretest(const float4 &mh, const float4 &ml, float p2,
+                                       const NodeP &q, float theta2f) {
+    const float ex = (mh.x - q.hi.x) + (ml.x - q.lo.x);
+    const float ey = (mh.y - q.hi.y) + (ml.y - q.lo.y);
+    const float ez = (mh.z - q.hi.z) + (ml.z - q.lo.z);
+    const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+    const float scale = p2 + fmaf(q.hi.x, q.hi.x, fmaf(q.hi.y, q.hi.y, q.hi.z * q.hi.z));
+    const float rhs = theta2f * e2, lhs = q.hi.w;
+    const float margin = 4e-6f * (lhs + rhs);
+    const bool sure = e2 >= 1e-30f && e2 > 1e-10f * scale && scale < 1e37f && rhs < 1e37f;
+    if (sure && lhs < rhs - margin) return 1;
+    if (sure && lhs > rhs + margin) return 0;
+    return -1;
+}
+
 template <bool kCount>
 __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
-    const NodeD *__restrict__ rec, const dbl4 *__restrict__ tpos,
-    const uint32_t *__restrict__ tid, uint32_t n, double theta2, double *__restrict__ acc,
-    uint32_t *err, unsigned long long *counts) {
+    const NodeD *__restrict__ rec, const NodeP *__restrict__ recp,
+    const float4 *__restrict__ thi, const float4 *__restrict__ tlo,
+    const dbl4 *__restrict__ tpos, const uint32_t *__restrict__ tid, uint32_t n,
+    double theta2, float theta2f, double *__restrict__ acc, uint32_t *err,
+    unsigned long long *counts) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t s = (blockIdx.x * kWalkWarps + warp) * 32 + lane;
     const bool valid = s < n;
@@ -41,6 +86,9 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
     // traversal stack: entry k (pending right child, lanes still descending) lives in lane k
     uint32_t st_node = 0, st_mask = 0;
     dbl4 me = valid ? tpos[s] : make_double4_32a(0.0, 0.0, 0.0, 0.0);
+    const float4 mh = valid ? thi[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 ml = valid ? tlo[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float p2 = fmaf(mh.x, mh.x, fmaf(mh.y, mh.y, mh.z * mh.z));
     double ax = 0.0, ay = 0.0, az = 0.0;
     unsigned long long c_p2p = 0, c_open = 0, c_m2p = 0, c_vis = 0;
     uint32_t node = 0;
@@ -58,36 +106,37 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
                     const uint32_t j = a + k;
                     if (j == s) continue;
                     const dbl4 q = ldg_dbl4(&tpos[j]);
-                    const double dx = __dsub_rn(me.x, q.x);
-                    const double dy = __dsub_rn(me.y, q.y);
-                    const double dz = __dsub_rn(me.z, q.z);
-                    const double dp2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
-                                                 __dmul_rn(dz, dz));
-                    const double dist = __dsqrt_rn(dp2);
-                    const double magi = __ddiv_rn(-q.w, __dmul_rn(__dmul_rn(dist, dist), dist));
-                    ax = __dadd_rn(ax, __dmul_rn(magi, dx));
-                    ay = __dadd_rn(ay, __dmul_rn(magi, dy));
-                    az = __dadd_rn(az, __dmul_rn(magi, dz));
+                    const double dx = me.x - q.x, dy = me.y - q.y, dz = me.z - q.z;
+                    const double dp2 = fma(dx, dx, fma(dy, dy, dz * dz));
+                    const double magi = -q.w * inv_cube(dp2);
+                    ax = fma(magi, dx, ax);
+                    ay = fma(magi, dy, ay);
+                    az = fma(magi, dz, az);
                     if (kCount) ++c_p2p;
                 }
             }
         } else {
             bool take = false;
             if (mask & bit) {
-                const double dx = __dsub_rn(me.x, cx);
-                const double dy = __dsub_rn(me.y, cy);
-                const double dz = __dsub_rn(me.z, cz);
-                const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
-                                            __dmul_rn(dz, dz));
                 if (kCount) ++c_open;
-                if (s2 < __dmul_rn(theta2, d2)) {
-                    take = true;
-                    const double dist = __dsqrt_rn(d2);
-                    const double magi = __ddiv_rn(-m, __dmul_rn(d2, dist));
-                    ax = __dadd_rn(ax, __dmul_rn(dx, magi));
-                    ay = __dadd_rn(ay, __dmul_rn(dy, magi));
-                    az = __dadd_rn(az, __dmul_rn(dz, magi));
-                    if (kCount) ++c_m2p;
+                const NodeP q = recp[node];
+                const int pre = pretest(mh, ml, p2, q, theta2f);
+                if (pre != 0) {
+                    // the reference's d and d^2 (exact FP64 order): the test when the FP32
+                    // estimate is undecided, and the force either way
+                    const double dx = __dsub_rn(me.x, cx);
+                    const double dy = __dsub_rn(me.y, cy);
+                    const double dz = __dsub_rn(me.z, cz);
+                    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                __dmul_rn(dz, dz));
+                    take = pre == 1 || s2 < __dmul_rn(theta2, d2);
+                    if (take) {
+                        const double magi = -m * inv_cube(d2);
+                        ax = fma(dx, magi, ax);
+                        ay = fma(dy, magi, ay);
+                        az = fma(dz, magi, az);
+                        if (kCount) ++c_m2p;
+                    }
                 }
             }
             const uint32_t open = mask & ~__ballot_sync(kFull, take);
@@ -135,17 +184,20 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
     }
 }
 
-void launch_walk_fp64(const NodeD *rec, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
+void launch_walk_fp64(const NodeD *rec, const NodeP *recp, const float4 *thi,
+                      const float4 *tlo, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
                       double theta, double *acc, uint32_t *err, unsigned long long *counts,
                       cudaStream_t st) {
     const uint32_t threads = kWalkWarps * 32;
     const uint32_t blocks = (n + threads - 1) / threads;
     const double theta2 = theta * theta;  // THETA * THETA is formed first (array_kd_tree.rs:606)
+    const float theta2f = (float)theta2;
     if (counts)
-        k_walk_fp64<true><<<blocks, threads, 0, st>>>(rec, tpos, tid, n, theta2, acc, err, counts);
+        k_walk_fp64<true><<<blocks, threads, 0, st>>>(rec, recp, thi, tlo, tpos, tid, n, theta2,
+                                                      theta2f, acc, err, counts);
     else
-        k_walk_fp64<false><<<blocks, threads, 0, st>>>(rec, tpos, tid, n, theta2, acc, err,
-                                                       nullptr);
+        k_walk_fp64<false><<<blocks, threads, 0, st>>>(rec, recp, thi, tlo, tpos, tid, n, theta2,
+                                                       theta2f, acc, err, nullptr);
 }
 
 // 0.5 m v^2 and 0.5 m phi summed per block in a fixed order (then on the host, in order).
