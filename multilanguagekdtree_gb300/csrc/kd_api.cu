@@ -377,7 +377,7 @@ int setup(kd_ctx *c) {
     KD_CHECK(c, c->alloc(&c->d_counts, 4));
     KD_CHECK(c, c->alloc(&c->d_heavy, kMaxHeavy));
     KD_CHECK(c, c->alloc(&c->d_nheavy, 1));
-    KD_CHECK(c, c->alloc(&c->d_total, 1));
+    KD_CHECK(c, c->alloc(&c->d_total, 1 + 304));  // total mass + per-block partials
     KD_CHECK(c, c->alloc(&c->gen_scratch, 6 * 256));
     KD_CHECK(c, cudaMemset(c->dev_err, 0, sizeof(uint32_t)));
     // the build's ping-pong buffers start as valid bodies (id 0 at the origin), so a slot a

@@ -264,6 +264,8 @@ constexpr uint32_t kDirectChunk = 1u << 18;
 constexpr int kDirectThreads = 128;
 void launch_direct(const Bodies &b, uint32_t n, const uint64_t *sinks, uint32_t ns,
                    double *partial, double *acc, cudaStream_t st);
+// Heavy bodies (m >= frac * total mass, at most kMaxHeavy listed); scratch_total holds the
+// total mass followed by 304 per-block partial sums.
 void launch_find_heavy(const Bodies &b, uint32_t n, double frac, double *scratch_total,
                        uint32_t *heavy_ids, uint32_t *n_heavy, uint32_t *err, cudaStream_t st);
 

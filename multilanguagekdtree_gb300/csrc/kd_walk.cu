@@ -372,17 +372,31 @@ void launch_direct(const Bodies &b, uint32_t n, const uint64_t *sinks, uint32_t 
 
 // Total mass in a fixed reduction order (one block), then every body at or above
 // frac * total is listed (unordered; the host sorts the short list).
-__global__ __launch_bounds__(1024) void k_total_mass(const double *m, uint32_t n, double *out) {
-    __shared__ double red[32];
+// Total mass in a fixed order: per-block partial sums over a fixed grid, then one block
+// adds the partials in block order (deterministic for a given n).
+constexpr int kMassBlocks = 304;
+
+__global__ __launch_bounds__(256) void k_mass_partial(const double *m, uint32_t n,
+                                                      double *part) {
+    __shared__ double red[8];
     double s = 0.0;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += m[i];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        s += m[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        for (int w = 0; w < 8; ++w) t += red[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_mass_total(const double *part, int nblk, double *out) {
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < nblk; ++q) t += part[q];
         *out = t;
     }
 }
@@ -403,7 +417,8 @@ void launch_find_heavy(const Bodies &b, uint32_t n, double frac, double *scratch
                        uint32_t *heavy_ids, uint32_t *n_heavy, uint32_t *err, cudaStream_t st) {
     (void)err;
     cudaMemsetAsync(n_heavy, 0, sizeof(uint32_t), st);
-    k_total_mass<<<1, 1024, 0, st>>>(b.m, n, scratch_total);
+    k_mass_partial<<<kMassBlocks, 256, 0, st>>>(b.m, n, scratch_total + 1);
+    k_mass_total<<<1, 32, 0, st>>>(scratch_total + 1, kMassBlocks, scratch_total);
     int blocks = (int)((n + 255) / 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
     k_heavy<<<blocks, 256, 0, st>>>(b.m, n, frac, scratch_total, heavy_ids, n_heavy);
