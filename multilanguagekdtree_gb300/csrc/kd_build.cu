@@ -321,11 +321,13 @@ __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
 // Block-wide search of the histogram bin holding rank r.  Every thread owns
 // kHistBins/blockDim consecutive bins.  Returns digit / count below / count in bin through
 // shared memory.
-__device__ void find_bin(const uint32_t *h, uint32_t r, uint32_t *out3) {
-    const int per = kHistBins / blockDim.x;
+__device__ void find_bin(const uint32_t *h, uint32_t r, uint32_t *out3,
+                         uint32_t nb = kHistBins) {
+    const int per = nb >= blockDim.x ? (int)(nb / blockDim.x) : 1;
     __shared__ uint32_t wsum[32];
     uint32_t mine = 0;
-    for (int i = 0; i < per; ++i) mine += h[threadIdx.x * per + i];
+    for (int i = 0; i < per; ++i)
+        if (threadIdx.x * per + i < nb) mine += h[threadIdx.x * per + i];
     // block exclusive scan of `mine`
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint32_t inc = mine;
@@ -351,6 +353,7 @@ __device__ void find_bin(const uint32_t *h, uint32_t r, uint32_t *out3) {
     if (r >= before && r < before + mine) {
         uint32_t cum = before;
         for (int i = 0; i < per; ++i) {
+            if (threadIdx.x * per + i >= nb) break;
             uint32_t c = h[threadIdx.x * per + i];
             if (r < cum + c) {
                 out3[0] = (uint32_t)(threadIdx.x * per + i);
@@ -474,22 +477,27 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
             red_k[0][warp] = kmn; red_k[1][warp] = kmx;
             red_i[0][warp] = imn; red_i[1][warp] = imx;
         }
-        for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) h[b] = 0;
-        if (threadIdx.x == 0) ncomp = 0;
-        __syncthreads();
         kmn = ~0ull; kmx = 0; imn = kFull; imx = 0;
+        __syncthreads();
         for (int i = 0; i < nw; ++i) {
             kmn = min(kmn, red_k[0][i]); kmx = max(kmx, red_k[1][i]);
             imn = min(imn, red_i[0][i]); imx = max(imx, red_i[1][i]);
         }
+        // bins for about 32 candidates each (at least 256, at most kHistBins): the zeroing
+        // and the scan of the histogram then cost in proportion to the candidates
+        int nbits = 8;
+        while (nbits < kHistBits && (c >> (nbits + 5)) > 0u) ++nbits;
+        const uint32_t nb = 1u << nbits;
         const bool bykey = kmn != kmx;
         int bits = bykey ? 64 - __clzll((long long)(kmn ^ kmx)) : 32 - __clz((int)(imn ^ imx));
-        const uint32_t shift = bits > kHistBits ? (uint32_t)(bits - kHistBits) : 0u;
+        const uint32_t shift = bits > nbits ? (uint32_t)(bits - nbits) : 0u;
         auto digit = [&](unsigned long long key, uint32_t id, uint32_t pos) -> uint32_t {
-            if (lin) return lin_bin(w[pos], st.lo, st.scale);
-            return bykey ? ((uint32_t)(key >> shift) & (kHistBins - 1))
-                         : ((id >> shift) & (kHistBins - 1));
+            if (lin) return lin_bin(w[pos], st.lo, st.scale) >> (kHistBits - nbits);
+            return bykey ? ((uint32_t)(key >> shift) & (nb - 1)) : ((id >> shift) & (nb - 1));
         };
+        for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) h[b] = 0;
+        if (threadIdx.x == 0) ncomp = 0;
+        __syncthreads();
         for (uint32_t j = threadIdx.x; j < c; j += blockDim.x) {
             unsigned long long key;
             uint32_t pos;
@@ -497,7 +505,7 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
             atomicAdd(&h[digit(key, ids[pos], pos)], 1u);
         }
         __syncthreads();
-        find_bin(h, r, out3);
+        find_bin(h, r, out3, nb);
         const uint32_t dig = out3[0], below = out3[1], inbin = out3[2];
         const int dst = src == 0 ? 1 : 0;
         for (uint32_t base = 0; base < c; base += blockDim.x) {
