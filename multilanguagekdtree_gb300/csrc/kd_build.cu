@@ -642,46 +642,39 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
     const uint32_t mid = split_rank(lv, r.cnt);
     const uint32_t lbase = tile_off[(size_t)r.seg * lv.tiles + r.tile];
     const uint32_t rbase = r.lo - lbase;
-    __shared__ uint32_t wl[kTileThreads / 32], wr[kTileThreads / 32];
+    // The tile as kRows rows of one element per thread: all loads first, then one ballot
+    // per row, one table of per-(row, warp) counts and its row-major exclusive scan, so the
+    // stable order costs three block barriers per tile.
+    constexpr int kRows = kTile / kTileThreads;
+    constexpr int kWarps = kTileThreads / 32;
+    __shared__ uint32_t cntL[kRows][kWarps], cntR[kRows][kWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1u;
-    uint32_t runL = 0, runR = 0;
-    for (uint32_t base = r.lo; base < r.hi; base += blockDim.x) {
-        uint32_t k = base + threadIdx.x;
-        bool in = k < r.hi;
-        double vx = 0, vy = 0, vz = 0;
-        uint32_t id = 0;
-        if (in) {
-            vx = sx[r.start + k];
-            vy = sy[r.start + k];
-            vz = sz[r.start + k];
-            id = sid[r.start + k];
+    double vx[kRows], vy[kRows], vz[kRows];
+    uint32_t vid[kRows], bl[kRows], br[kRows];
+    bool isL[kRows], in[kRows];
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+        const uint32_t k = r.lo + (uint32_t)i * kTileThreads + threadIdx.x;
+        in[i] = k < r.hi;
+        vx[i] = vy[i] = vz[i] = 0.0;
+        vid[i] = 0u;
+        if (in[i]) {
+            vx[i] = sx[r.start + k];
+            vy[i] = sy[r.start + k];
+            vz[i] = sz[r.start + k];
+            vid[i] = sid[r.start + k];
         }
-        const unsigned long long kx = ord_key(vx), ky = ord_key(vy), kz = ord_key(vz);
+    }
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+        const unsigned long long kx = ord_key(vx[i]), ky = ord_key(vy[i]), kz = ord_key(vz[i]);
         const unsigned long long key = s.sd == 0 ? kx : (s.sd == 1 ? ky : kz);
-        bool isL = in && goes_left(key, id, s.kmed, s.idmed);
-        bool isR = in && !isL;
-        uint32_t bl = __ballot_sync(kFull, isL), br = __ballot_sync(kFull, isR);
-        if (lane == 0) { wl[warp] = __popc(bl); wr[warp] = __popc(br); }
-        __syncthreads();
-        uint32_t offL = 0, offR = 0, totL = 0, totR = 0;
-        for (int q = 0; q < kTileThreads / 32; ++q) {
-            if (q < warp) { offL += wl[q]; offR += wr[q]; }
-            totL += wl[q];
-            totR += wr[q];
-        }
-        const uint32_t dst = isL ? r.start + lbase + runL + offL + __popc(bl & lt)
-                                 : r.start + mid + rbase + runR + offR + __popc(br & lt);
-        // a failed select (flagged by k_tile_scan) must not write outside the segment
-        if (in && dst < r.start + r.cnt) {
-            dx[dst] = vx;
-            dy[dst] = vy;
-            dz[dst] = vz;
-            did[dst] = id;
-            if (lv.med_pos && id == s.idmed && key == s.kmed) *lv.med_pos = dst;
-        }
-        if (nbmin && in) {
-            if (isL) {
+        isL[i] = in[i] && goes_left(key, vid[i], s.kmed, s.idmed);
+        bl[i] = __ballot_sync(kFull, isL[i]);
+        br[i] = __ballot_sync(kFull, in[i] && !isL[i]);
+        if (nbmin && in[i]) {
+            if (isL[i]) {
                 cmn[0][0] = min(cmn[0][0], kx); cmx[0][0] = max(cmx[0][0], kx);
                 cmn[0][1] = min(cmn[0][1], ky); cmx[0][1] = max(cmx[0][1], ky);
                 cmn[0][2] = min(cmn[0][2], kz); cmx[0][2] = max(cmx[0][2], kz);
@@ -691,9 +684,52 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
                 cmn[1][2] = min(cmn[1][2], kz); cmx[1][2] = max(cmx[1][2], kz);
             }
         }
-        runL += totL;
-        runR += totR;
-        __syncthreads();
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < kRows; ++i) {
+            cntL[i][warp] = __popc(bl[i]);
+            cntR[i][warp] = __popc(br[i]);
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // exclusive scan over the kRows x kWarps counts in row-major (element) order
+        constexpr int kCells = kRows * kWarps;
+        static_assert(kCells <= 64, "two cells per lane");
+        uint32_t a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+        const int c0 = 2 * lane, c1 = 2 * lane + 1;
+        if (c0 < kCells) { a0 = cntL[c0 / kWarps][c0 % kWarps]; b0 = cntR[c0 / kWarps][c0 % kWarps]; }
+        if (c1 < kCells) { a1 = cntL[c1 / kWarps][c1 % kWarps]; b1 = cntR[c1 / kWarps][c1 % kWarps]; }
+        uint32_t sa = a0 + a1, sb = b0 + b1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t ua = __shfl_up_sync(kFull, sa, o), ub = __shfl_up_sync(kFull, sb, o);
+            if (lane >= o) { sa += ua; sb += ub; }
+        }
+        const uint32_t ea = sa - a0 - a1, eb = sb - b0 - b1;
+        __syncwarp();
+        if (c0 < kCells) { cntL[c0 / kWarps][c0 % kWarps] = ea; cntR[c0 / kWarps][c0 % kWarps] = eb; }
+        if (c1 < kCells) { cntL[c1 / kWarps][c1 % kWarps] = ea + a0; cntR[c1 / kWarps][c1 % kWarps] = eb + b0; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+        if (!in[i]) continue;
+        const uint32_t dst = isL[i] ? r.start + lbase + cntL[i][warp] + __popc(bl[i] & lt)
+                                    : r.start + mid + rbase + cntR[i][warp] + __popc(br[i] & lt);
+        // a failed select (flagged by k_tile_scan) must not write outside the segment
+        if (dst < r.start + r.cnt) {
+            dx[dst] = vx[i];
+            dy[dst] = vy[i];
+            dz[dst] = vz[i];
+            did[dst] = vid[i];
+            if (lv.med_pos && vid[i] == s.idmed) {
+                const unsigned long long key =
+                    ord_key(s.sd == 0 ? vx[i] : (s.sd == 1 ? vy[i] : vz[i]));
+                if (key == s.kmed) *lv.med_pos = dst;
+            }
+        }
     }
     if (nbmin) {
         __shared__ unsigned long long red[kTileThreads / 32][12];
