@@ -237,6 +237,11 @@ struct kd_ctx {
     int graph_prec = -1, graph_heavy = -1;
     uint64_t graph_launches = 0;
     bool graph_off = false;  // capture failed once: launch directly from then on
+    // one backward step (rebuild + transpose-Jacobian step) as a CUDA graph
+    cudaGraphExec_t adj_graph = nullptr;
+    double adj_graph_dt = 0.0;
+    int adj_graph_heavy = -1;
+    uint64_t adj_graph_launches = 0;
 
     // adjoint state, allocated by the first kd_forward
     bool adj_ready = false;
@@ -622,6 +627,46 @@ void enqueue_steps(kd_ctx *c, double dt, int64_t steps) {
     }
 }
 
+// One backward step over the bodies' current positions: rebuild the (mixed) tree and apply
+// the transpose-Jacobian step.  Replayed from a CUDA graph like the forward step (recaptured
+// when dt or the heavy-body count changes).
+void enqueue_adj_step(kd_ctx *c, const AdjArgs &a) {
+    auto direct = [&]() {
+        enqueue_build(c, false, true);
+        c->launches += launch_adjoint_step(a, c->st);
+    };
+    if (c->counting || c->timing || c->graph_off) {
+        direct();
+        return;
+    }
+    if (!c->adj_graph || c->adj_graph_dt != a.dt || c->adj_graph_heavy != c->n_heavy) {
+        if (c->adj_graph) cudaGraphExecDestroy(c->adj_graph);
+        c->adj_graph = nullptr;
+        const uint64_t l0 = c->launches;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            direct();
+            e = cudaStreamEndCapture(c->st, &g);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&c->adj_graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        c->adj_graph_launches = c->launches - l0;
+        c->launches = l0;
+        if (e != cudaSuccess || !c->adj_graph) {
+            cudaGetLastError();
+            c->adj_graph = nullptr;
+            c->graph_off = true;
+            direct();
+            return;
+        }
+        c->adj_graph_dt = a.dt;
+        c->adj_graph_heavy = c->n_heavy;
+    }
+    cudaGraphLaunch(c->adj_graph, c->st);
+    c->launches += c->adj_graph_launches;
+}
+
 namespace kd {
 void set_thread_error(const char *msg) { g_create_error = msg ? msg : ""; }
 }  // namespace kd
@@ -739,6 +784,7 @@ void kd_destroy(kd_ctx *c) {
     cudaSetDevice(c->prm.device);
     if (c->st) cudaStreamSynchronize(c->st);
     if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->adj_graph) cudaGraphExecDestroy(c->adj_graph);
     for (void *p : c->owned) cudaFree(p);
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -1258,8 +1304,7 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
             for (int k = 0; k < 3; ++k)
                 KD_CHECK(c, cudaMemcpyAsync(pos[k], src + k * n, n * sizeof(double),
                                             cudaMemcpyDeviceToDevice, c->st));
-            enqueue_build(c, false, true);
-            c->launches += launch_adjoint_step(a, c->st);
+            enqueue_adj_step(c, a);
         }
     }
     if (!rc) rc = copy_state(c, t->final_state, false);
