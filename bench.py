@@ -313,13 +313,14 @@ def run_ours(a, ws, rank, local):
     line["phases_ms_per_step"] = {k: ph[k] / 2 for k in ("build_ms", "moments_ms", "walk_ms",
                                                          "kick_ms")}
     line["interactions_per_body"] = {k: v / n for k, v in cnt.items()}
-    # DRAM bytes per launch: ncu capture of the 1M-body walk (117.0 MB read + 18.4 MB
-    # written, profiles/k_walk_mixed_ring1M.md) scaled by the number of bodies
-    walk_traffic = 135.4 * n
+    # DRAM bytes per launch: one-pass ncu capture of the 10M-body walk (4.28 GB read +
+    # 0.475 GB written, 476 B per body), scaled by the number of bodies
+    walk_traffic = 476.0 * n
     line["roofline"] = {
         "kernel": "k_walk_group", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": walk_traffic,
-        "traffic_unit": "bytes per launch (ncu, 1M ring, scaled by N)",
+        "traffic_unit": "bytes per launch (ncu dram read + write of the 10M ring walk, scaled "
+                        "by N)",
         "note": WALK_FLOPS_NOTE}
     # build: algorithmic bytes ~ N*(40 L + 32) with L = multi-block levels, see the design doc
     peaks = {}

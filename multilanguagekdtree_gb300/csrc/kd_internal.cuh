@@ -33,7 +33,10 @@ constexpr int kHistBits = 12;       // radix digit of the median select
 constexpr int kHistBins = 1 << kHistBits;
 constexpr int kSelCap = 2048;       // capacity of the select's shared-memory sort
 constexpr int kSortDirect = 256;    // candidate sets this small are sorted without a pass
-constexpr int kSelThreads = 512;
+#ifndef KD_SEL_THREADS
+#define KD_SEL_THREADS 512
+#endif
+constexpr int kSelThreads = KD_SEL_THREADS;
 constexpr uint32_t kMultiMin = 32768;  // segments above this use multi-block histograms
 constexpr int kSelMaxIters = 16;    // radix refinement passes before giving up (error)
 constexpr int kWalkWarps = 4;       // warps per walk block
