@@ -30,6 +30,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 from pathlib import Path
@@ -125,11 +126,10 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"kd_bench_clocks_{os.getpid()}.csv"
 
     def start(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
@@ -322,19 +322,22 @@ def run_ours(a, ws, rank, local):
         "traffic_unit": "bytes per launch (ncu dram read + write of the 10M ring walk, scaled "
                         "by N)",
         "note": WALK_FLOPS_NOTE}
-    # build: algorithmic bytes ~ N*(40 L + 32) with L = multi-block levels, see the design doc
+    # build: algorithmic bytes per build = N*(40 L + 32), L = internal levels of the tree
+    # (each level reads x, y, z for the box, the split key and the index; a final gather of
+    # the leaves)
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
     except (OSError, ValueError):
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    levels = max(1, int(np.ceil(np.log2(n / 1024.0))))
+    levels = tree_levels(n, a.leaf)
     build_bytes = n * (40 * levels + 32)
     build_s = ph["build_ms"] / 2 / 1e3
     line["roofline_build"] = {
         "bound": "hbm", "achieved": build_bytes / build_s / 1e9, "peak": hbm, "unit": "GB/s",
         "frac": build_bytes / build_s / 1e9 / hbm, "traffic": None,
+        "note": f"algorithmic bytes N*(40 L + 32), L = {levels} internal levels",
         "peak_source": "MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
 
     # ---- energy drift over the timed run length
@@ -464,6 +467,15 @@ WALK_FLOPS_NOTE = ("walk flops = 18 per body interaction (P2P or accepted node, 
                    "measured FP32 figure exists)")
 
 
+def tree_levels(n: int, leaf: int) -> int:
+    """Internal levels of the median-split tree of n bodies (halvings until <= leaf)."""
+    levels, c = 0, n
+    while c > leaf:
+        c = c - c // 2
+        levels += 1
+    return levels
+
+
 def walk_flops(cnt):
     """Algorithmic FP32 work of one grouped walk from its device counts."""
     return 18 * (cnt["p2p"] + cnt["m2p"]) + 20 * cnt["opened"]
@@ -521,7 +533,7 @@ def run_plummer(a, dev):
         hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", 6800.0)
     except (OSError, ValueError):
         hbm = 6800.0
-    levels = max(1, int(np.ceil(np.log2(n / 1024.0))))
+    levels = tree_levels(n, a.leaf)
     bb = n * (40 * levels + 32) / (ph["build_ms"] / 2 / 1e3) / 1e9
     line["roofline_build"] = {"bound": "hbm", "achieved": bb, "peak": hbm, "unit": "GB/s",
                               "frac": bb / hbm}

@@ -40,3 +40,11 @@ def test_replica_value_is_whole_job(ws, t, expect):
     sys.path.insert(0, str(ROOT))
     import bench
     assert bench.replica_value(ws, 100, 10, t) == pytest.approx(expect)
+
+
+@pytest.mark.parametrize("n,leaf,expect", [(10_000_000, 7, 21), (20_000_000, 7, 22), (7, 7, 0),
+                                           (8, 7, 1)])
+def test_tree_levels(n, leaf, expect):
+    sys.path.insert(0, str(ROOT))
+    import bench
+    assert bench.tree_levels(n, leaf) == expect
