@@ -232,20 +232,29 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
         const uint32_t pi = warp_incl_scan(fc | (oc << 16), lane);
         const uint32_t pt = __shfl_sync(kFull, pi, 31);
         const uint32_t fi = pi & 0xffffu, oi = pi >> 16, ft = pt & 0xffffu, ot = pt >> 16;
-        if (far) {
-            // all member loads of the leaf in flight at once (leaf size <= 8)
-            float4 t[8];
+        // the far leaves' bodies, written cooperatively: lane j of a round takes body j of
+        // the wave, finds its leaf (the first lane whose inclusive count exceeds j) by binary
+        // search, and writes the same entry, at the same place, the leaf's lane would
+        for (uint32_t j0 = 0; j0 < ft; j0 += 32) {
+            const uint32_t j = j0 + (uint32_t)lane;
+            int q = 0;
 #pragma unroll
-            for (uint32_t k = 0; k < 8; ++k)
-                if (k < ab.y) t[k] = __ldg(&trel[ab.x + k]);
-            const uint32_t d0 = nl + fi - fc;
-#pragma unroll
-            for (uint32_t k = 0; k < 8; ++k)
-                if (k < ab.y) {
-                    W.list[d0 + k] = make_float4(cx + t[k].x, cy + t[k].y, cz + t[k].z, t[k].w);
-                    if (kTgt) W.tgt[d0 + k] = ab.x + k;
-                }
-        } else if (mine) {
+            for (int step = 16; step > 0; step >>= 1) {
+                const uint32_t v = __shfl_sync(kFull, fi, q + step - 1);
+                if (v <= j) q += step;
+            }
+            const uint32_t first = __shfl_sync(kFull, ab.x, q);
+            const uint32_t before = __shfl_sync(kFull, fi - fc, q);
+            const float ox = __shfl_sync(kFull, cx, q), oy = __shfl_sync(kFull, cy, q),
+                        oz = __shfl_sync(kFull, cz, q);
+            if (j < ft) {
+                const uint32_t body = first + (j - before);
+                const float4 t = __ldg(&trel[body]);
+                W.list[nl + j] = make_float4(ox + t.x, oy + t.y, oz + t.z, t.w);
+                if (kTgt) W.tgt[nl + j] = body;
+            }
+        }
+        if (mine) {
             const uint32_t o0 = nown + oi - oc;
             for (uint32_t k = 0; k < ab.y && o0 + k < 32u; ++k) {
                 const float4 hi = __ldg(&thi[ab.x + k]), lo = __ldg(&tlo[ab.x + k]);
