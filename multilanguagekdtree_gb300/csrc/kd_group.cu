@@ -18,7 +18,7 @@
 // opening test -- a refinement of the reference walk's partition, never a coarser one.
 //
 // Coordinates are relative to the group's first body (split hi + lo to FP32), forces are
-// FP32 with compensated (Kahan) sums per block of 32 list entries, and the heavy bodies are
+// FP32 with compensated (Kahan) sums per block of 64 list entries, and the heavy bodies are
 // summed in FP64 at the end.
 //
 // The adjoint walk runs the same traversal (the same code, so the same decisions) and
@@ -283,15 +283,15 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
     __syncwarp();
 }
 
-// Sum of the entries [0, nl) on the lane's body: plain FP32 partial sums over 32 entries,
+// Sum of the entries [0, nl) on the lane's body: plain FP32 partial sums over 64 entries,
 // each folded into the compensated sums.
 template <bool kPot>
 __device__ __forceinline__ void sum_list(const float4 *list, uint32_t nl, float qx, float qy,
                                          float qz, float (&s)[4], float (&c)[4]) {
-    for (uint32_t k0 = 0; k0 < nl; k0 += 32) {
-        const uint32_t k1 = min(nl, k0 + 32u);
+    for (uint32_t k0 = 0; k0 < nl; k0 += 64) {
+        const uint32_t k1 = min(nl, k0 + 64u);
         float px = 0.f, py = 0.f, pz = 0.f, pp = 0.f;
-#pragma unroll 8
+#pragma unroll 16
         for (uint32_t k = k0; k < k1; ++k) {
             const float4 e = list[k];
             const float dx = e.x - qx, dy = e.y - qy, dz = e.z - qz;
