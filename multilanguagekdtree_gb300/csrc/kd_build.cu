@@ -1019,7 +1019,7 @@ __device__ __forceinline__ void small_subtree(LocalSmem &S, const Topology &t, c
     __syncwarp();
 }
 
-__global__ __launch_bounds__(kLocalThreads) void k_local(Topology t, const uint32_t *roots,
+__global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const uint32_t *roots,
                                                          NodeOut no, const double *wx,
                                                          const double *wy, const double *wz,
                                                          const uint32_t *wid, LocalOut o,
