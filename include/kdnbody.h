@@ -236,7 +236,7 @@ int kd_direct_accel_noalloc(const double *x, const double *y, const double *z,
 /* Interaction counts of the last walk, summed over bodies: out[0] = pair (P2P)
  * interactions, out[2] = accepted multipole (M2P) interactions.  FP64 walk: out[1] =
  * opening tests at internal nodes, out[3] = node visits, both per body.  Mixed (grouped)
- * walk: out[1] = node tests, each made once for a group of up to 32 bodies, out[3] = the
+ * walk: out[1] = node tests, each made once for a group of up to 64 bodies, out[3] = the
  * same tests counted once per body of the group.  Counting is enabled by
  * kd_set_counting(ctx, 1) (it costs a few percent). */
 int kd_set_counting(kd_ctx *ctx, int32_t on);

@@ -136,15 +136,15 @@ bool make_plan(uint32_t n, uint32_t leaf, Plan &p, std::string &err) {
         }
         cur.swap(nxt);
     }
-    // Sink groups: whole leaves in tree order, packed greedily up to 32 bodies.
+    // Sink groups: whole leaves in tree order, packed greedily up to kGroupSinks bodies.
     std::vector<std::pair<uint32_t, uint32_t>> lv;
     lv.reserve(p.leaves.size());
     for (uint32_t id : p.leaves) lv.emplace_back(p.start[id], p.count[id]);
     std::sort(lv.begin(), lv.end());
     p.gstart.clear();
-    uint32_t fill = 32;
+    uint32_t fill = kGroupSinks;
     for (const auto &e : lv) {
-        if (fill + e.second > 32) {
+        if (fill + e.second > (uint32_t)kGroupSinks) {
             p.gstart.push_back(e.first);
             fill = 0;
         }

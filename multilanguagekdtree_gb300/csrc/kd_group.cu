@@ -1,7 +1,7 @@
 // kd_group.cu -- grouped theta-opening walk of the mixed-precision path, and its adjoint.
 //
-// The sinks are cut into groups of whole leaves, consecutive in tree order, at most 32
-// bodies each (one per lane).  A warp walks the tree once for its group: the 32 lanes test
+// The sinks are cut into groups of whole leaves, consecutive in tree order, at most 64
+// bodies each (two per lane).  A warp walks the tree once for its group: the 32 lanes test
 // 32 stack nodes at a time against the group's bounding box with the opening test
 // size^2 < theta^2 dmin^2, dmin the distance from the node's centre of mass to the box
 // (Barnes 1990, "A modified tree code: don't laugh; it runs", J. Comput. Phys. 87:161).
@@ -10,7 +10,9 @@
 // of the tree, and one box around both would open nearly every node for that group.
 // Accepted nodes and the bodies of reached leaves go to an interaction list in shared
 // memory; whenever the list holds kGroupFlush entries every lane sums it for its own body,
-// so the force loop runs without divergence and without per-lane traversal state.
+// so the force loop runs without divergence and without per-lane traversal state.  Two
+// sinks per lane halve the traversal per body against 32-body groups, for a group box that
+// accepts somewhat fewer nodes.
 //
 // A node the group accepts passes the reference's per-body test (array_kd_tree.rs:600-609)
 // for every body of the group, because dmin is at most each body's distance: every body's
@@ -18,12 +20,12 @@
 // opening test -- a refinement of the reference walk's partition, never a coarser one.
 //
 // Coordinates are relative to the group's first body (split hi + lo to FP32), forces are
-// FP32 with compensated (Kahan) sums per block of 64 list entries, and the heavy bodies are
-// summed in FP64 at the end.
+// FP32, two list entries per packed f32x2 instruction, with compensated (Kahan) sums per
+// block of 64 list entries, and the heavy bodies are summed in FP64 at the end.
 //
 // The adjoint walk runs the same traversal (the same code, so the same decisions) and
-// evaluates each block of 32 list entries against the 32 sinks with a rotation: at step k
-// lane l pairs its sink with entry (l + k) mod 32 and passes the entry's source-side
+// evaluates each block of 32 list entries against the 64 sinks with a rotation: at step k
+// lane l pairs its two sinks with entry (l + k) mod 32 and passes the entry's source-side
 // accumulator one lane down, so after 32 steps lane l holds the sum over all sinks for
 // entry l -- both sides of J^T mu from one tidal product per pair, one FP64 atomic per entry
 // and component (the sums over groups then carry no FP32 rounding).
@@ -42,6 +44,44 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// Two FP32 values in one 64-bit register, for the packed f32x2 arithmetic of sm_100 and
+// later (one instruction, two IEEE round-to-nearest results).
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+__device__ __forceinline__ void upk(f2 v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
 }
 
 __device__ __forceinline__ void kahan(float &sum, float &comp, float x) {
@@ -92,18 +132,39 @@ __device__ __forceinline__ WarpMem warp_mem(float4 *smem, int warp, uint32_t stk
     WarpMem w;
     w.list = reinterpret_cast<float4 *>(reinterpret_cast<char *>(smem) + warp * wbytes);
     w.own = w.list + kGroupListCap;
-    w.stk = reinterpret_cast<uint32_t *>(w.own + 64);
+    w.stk = reinterpret_cast<uint32_t *>(w.own + 2 * kGroupSinks);
     w.tgt = w.stk + stk_cap;
     return w;
 }
 
-// One lane's view of its group: tree positions, frame origin, own position, the two boxes.
+// List entry k.  The adjoint keeps one float4 per entry; the force walk keeps four component
+// arrays X, Y, Z, M of kGroupListCap floats each in the same space, so that four
+// consecutive entries of a component are one aligned float4 and two of them fill one packed
+// register.
+static_assert(kGroupListCap % 4 == 0, "component arrays must stay 16-byte aligned");
+
+template <bool kSoA>
+__device__ __forceinline__ void put_entry(const WarpMem &W, uint32_t k, float x, float y,
+                                          float z, float m) {
+    if (kSoA) {
+        float *L = reinterpret_cast<float *>(W.list);
+        L[k] = x;
+        L[kGroupListCap + k] = y;
+        L[2 * kGroupListCap + k] = z;
+        L[3 * kGroupListCap + k] = m;
+    } else {
+        W.list[k] = make_float4(x, y, z, m);
+    }
+}
+
+// One lane's view of its group: tree positions, frame origin, the lane's two sinks (bodies
+// lane and lane + 32 of the group), the two boxes.
 struct Group {
-    uint32_t g0, g1, s;
-    bool valid;
+    uint32_t g0, g1;
+    uint32_t s[2];                       // the sinks' tree positions (g0 when absent)
+    bool valid[2];
     float ohx, ohy, ohz, olx, oly, olz;  // origin: the group's first body, hi + lo
-    float qx, qy, qz;                    // the lane's body in the group frame
-    float4 mh, ml;                       // the lane's body, split absolute position
+    float qx[2], qy[2], qz[2];           // the sinks in the group frame
     float a[6], b[6];                    // boxes (lo xyz, hi xyz) before / after the split
 };
 
@@ -113,35 +174,50 @@ __device__ __forceinline__ Group make_group(const float4 *__restrict__ thi,
     Group G;
     G.g0 = g0;
     G.g1 = g1;
-    G.valid = lane < (int)(g1 - g0);
-    G.s = G.valid ? g0 + lane : g0;
-    const float4 mh = thi[G.s], ml = tlo[G.s];
-    G.mh = mh;
-    G.ml = ml;
-    G.ohx = __shfl_sync(kFull, mh.x, 0);
-    G.ohy = __shfl_sync(kFull, mh.y, 0);
-    G.ohz = __shfl_sync(kFull, mh.z, 0);
-    G.olx = __shfl_sync(kFull, ml.x, 0);
-    G.oly = __shfl_sync(kFull, ml.y, 0);
-    G.olz = __shfl_sync(kFull, ml.z, 0);
-    G.qx = (mh.x - G.ohx) + (ml.x - G.olx);
-    G.qy = (mh.y - G.ohy) + (ml.y - G.oly);
-    G.qz = (mh.z - G.ohz) + (ml.z - G.olz);
-    const bool inA = G.valid && G.s < gs, inB = G.valid && G.s >= gs;
-    const float q[3] = {G.qx, G.qy, G.qz};
+    float4 mh[2], ml[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        G.valid[u] = lane + 32 * u < (int)(g1 - g0);
+        G.s[u] = G.valid[u] ? g0 + lane + 32 * u : g0;
+        mh[u] = thi[G.s[u]];
+        ml[u] = tlo[G.s[u]];
+    }
+    G.ohx = __shfl_sync(kFull, mh[0].x, 0);
+    G.ohy = __shfl_sync(kFull, mh[0].y, 0);
+    G.ohz = __shfl_sync(kFull, mh[0].z, 0);
+    G.olx = __shfl_sync(kFull, ml[0].x, 0);
+    G.oly = __shfl_sync(kFull, ml[0].y, 0);
+    G.olz = __shfl_sync(kFull, ml[0].z, 0);
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        G.qx[u] = (mh[u].x - G.ohx) + (ml[u].x - G.olx);
+        G.qy[u] = (mh[u].y - G.ohy) + (ml[u].y - G.oly);
+        G.qz[u] = (mh[u].z - G.ohz) + (ml[u].z - G.olz);
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        G.a[d] = warp_min(inA ? q[d] : INFINITY);
-        G.a[d + 3] = warp_max(inA ? q[d] : -INFINITY);
-        G.b[d] = warp_min(inB ? q[d] : INFINITY);
-        G.b[d + 3] = warp_max(inB ? q[d] : -INFINITY);
+        float alo = INFINITY, ahi = -INFINITY, blo = INFINITY, bhi = -INFINITY;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const float q = d == 0 ? G.qx[u] : d == 1 ? G.qy[u] : G.qz[u];
+            const bool inA = G.valid[u] && G.s[u] < gs, inB = G.valid[u] && G.s[u] >= gs;
+            alo = fminf(alo, inA ? q : INFINITY);
+            ahi = fmaxf(ahi, inA ? q : -INFINITY);
+            blo = fminf(blo, inB ? q : INFINITY);
+            bhi = fmaxf(bhi, inB ? q : -INFINITY);
+        }
+        G.a[d] = warp_min(alo);
+        G.a[d + 3] = warp_max(ahi);
+        G.b[d] = warp_min(blo);
+        G.b[d + 3] = warp_max(bhi);
     }
     return G;
 }
 
 // Walk of one group.  Accepted nodes and far leaves' bodies are appended to W.list (with
-// their source targets when kTgt); the group's own leaves go to W.own.  flush(nl) is
-// called whenever the list holds kGroupFlush entries or more, and at the end.
+// their source targets when kTgt, as float4 entries; else in component arrays); the group's
+// own leaves go to W.own.  flush(nl) is called whenever the list holds kGroupFlush entries
+// or more, and at the end.
 template <bool kTgt, bool kCount, typename Flush>
 __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
                                          const float4 *__restrict__ trel,
@@ -220,7 +296,7 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
         const uint32_t am = __ballot_sync(kFull, take_m);
         if (take_m) {
             const uint32_t k = nl + __popc(am & lt);
-            W.list[k] = make_float4(cx, cy, cz, l.w);
+            put_entry<!kTgt>(W, k, cx, cy, cz, l.w);
             if (kTgt) W.tgt[k] = node | kNodeTarget;
         }
         nl += __popc(am);
@@ -250,20 +326,20 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
             if (j < ft) {
                 const uint32_t body = first + (j - before);
                 const float4 t = __ldg(&trel[body]);
-                W.list[nl + j] = make_float4(ox + t.x, oy + t.y, oz + t.z, t.w);
+                put_entry<!kTgt>(W, nl + j, ox + t.x, oy + t.y, oz + t.z, t.w);
                 if (kTgt) W.tgt[nl + j] = body;
             }
         }
         if (mine) {
             const uint32_t o0 = nown + oi - oc;
-            for (uint32_t k = 0; k < ab.y && o0 + k < 32u; ++k) {
+            for (uint32_t k = 0; k < ab.y && o0 + k < (uint32_t)kGroupSinks; ++k) {
                 const float4 hi = __ldg(&thi[ab.x + k]), lo = __ldg(&tlo[ab.x + k]);
                 W.own[2 * (o0 + k)] = hi;
                 W.own[2 * (o0 + k) + 1] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(ab.x + k));
             }
         }
         nl += ft;
-        nown = min(nown + ot, 32u);
+        nown = min(nown + ot, (uint32_t)kGroupSinks);
         if (kCount) cnt[0] += ft;
         __syncwarp();
         if (nl >= (uint32_t)kGroupFlush) {
@@ -283,31 +359,69 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
     __syncwarp();
 }
 
-// Sum of the entries [0, nl) on the lane's body: plain FP32 partial sums over 64 entries,
-// each folded into the compensated sums.
+// Two list entries (packed source coordinates and masses) on the lane's body (q, packed
+// twice): the pair kernel of one entry per half.
 template <bool kPot>
-__device__ __forceinline__ void sum_list(const float4 *list, uint32_t nl, float qx, float qy,
-                                         float qz, float (&s)[4], float (&c)[4]) {
+__device__ __forceinline__ void pair_term2(f2 ex, f2 ey, f2 ez, f2 em, f2 qx, f2 qy, f2 qz,
+                                           f2 &px, f2 &py, f2 &pz, f2 &pp) {
+    const f2 dx = sub2(ex, qx), dy = sub2(ey, qy), dz = sub2(ez, qz);
+    const f2 d2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+    float da, db;
+    upk(d2, da, db);
+    const f2 inv = pk(rsqrt_ftz(da), rsqrt_ftz(db));
+    const f2 mi = mul2(em, inv);
+    const f2 f = mul2(mi, mul2(inv, inv));
+    px = fma2(f, dx, px);
+    py = fma2(f, dy, py);
+    pz = fma2(f, dz, pz);
+    if (kPot) pp = add2(pp, mi);
+}
+
+// Sum of the entries [0, nl) (nl a multiple of 4) of the component arrays L on the lane's
+// two sinks, two entries per packed instruction: plain FP32 partial sums over 64 entries
+// (even entries in one half, odd in the other), each folded into the compensated sums.
+template <bool kPot>
+__device__ __forceinline__ void sum_list(const float *L, uint32_t nl, const Group &G,
+                                         float (&s)[2][4], float (&c)[2][4]) {
+    f2 qx[2], qy[2], qz[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        qx[u] = pk(G.qx[u], G.qx[u]);
+        qy[u] = pk(G.qy[u], G.qy[u]);
+        qz[u] = pk(G.qz[u], G.qz[u]);
+    }
     for (uint32_t k0 = 0; k0 < nl; k0 += 64) {
         const uint32_t k1 = min(nl, k0 + 64u);
-        float px = 0.f, py = 0.f, pz = 0.f, pp = 0.f;
-#pragma unroll 16
-        for (uint32_t k = k0; k < k1; ++k) {
-            const float4 e = list[k];
-            const float dx = e.x - qx, dy = e.y - qy, dz = e.z - qz;
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float inv = rsqrt_ftz(d2);
-            const float mi = e.w * inv;
-            const float f = mi * (inv * inv);
-            px = fmaf(f, dx, px);
-            py = fmaf(f, dy, py);
-            pz = fmaf(f, dz, pz);
-            if (kPot) pp += mi;
+        f2 px[2] = {0ull, 0ull}, py[2] = {0ull, 0ull}, pz[2] = {0ull, 0ull},
+           pp[2] = {0ull, 0ull};  // 0 bits: +0.0f in both halves
+#pragma unroll 2
+        for (uint32_t k = k0; k < k1; k += 4) {
+            const float4 x = *reinterpret_cast<const float4 *>(L + k);
+            const float4 y = *reinterpret_cast<const float4 *>(L + kGroupListCap + k);
+            const float4 z = *reinterpret_cast<const float4 *>(L + 2 * kGroupListCap + k);
+            const float4 m = *reinterpret_cast<const float4 *>(L + 3 * kGroupListCap + k);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                pair_term2<kPot>(pk(x.x, x.y), pk(y.x, y.y), pk(z.x, z.y), pk(m.x, m.y), qx[u],
+                                 qy[u], qz[u], px[u], py[u], pz[u], pp[u]);
+                pair_term2<kPot>(pk(x.z, x.w), pk(y.z, y.w), pk(z.z, z.w), pk(m.z, m.w), qx[u],
+                                 qy[u], qz[u], px[u], py[u], pz[u], pp[u]);
+            }
         }
-        kahan(s[0], c[0], px);
-        kahan(s[1], c[1], py);
-        kahan(s[2], c[2], pz);
-        if (kPot) kahan(s[3], c[3], -pp);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            float a, b;
+            upk(px[u], a, b);
+            kahan(s[u][0], c[u][0], a + b);
+            upk(py[u], a, b);
+            kahan(s[u][1], c[u][1], a + b);
+            upk(pz[u], a, b);
+            kahan(s[u][2], c[u][2], a + b);
+            if (kPot) {
+                upk(pp[u], a, b);
+                kahan(s[u][3], c[u][3], -(a + b));
+            }
+        }
     }
 }
 
@@ -328,42 +442,54 @@ __device__ __forceinline__ void tidal_v(float dx, float dy, float dz, float mx, 
 }
 
 // Adjoint terms of 32 sources (padding sources far away with zero mass) against the warp's
-// 32 sinks by rotation: the sink terms -m w into the compensated sums (sum, comp), folded
-// every 8 pairs, and lane l returns the sum over the sinks of w for source l.
-// `pair(slot, dx, dy, dz)` gives the separation sink - source and returns the source mass.
+// 64 sinks by rotation: the sink terms -m w into the compensated sums (sum, comp), folded
+// every 8 steps, and lane l returns the sum over the sinks of w for source l.
+// `pair(slot, dx, dy, dz, m)` gives, for both of the lane's sinks, the separation
+// sink - source and the source mass (zero where the pair does not exist).
 template <typename Pair>
-__device__ __forceinline__ void rotate32(int lane, float mx, float my, float mz,
-                                         float (&sum)[3], float (&comp)[3], float &ax,
-                                         float &ay, float &az, Pair &&pair) {
+__device__ __forceinline__ void rotate32(int lane, const float (&mx)[2], const float (&my)[2],
+                                         const float (&mz)[2], float (&sum)[2][3],
+                                         float (&comp)[2][3], float &ax, float &ay, float &az,
+                                         Pair &&pair) {
     ax = ay = az = 0.f;
     const int up = (lane + 1) & 31;
 #pragma unroll 1
     for (int k0 = 0; k0 < 32; k0 += 8) {
-        float px = 0.f, py = 0.f, pz = 0.f;
+        float px[2] = {0.f, 0.f}, py[2] = {0.f, 0.f}, pz[2] = {0.f, 0.f};
 #pragma unroll
         for (int k = k0; k < k0 + 8; ++k) {
-            float dx, dy, dz;
-            const float m = pair((lane + k) & 31, dx, dy, dz);
-            float inv3, vx, vy, vz;
-            tidal_v(dx, dy, dz, mx, my, mz, inv3, vx, vy, vz);
-            const float sm = -m * inv3;
-            px = fmaf(sm, vx, px);
-            py = fmaf(sm, vy, py);
-            pz = fmaf(sm, vz, pz);
-            ax = __shfl_sync(kFull, fmaf(inv3, vx, ax), up);
-            ay = __shfl_sync(kFull, fmaf(inv3, vy, ay), up);
-            az = __shfl_sync(kFull, fmaf(inv3, vz, az), up);
+            float dx[2], dy[2], dz[2], m[2];
+            pair((lane + k) & 31, dx, dy, dz, m);
+            float bx = ax, by = ay, bz = az;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                float inv3, vx, vy, vz;
+                tidal_v(dx[u], dy[u], dz[u], mx[u], my[u], mz[u], inv3, vx, vy, vz);
+                const float sm = -m[u] * inv3;
+                px[u] = fmaf(sm, vx, px[u]);
+                py[u] = fmaf(sm, vy, py[u]);
+                pz[u] = fmaf(sm, vz, pz[u]);
+                bx = fmaf(inv3, vx, bx);
+                by = fmaf(inv3, vy, by);
+                bz = fmaf(inv3, vz, bz);
+            }
+            ax = __shfl_sync(kFull, bx, up);
+            ay = __shfl_sync(kFull, by, up);
+            az = __shfl_sync(kFull, bz, up);
         }
-        kahan(sum[0], comp[0], px);
-        kahan(sum[1], comp[1], py);
-        kahan(sum[2], comp[2], pz);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            kahan(sum[u][0], comp[u][0], px[u]);
+            kahan(sum[u][1], comp[u][1], py[u]);
+            kahan(sum[u][2], comp[u][2], pz[u]);
+        }
     }
 }
 
 }  // namespace
 
 template <bool kCount, bool kPot>
-__global__ __launch_bounds__(kGroupWarps * 32, 5) void k_walk_group(
+__global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
     const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
     const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,
@@ -382,25 +508,33 @@ __global__ __launch_bounds__(kGroupWarps * 32, 5) void k_walk_group(
     if (g >= n_groups) return;  // no block-wide barrier follows
     const WarpMem W = warp_mem(smem, warp, stk_cap, false);
     const Group G = make_group(thi, tlo, gstart[g], gstart[g + 1], gsplit[g], lane);
-    const uint32_t s = G.s;
 
-    float sum[4] = {0.f, 0.f, 0.f, 0.f}, comp[4] = {0.f, 0.f, 0.f, 0.f};
+    float sum[2][4] = {}, comp[2][4] = {};
     uint32_t nown = 0;
     unsigned long long cnt[3] = {0, 0, 0};  // pair entries, node entries, node tests
     traverse<false, kCount>(rec, trel, thi, tlo, G, W, stk_cap, theta2, lane, err, nown, cnt,
                             [&](uint32_t nl) {
-                                sum_list<kPot>(W.list, nl, G.qx, G.qy, G.qz, sum, comp);
+                                // padded to a multiple of 4 with entries that add nothing
+                                // (nl < kGroupFlush + 32 * 8, so the padding stays inside)
+                                const uint32_t n4 = (nl + 3u) & ~3u;
+                                if ((uint32_t)lane < n4 - nl)
+                                    put_entry<true>(W, nl + lane, kFar, kFar, kFar, 0.f);
+                                __syncwarp();
+                                sum_list<kPot>(reinterpret_cast<const float *>(W.list), n4, G,
+                                               sum, comp);
                             });
     // the group's own leaves, self excluded by tree position, separations from the split
     // absolute positions
-    {
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const float4 mh = thi[G.s[u]], ml = tlo[G.s[u]];
         float px = 0.f, py = 0.f, pz = 0.f, pp = 0.f;
         for (uint32_t k = 0; k < nown; ++k) {
             const float4 eh = W.own[2 * k], el = W.own[2 * k + 1];
-            if (__float_as_uint(el.w) == s) continue;
-            const float dx = (eh.x - G.mh.x) + (el.x - G.ml.x);
-            const float dy = (eh.y - G.mh.y) + (el.y - G.ml.y);
-            const float dz = (eh.z - G.mh.z) + (el.z - G.ml.z);
+            if (__float_as_uint(el.w) == G.s[u]) continue;
+            const float dx = (eh.x - mh.x) + (el.x - ml.x);
+            const float dy = (eh.y - mh.y) + (el.y - ml.y);
+            const float dz = (eh.z - mh.z) + (el.z - ml.z);
             const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const float inv = rsqrt_ftz(d2);
             const float mi = eh.w * inv;
@@ -410,17 +544,19 @@ __global__ __launch_bounds__(kGroupWarps * 32, 5) void k_walk_group(
             pz = fmaf(f, dz, pz);
             if (kPot) pp += mi;
         }
-        kahan(sum[0], comp[0], px);
-        kahan(sum[1], comp[1], py);
-        kahan(sum[2], comp[2], pz);
-        if (kPot) kahan(sum[3], comp[3], -pp);
+        kahan(sum[u][0], comp[u][0], px);
+        kahan(sum[u][1], comp[u][1], py);
+        kahan(sum[u][2], comp[u][2], pz);
+        if (kPot) kahan(sum[u][3], comp[u][3], -pp);
     }
-    if (G.valid) {
-        const uint32_t o = tid[s];
-        double ax = (double)sum[0] - (double)comp[0];
-        double ay = (double)sum[1] - (double)comp[1];
-        double az = (double)sum[2] - (double)comp[2];
-        double ph = (double)sum[3] - (double)comp[3];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        if (!G.valid[u]) continue;
+        const uint32_t o = tid[G.s[u]];
+        double ax = (double)sum[u][0] - (double)comp[u][0];
+        double ay = (double)sum[u][1] - (double)comp[u][1];
+        double az = (double)sum[u][2] - (double)comp[u][2];
+        double ph = (double)sum[u][3] - (double)comp[u][3];
         // heavy bodies in FP64, pair kernel of array_particle.rs:67-76
         const double px64 = b.x[o], py64 = b.y[o], pz64 = b.z[o];
         for (int hh = 0; hh < n_heavy; ++hh) {
@@ -455,7 +591,7 @@ __global__ __launch_bounds__(kGroupWarps * 32, 5) void k_walk_group(
 // ysink_s (tree order) = -sum m w + the FP64 heavy-body terms; per list entry the sum over
 // the group's sinks of w goes to U (a body, tree order) or G (a node); the heavy bodies'
 // source sums go to yheavy.
-__global__ __launch_bounds__(kGroupWarps * 32, 4) void k_adj_group(
+__global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
     const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
     const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,
@@ -479,19 +615,22 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_adj_group(
     if (g < n_groups) {  // warp-uniform; the block barrier below is reached by every warp
         const WarpMem W = warp_mem(smem, warp, stk_cap, true);
         const Group G = make_group(thi, tlo, gstart[g], gstart[g + 1], gsplit[g], lane);
-        const uint32_t s = G.s;
-        const uint32_t o = G.valid ? tid[s] : 0u;
-        double mux = 0.0, muy = 0.0, muz = 0.0;
-        if (G.valid) {
-            mux = mu[3 * (size_t)o];
-            muy = mu[3 * (size_t)o + 1];
-            muz = mu[3 * (size_t)o + 2];
+        // sinks without a body sit far away with mu = 0: every term they make is zero
+        float mx[2], my[2], mz[2], qx[2], qy[2], qz[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            mx[u] = my[u] = mz[u] = 0.f;
+            if (G.valid[u]) {
+                const size_t o = tid[G.s[u]];
+                mx[u] = (float)mu[3 * o];
+                my[u] = (float)mu[3 * o + 1];
+                mz[u] = (float)mu[3 * o + 2];
+            }
+            qx[u] = G.valid[u] ? G.qx[u] : -kFar;
+            qy[u] = G.valid[u] ? G.qy[u] : -kFar;
+            qz[u] = G.valid[u] ? G.qz[u] : -kFar;
         }
-        const float mx = (float)mux, my = (float)muy, mz = (float)muz;
-        // lanes without a body sit far away with mu = 0: every term they make is zero
-        const float qx = G.valid ? G.qx : -kFar, qy = G.valid ? G.qy : -kFar,
-                    qz = G.valid ? G.qz : -kFar;
-        float sum[3] = {0.f, 0.f, 0.f}, comp[3] = {0.f, 0.f, 0.f};
+        float sum[2][3] = {}, comp[2][3] = {};
         uint32_t nown = 0;
         unsigned long long cnt[3] = {0, 0, 0};
         traverse<true, false>(
@@ -506,12 +645,16 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_adj_group(
                     float ax, ay, az;
                     const float4 *e = W.list + k0;
                     rotate32(lane, mx, my, mz, sum, comp, ax, ay, az,
-                             [&](int slot, float &dx, float &dy, float &dz) {
+                             [&](int slot, float(&dx)[2], float(&dy)[2], float(&dz)[2],
+                                 float(&m)[2]) {
                                  const float4 c = e[slot];
-                                 dx = qx - c.x;
-                                 dy = qy - c.y;
-                                 dz = qz - c.z;
-                                 return c.w;
+#pragma unroll
+                                 for (int u = 0; u < 2; ++u) {
+                                     dx[u] = qx[u] - c.x;
+                                     dy[u] = qy[u] - c.y;
+                                     dz[u] = qz[u] - c.z;
+                                     m[u] = c.w;
+                                 }
                              });
                     const uint32_t t = W.tgt[k0 + lane];
                     if (t != kNoTarget) {
@@ -524,40 +667,61 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_adj_group(
                 }
             });
         // the group's own leaves: pairs among the group's bodies, self excluded, separations
-        // from the split absolute positions
+        // from the split absolute positions; own entries in blocks of 32, padded far away
         {
-            if ((uint32_t)lane >= nown) {
-                W.own[2 * lane] = make_float4(kFar, kFar, kFar, 0.f);
-                W.own[2 * lane + 1] = make_float4(0.f, 0.f, 0.f, __uint_as_float(kNoTarget));
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const uint32_t k = lane + 32 * u;
+                if (k >= nown) {
+                    W.own[2 * k] = make_float4(kFar, kFar, kFar, 0.f);
+                    W.own[2 * k + 1] = make_float4(0.f, 0.f, 0.f, __uint_as_float(kNoTarget));
+                }
             }
             __syncwarp();
-            // lanes without a body sit far away on the other side: no pair reaches zero
-            const float4 mh = G.valid ? G.mh : make_float4(-kFar, -kFar, -kFar, 0.f);
-            const float4 ml = G.valid ? G.ml : make_float4(0.f, 0.f, 0.f, 0.f);
-            float ax, ay, az;
-            rotate32(lane, mx, my, mz, sum, comp, ax, ay, az,
-                     [&](int slot, float &dx, float &dy, float &dz) {
-                         const float4 eh = W.own[2 * slot], el = W.own[2 * slot + 1];
-                         if (__float_as_uint(el.w) == s && G.valid) {
-                             dx = dy = dz = kFar;
-                             return 0.f;
-                         }
-                         dx = (mh.x - eh.x) + (ml.x - el.x);
-                         dy = (mh.y - eh.y) + (ml.y - el.y);
-                         dz = (mh.z - eh.z) + (ml.z - el.z);
-                         return eh.w;
-                     });
-            const uint32_t t = __float_as_uint(W.own[2 * lane + 1].w);
-            if (t != kNoTarget) {
-                atomicAdd(&U[3 * (size_t)t], (double)ax);
-                atomicAdd(&U[3 * (size_t)t + 1], (double)ay);
-                atomicAdd(&U[3 * (size_t)t + 2], (double)az);
+            // sinks without a body sit far away on the other side: no pair reaches zero
+            float4 mh[2], ml[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                mh[u] = G.valid[u] ? thi[G.s[u]] : make_float4(-kFar, -kFar, -kFar, 0.f);
+                ml[u] = G.valid[u] ? tlo[G.s[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            for (uint32_t k0 = 0; k0 < nown; k0 += 32) {
+                const float4 *own = W.own + 2 * k0;
+                float ax, ay, az;
+                rotate32(lane, mx, my, mz, sum, comp, ax, ay, az,
+                         [&](int slot, float(&dx)[2], float(&dy)[2], float(&dz)[2],
+                             float(&m)[2]) {
+                             const float4 eh = own[2 * slot], el = own[2 * slot + 1];
+#pragma unroll
+                             for (int u = 0; u < 2; ++u) {
+                                 if (__float_as_uint(el.w) == G.s[u] && G.valid[u]) {
+                                     dx[u] = dy[u] = dz[u] = kFar;
+                                     m[u] = 0.f;
+                                 } else {
+                                     dx[u] = (mh[u].x - eh.x) + (ml[u].x - el.x);
+                                     dy[u] = (mh[u].y - eh.y) + (ml[u].y - el.y);
+                                     dz[u] = (mh[u].z - eh.z) + (ml[u].z - el.z);
+                                     m[u] = eh.w;
+                                 }
+                             }
+                         });
+                const uint32_t t = __float_as_uint(own[2 * lane + 1].w);
+                if (t != kNoTarget) {
+                    atomicAdd(&U[3 * (size_t)t], (double)ax);
+                    atomicAdd(&U[3 * (size_t)t + 1], (double)ay);
+                    atomicAdd(&U[3 * (size_t)t + 2], (double)az);
+                }
             }
         }
-        if (G.valid) {
-            double ysx = (double)sum[0] - (double)comp[0];
-            double ysy = (double)sum[1] - (double)comp[1];
-            double ysz = (double)sum[2] - (double)comp[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (!G.valid[u]) continue;
+            const uint32_t s = G.s[u];
+            const size_t o = tid[s];
+            const double mux = mu[3 * o], muy = mu[3 * o + 1], muz = mu[3 * o + 2];
+            double ysx = (double)sum[u][0] - (double)comp[u][0];
+            double ysy = (double)sum[u][1] - (double)comp[u][1];
+            double ysz = (double)sum[u][2] - (double)comp[u][2];
             // heavy bodies in FP64: sink side here, source side reduced over the block
             const double X = b.x[o], Y = b.y[o], Z = b.z[o];
 #pragma unroll
@@ -575,9 +739,9 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_adj_group(
                 ysx -= q.m * wx;
                 ysy -= q.m * wy;
                 ysz -= q.m * wz;
-                hx[h][0] = q.m * wx;
-                hx[h][1] = q.m * wy;
-                hx[h][2] = q.m * wz;
+                hx[h][0] += q.m * wx;
+                hx[h][1] += q.m * wy;
+                hx[h][2] += q.m * wz;
             }
             ysink[3 * (size_t)s] = ysx;
             ysink[3 * (size_t)s + 1] = ysy;

@@ -240,15 +240,18 @@ void launch_walk_fp64(const NodeD *rec, const NodeP *recp, const float4 *thi,
                       const float4 *tlo, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
                       double theta, double *acc, uint32_t *err,
                       unsigned long long *counts, cudaStream_t st);
-// Grouped mixed walk: groups of whole leaves, <= 32 bodies, gstart[g]..gstart[g+1] in tree
-// order, boxed in two parts split at gsplit[g]; stk_cap = per-warp stack entries (a multiple
-// of 32).
+// Grouped mixed walk: groups of whole leaves, <= kGroupSinks bodies (two per lane of a warp),
+// gstart[g]..gstart[g+1] in tree order, boxed in two parts split at gsplit[g]; stk_cap =
+// per-warp stack entries (a multiple of 32).
+constexpr int kGroupSinks = 64;
 constexpr int kGroupWarps = 4;
 constexpr int kGroupFlush = 128;
 constexpr int kGroupListCap = kGroupFlush + 32 * 8;
-// shared memory of one warp: interaction list, own-leaf list (split positions), stack
+// shared memory of one warp: interaction list, own-leaf list (two float4 per body: split
+// positions), stack
 __host__ __device__ inline uint32_t group_warp_bytes(uint32_t stk_cap) {
-    return (uint32_t)((kGroupListCap + 64) * sizeof(float4) + stk_cap * sizeof(uint32_t));
+    return (uint32_t)((kGroupListCap + 2 * kGroupSinks) * sizeof(float4) +
+                      stk_cap * sizeof(uint32_t));
 }
 void launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
                        const float4 *trel, const uint32_t *tid, const uint32_t *gstart,

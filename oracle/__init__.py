@@ -151,7 +151,7 @@ class Oracle:
 
     def calc_accel_group(self, bodies, nodes, theta: float = 0.3):
         """FP64 restatement of the grouped walk of the mixed path: sinks in groups of whole
-        leaves (depth-first, <= 32 bodies), node accepted for a group when
+        leaves (depth-first, <= 64 bodies), node accepted for a group when
         size^2 < theta^2 dmin^2 to the group's bounding box.  Returns (acc, counts)."""
         b = self._bodies(bodies)
         nodes = np.ascontiguousarray(nodes, dtype=NODE)

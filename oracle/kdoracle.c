@@ -378,11 +378,13 @@ void orc_walk_counts(const orc_particle *P, const orc_node *nodes, double theta,
 /* ---------------------------------------------------------------- grouped walk */
 
 /* The sink groups of the GPU's grouped mixed walk: whole leaves in depth-first order
- * (left before right), packed greedily up to 32 bodies.  A node is accepted for a whole
+ * (left before right), packed greedily up to ORC_GROUP_MAX bodies.  A node is accepted for a whole
  * group when size^2 < theta^2 dmin^2, dmin the distance from the node's centre of mass to
  * the nearer of the group's two bounding boxes (Barnes 1990, J. Comput. Phys. 87:161); leaves
  * reached are summed pairwise, self excluded by index.  Everything in FP64, each sink's
  * terms added in traversal order. */
+#define ORC_GROUP_MAX 64
+
 static size_t dfs_leaves(const orc_node *nodes, size_t cur, size_t *out, size_t k) {
     if (nodes[cur].num_parts > 0) {
         out[k] = cur;
@@ -470,10 +472,10 @@ static size_t group_split(const orc_node *nodes, size_t n, size_t g0, size_t g1)
 static size_t make_groups(const orc_node *nodes, size_t n_nodes, uint64_t *order,
                           size_t *gstart) {
     size_t *lv = (size_t *)malloc(sizeof(size_t) * (n_nodes + 1));
-    size_t nl = dfs_leaves(nodes, 0, lv, 0), pos = 0, ng = 0, fill = 32;
+    size_t nl = dfs_leaves(nodes, 0, lv, 0), pos = 0, ng = 0, fill = ORC_GROUP_MAX;
     for (size_t k = 0; k < nl; ++k) {
         const orc_node *nd = &nodes[lv[k]];
-        if (fill + nd->num_parts > 32) {
+        if (fill + nd->num_parts > ORC_GROUP_MAX) {
             gstart[ng++] = pos;
             fill = 0;
         }
@@ -504,7 +506,7 @@ int orc_calc_accel_group(const orc_particle *P, size_t n, const orc_node *nodes,
         const uint64_t *sk = order + gstart[g];
         const size_t ns = gstart[g + 1] - gstart[g];
         const size_t sp = group_split(nodes, n, gstart[g], gstart[g + 1]) - gstart[g];
-        double lo[2][3], hi[2][3], a[3 * 32];
+        double lo[2][3], hi[2][3], a[3 * ORC_GROUP_MAX];
         for (int h = 0; h < 2; ++h)
             for (int d = 0; d < 3; ++d) {
                 lo[h][d] = INFINITY;
@@ -870,7 +872,7 @@ int orc_tree_jt_group(const orc_particle *P, size_t n, const orc_node *nodes, si
         const uint64_t *sk = order + gstart[g];
         const size_t ns = gstart[g + 1] - gstart[g];
         const size_t sp = group_split(nodes, n, gstart[g], gstart[g + 1]) - gstart[g];
-        double lo[2][3], hi[2][3], ys[3 * 32];
+        double lo[2][3], hi[2][3], ys[3 * ORC_GROUP_MAX];
         for (int h = 0; h < 2; ++h)
             for (int d = 0; d < 3; ++d) {
                 lo[h][d] = INFINITY;
