@@ -417,7 +417,7 @@ int check_device(kd_ctx *c) {
 
 // Build: multi-block levels, then the shared-memory subtree finish, which also produces the
 // moments and walk records below the local roots; then the nodes above them.  Leaves the
-// bodies in tree order in tpos/tid (and thi/tlo when mixed records are wanted).
+// bodies in tree order in tid, thi and tlo (and tpos when FP64 records are wanted).
 void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     Plan &p = c->plan;
     launch_init_work(c->bodies, c->work, (uint32_t)c->n, c->st);
@@ -438,7 +438,7 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     }
     LocalOut o;
     o.mass = c->bodies.m;
-    o.tpos = c->tpos;
+    o.tpos = want_d ? c->tpos : nullptr;  // FP64 positions: read by the FP64 walk only
     o.tid = c->tid;
     o.thi = c->thi;
     o.tlo = c->tlo;

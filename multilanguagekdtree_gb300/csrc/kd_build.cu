@@ -1344,7 +1344,7 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
         const uint32_t l = S.perm[k];
         const uint32_t id = S.id[l];
         const double x = S.x[l], y = S.y[l], z = S.z[l], mm = S.m[l];
-        o.tpos[s0 + k] = make_double4_32a(x, y, z, mm);
+        if (o.tpos) o.tpos[s0 + k] = make_double4_32a(x, y, z, mm);
         o.tid[s0 + k] = id;
         {
             const float hx = (float)x, hy = (float)y, hz = (float)z;
