@@ -73,19 +73,28 @@ __device__ __forceinline__ void choose_split(const double mn_in[3], const double
         er[d] = 2.4e-7f * (fabsf(a) + fabsf(b)) + 1.2e-7f * fabsf(ef[d]);
         ok = ok && isfinite(ef[d]) && isfinite(er[d]);
     }
+    // the current winner is carried in scalars (no array indexed at run time)
     sd = 0;
+    float bef = ef[0], ber = er[0];
+    double bmx = mx[0], bmn = mn[0];
 #pragma unroll
     for (int d = 1; d < 3; ++d) {
         bool gt;
-        if (ok && ef[d] - er[d] > ef[sd] + er[sd])
+        if (ok && ef[d] - er[d] > bef + ber)
             gt = true;
-        else if (ok && ef[d] + er[d] < ef[sd] - er[sd])
+        else if (ok && ef[d] + er[d] < bef - ber)
             gt = false;
         else
-            gt = __dsub_rn(mx[d], mn[d]) > __dsub_rn(mx[sd], mn[sd]);
-        if (gt) sd = (uint32_t)d;
+            gt = __dsub_rn(mx[d], mn[d]) > __dsub_rn(bmx, bmn);
+        if (gt) {
+            sd = (uint32_t)d;
+            bef = ef[d];
+            ber = er[d];
+            bmx = mx[d];
+            bmn = mn[d];
+        }
     }
-    size = __dsub_rn(mx[sd], mn[sd]);
+    size = __dsub_rn(bmx, bmn);
 }
 
 __device__ __forceinline__ const double *pick(const double *x, const double *y,
@@ -283,8 +292,8 @@ __global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin
     no.size[id] = size;
     SegSel s;
     s.sd = sd;
-    s.lo = trunc_float(mn[sd]);
-    const float range = trunc_float(mx[sd]) - s.lo;
+    s.lo = trunc_float(sd == 0 ? mn[0] : (sd == 1 ? mn[1] : mn[2]));
+    const float range = trunc_float(sd == 0 ? mx[0] : (sd == 1 ? mx[1] : mx[2])) - s.lo;
     const float scale = (float)kHistBins / range;
     s.scale = (range > 0.0f && isfinite(scale)) ? scale : 0.0f;
     s.digit = 0;
@@ -444,8 +453,8 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
             pos = j;
             key = ord_key(w[j]);
         } else {
-            pos = s.cpos[src][start + j];
-            key = s.ckey[src][start + j];
+            pos = (src == 0 ? s.cpos[0] : s.cpos[1])[start + j];
+            key = (src == 0 ? s.ckey[0] : s.ckey[1])[start + j];
         }
     };
 
@@ -522,8 +531,8 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
                 slot = __shfl_sync(kFull, slot, leader);
                 if (hit) {
                     uint32_t o = slot + __popc(m & ((1u << lane) - 1u));
-                    s.ckey[dst][start + o] = key;
-                    s.cpos[dst][start + o] = pos;
+                    (dst == 0 ? s.ckey[0] : s.ckey[1])[start + o] = key;
+                    (dst == 0 ? s.cpos[0] : s.cpos[1])[start + o] = pos;
                 }
             }
         }
@@ -869,18 +878,14 @@ __device__ __forceinline__ double coord(const LocalSmem &S, uint32_t sd, uint32_
     return sd == 0 ? S.x[l] : (sd == 1 ? S.y[l] : S.z[l]);
 }
 
-// Mixed leaf record: origin o = position of the leaf's first body, as hi + lo floats; each
-// body's offset from o is written to trel.
-__device__ __forceinline__ NodeF leaf_nodef(const LocalSmem &S, uint32_t st, uint32_t cn,
+// Mixed leaf record: origin o = position of the leaf's first body, as hi + lo floats.  The
+// leaf's first position is noted in perm2 for every body of the leaf, whose offset from o
+// goes to trel with the tree-ordered bodies.
+__device__ __forceinline__ NodeF leaf_nodef(LocalSmem &S, uint32_t st, uint32_t cn,
                                             uint32_t s0, const LocalOut &o) {
     const uint32_t l0 = S.perm[st];
     const double ox = S.x[l0], oy = S.y[l0], oz = S.z[l0];
-    for (uint32_t k = st; k < st + cn; ++k) {
-        const uint32_t l = S.perm[k];
-        const float fm = is_heavy(S.id[l], o.heavy, o.n_heavy) ? 0.0f : (float)S.m[l];
-        o.trel[s0 + k] = make_float4((float)(S.x[l] - ox), (float)(S.y[l] - oy),
-                                     (float)(S.z[l] - oz), fm);
-    }
+    for (uint32_t k = st; k < st + cn; ++k) S.perm2[k] = (uint16_t)st;
     NodeF r;
     const float hx = (float)ox, hy = (float)oy, hz = (float)oz;
     r.hi = make_float4(hx, hy, hz, 0.0f);
@@ -892,7 +897,8 @@ __device__ __forceinline__ NodeF leaf_nodef(const LocalSmem &S, uint32_t st, uin
     return r;
 }
 
-// Sums of a leaf's bodies (tree positions [st, st+cn) of this block), full and light mass.
+// Sums of a leaf's bodies (tree positions [st, st+cn) of this block): full mass (f, for the
+// FP64 records) and light mass (g, for the mixed records), each only when wanted.
 __device__ __forceinline__ void leaf_sums(const LocalSmem &S, uint32_t st, uint32_t cn,
                                           const LocalOut &o, double f[4], double g[4]) {
     f[0] = f[1] = f[2] = f[3] = 0.0;
@@ -900,10 +906,12 @@ __device__ __forceinline__ void leaf_sums(const LocalSmem &S, uint32_t st, uint3
     for (uint32_t k = st; k < st + cn; ++k) {
         const uint32_t l = S.perm[k];
         const double mm = S.m[l];
-        f[0] += mm;
-        f[1] = fma(mm, S.x[l], f[1]);
-        f[2] = fma(mm, S.y[l], f[2]);
-        f[3] = fma(mm, S.z[l], f[3]);
+        if (o.recd) {
+            f[0] += mm;
+            f[1] = fma(mm, S.x[l], f[1]);
+            f[2] = fma(mm, S.y[l], f[2]);
+            f[3] = fma(mm, S.z[l], f[3]);
+        }
         if (o.recf && !is_heavy(S.id[l], o.heavy, o.n_heavy)) {
             g[0] += mm;
             g[1] = fma(mm, S.x[l], g[1]);
@@ -1094,7 +1102,8 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
             uint32_t r = cn / 2, ccount = cn;
             RadixState rs;
             {
-                const unsigned long long kmin = kmn[sd], kmax = kmx[sd];
+                const unsigned long long kmin = sd == 0 ? kmn[0] : (sd == 1 ? kmn[1] : kmn[2]);
+                const unsigned long long kmax = sd == 0 ? kmx[0] : (sd == 1 ? kmx[1] : kmx[2]);
                 rs.kb = __clzll((long long)(kmin ^ kmax));
                 rs.kp = rs.kb == 0 ? 0ull : (rs.kb == 64 ? kmin : (kmin >> (64 - rs.kb)));
                 rs.ib = 0;
@@ -1319,8 +1328,8 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
                 }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    fs[q] = __dadd_rn(fs[q], f[q]);
-                    gs[q] = __dadd_rn(gs[q], g[q]);
+                    if (want_d) fs[q] = __dadd_rn(fs[q], f[q]);
+                    if (want_f) gs[q] = __dadd_rn(gs[q], g[q]);
                 }
             }
             const double size = no.size[nid];
@@ -1352,6 +1361,11 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
             o.thi[s0 + k] = make_float4(hx, hy, hz, fm);
             o.tlo[s0 + k] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
                                         (float)(z - (double)hz), 0.0f);
+            if (o.recf) {
+                const uint32_t l0 = S.perm[S.perm2[k]];
+                o.trel[s0 + k] = make_float4((float)(x - S.x[l0]), (float)(y - S.y[l0]),
+                                             (float)(z - S.z[l0]), fm);
+            }
         }
     }
 }
