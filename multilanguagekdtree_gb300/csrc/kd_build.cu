@@ -1349,6 +1349,7 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
     }
 
     // ================================================================ tree-ordered bodies
+    __syncthreads();  // leaf starts in perm2 (a root leaf has no level barrier above)
     for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
         const uint32_t l = S.perm[k];
         const uint32_t id = S.id[l];
