@@ -458,8 +458,9 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
         }
     };
 
-    // sort directly only small candidate sets; larger ones take one radix/bin pass first
-    for (int iter = 0; c > (uint32_t)kSortDirect; ++iter) {
+    // refine until at most 32 candidates are left (ranked in one warp below); a pass that
+    // cannot narrow any further (the error path) leaves up to kSelCap for the block sort
+    for (int iter = 0; c > 32u; ++iter) {
         if (iter >= kSelMaxIters) {
             if (threadIdx.x == 0) atomicOr(s.err, kErrSelect);
             c = min(c, (uint32_t)kSelCap);
@@ -543,6 +544,30 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
         __syncthreads();
     }
 
+    if (c <= 32u) {
+        // rank of each candidate among the others by (key, id): the one of rank r is the median
+        if (warp == 0) {
+            unsigned long long key = ~0ull;
+            uint32_t pos = 0, id = kFull;
+            if ((uint32_t)lane < c) {
+                get((uint32_t)lane, key, pos);
+                id = ids[pos];
+            }
+            uint32_t rank = 0;
+            for (uint32_t j = 0; j < c; ++j) {
+                const unsigned long long kj = __shfl_sync(kFull, key, j);
+                const uint32_t ij = __shfl_sync(kFull, id, j);
+                rank += (kj < key || (kj == key && ij < id)) ? 1u : 0u;
+            }
+            if ((uint32_t)lane < c && rank == r) {
+                sel[seg].kmed = key;
+                sel[seg].idmed = id;
+                sel[seg].posmed = pos;
+                no.split_val[nid] = w[pos];
+            }
+        }
+        return;
+    }
     const uint32_t P = next_pow2(c);
     for (uint32_t j = threadIdx.x; j < P; j += blockDim.x) {
         if (j < c) {

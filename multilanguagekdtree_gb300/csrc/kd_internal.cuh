@@ -32,7 +32,6 @@ constexpr int kTileThreads = 256;
 constexpr int kHistBits = 12;       // radix digit of the median select
 constexpr int kHistBins = 1 << kHistBits;
 constexpr int kSelCap = 2048;       // capacity of the select's shared-memory sort
-constexpr int kSortDirect = 256;    // candidate sets this small are sorted without a pass
 #ifndef KD_SEL_THREADS
 #define KD_SEL_THREADS 512
 #endif
