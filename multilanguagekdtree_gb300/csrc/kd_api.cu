@@ -420,7 +420,9 @@ int check_device(kd_ctx *c) {
 // bodies in tree order in tid, thi and tlo (and tpos when FP64 records are wanted).
 void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     Plan &p = c->plan;
-    launch_init_work(c->bodies, c->work, (uint32_t)c->n, c->st);
+    const bool levels = !p.glevels.empty();
+    launch_init_work(c->bodies, c->work, (uint32_t)c->n, levels ? c->scr.bmin[0] : nullptr,
+                     levels ? c->scr.bmax[0] : nullptr, c->st);
     c->launches += 3;  // init + local finish + upward pass
     int cur = 0;
     for (size_t l = 0; l < p.glevels.size(); ++l) {
@@ -433,7 +435,7 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
         lv.med_pos = nullptr;
         const uint32_t G_next = l + 1 < p.glevels.size() ? (uint32_t)p.glevels[l + 1].size() : 0u;
         c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, (int)l, G_next,
-                                    c->st);
+                                    c->st, true);
         cur ^= 1;
     }
     LocalOut o;

@@ -132,21 +132,70 @@ __device__ __forceinline__ uint32_t next_pow2(uint32_t v) {
 
 // ------------------------------------------------------------------ work init
 
-__global__ void k_init_work(Bodies b, double *wx, double *wy, double *wz, uint32_t *wid,
-                            uint32_t n) {
+template <typename T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(kFull, v, o));
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
+    return v;
+}
+// The build's first work arrays (positions and body ids in original order); with `bmin` set,
+// also the bounding box of the whole set (segment 0 of level 0) on ordered keys.
+__global__ __launch_bounds__(256) void k_init_work(Bodies b, double *wx, double *wy, double *wz,
+                                                   uint32_t *wid, uint32_t n,
+                                                   unsigned long long *bmin,
+                                                   unsigned long long *bmax) {
+    unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += gridDim.x * blockDim.x) {
-        wx[i] = b.x[i];
-        wy[i] = b.y[i];
-        wz[i] = b.z[i];
+        const double x = b.x[i], y = b.y[i], z = b.z[i];
+        wx[i] = x;
+        wy[i] = y;
+        wz[i] = z;
         wid[i] = i;
+        const unsigned long long k0 = ord_key(x), k1 = ord_key(y), k2 = ord_key(z);
+        mn[0] = min(mn[0], k0); mx[0] = max(mx[0], k0);
+        mn[1] = min(mn[1], k1); mx[1] = max(mx[1], k1);
+        mn[2] = min(mn[2], k2); mx[2] = max(mx[2], k2);
+    }
+    if (!bmin) return;
+    __shared__ unsigned long long red[8][6];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        mn[d] = warp_min(mn[d]);
+        mx[d] = warp_max(mx[d]);
+    }
+    if (lane == 0) {
+        for (int d = 0; d < 3; ++d) { red[warp][d] = mn[d]; red[warp][3 + d] = mx[d]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int d = threadIdx.x;
+        unsigned long long a = ~0ull, c = 0ull;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            a = min(a, red[w][d]);
+            c = max(c, red[w][3 + d]);
+        }
+        atomicMin(&bmin[d], a);
+        atomicMax(&bmax[d], c);
     }
 }
 
-void launch_init_work(const Bodies &b, Work &w, uint32_t n, cudaStream_t st) {
+void launch_init_work(const Bodies &b, Work &w, uint32_t n, unsigned long long *bmin,
+                      unsigned long long *bmax, cudaStream_t st) {
     int blocks = (int)((n + 255) / 256);
-    if (blocks > 4096) blocks = 4096;
-    k_init_work<<<blocks, 256, 0, st>>>(b, w.x[0], w.y[0], w.z[0], w.id[0], n);
+    if (blocks > 2432) blocks = 2432;  // 16 per SM: a few thousand box atomics in all
+    if (bmin) {
+        cudaMemsetAsync(bmin, 0xff, sizeof(unsigned long long) * 3, st);
+        cudaMemsetAsync(bmax, 0x00, sizeof(unsigned long long) * 3, st);
+    }
+    k_init_work<<<blocks, 256, 0, st>>>(b, w.x[0], w.y[0], w.z[0], w.id[0], n, bmin, bmax);
 }
 
 __global__ void k_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx,
@@ -200,18 +249,6 @@ __device__ __forceinline__ bool tile_of(const Topology &t, const LevelArgs &lv, 
     return true;
 }
 
-template <typename T>
-__device__ __forceinline__ T warp_min(T v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(kFull, v, o));
-    return v;
-}
-template <typename T>
-__device__ __forceinline__ T warp_max(T v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
-    return v;
-}
 __device__ __forceinline__ double warp_fmin(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(kFull, v, o));
@@ -798,7 +835,7 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
 }
 
 int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
-                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st) {
+                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready) {
     const int nxt = cur ^ 1;
     const uint32_t G = lv.G;
     const uint32_t grid = G * lv.tiles;
@@ -806,7 +843,7 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
     unsigned long long *nbmin = G_next ? s.bmin[(lvl + 1) & 1] : nullptr;
     unsigned long long *nbmax = G_next ? s.bmax[(lvl + 1) & 1] : nullptr;
     int launched = 5;
-    if (lvl == 0) {
+    if (lvl == 0 && !box0_ready) {
         cudaMemsetAsync(bmin, 0xff, sizeof(unsigned long long) * 3 * G, st);
         cudaMemsetAsync(bmax, 0x00, sizeof(unsigned long long) * 3 * G, st);
         k_bbox<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], bmin, bmax);

@@ -213,18 +213,20 @@ __device__ __forceinline__ NodeP make_nodep(const NodeD &q) {
     return p;
 }
 
-void launch_init_work(const Bodies &b, Work &w, uint32_t n, cudaStream_t st);
+// Work arrays of the build; with bmin/bmax set, also the level-0 bounding box into them.
+void launch_init_work(const Bodies &b, Work &w, uint32_t n, unsigned long long *bmin,
+                      unsigned long long *bmax, cudaStream_t st);
 // quickselect set-up: key[i] = vals[idx[i]], id[i] = idx[i]; flags an index >= n_vals
 void launch_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx, uint32_t n,
                         double *key, uint32_t *id, uint32_t *err, cudaStream_t st);
 // puts the selected element at position `goal` (it was written at *med_pos)
 void launch_place_selected(uint32_t *id, const uint32_t *med_pos, uint32_t goal, cudaStream_t st);
 // One multi-block level.  `lvl` selects the bounding-box buffers (lvl & 1); the boxes of
-// level 0 are computed here, deeper levels receive theirs from the previous level's scatter
-// (`G_next` > 0 when the next level is a multi-block level too).  Returns the number of
-// kernels launched.
+// level 0 are computed here unless `box0_ready` (launch_init_work made them), deeper levels
+// receive theirs from the previous level's scatter (`G_next` > 0 when the next level is a
+// multi-block level too).  Returns the number of kernels launched.
 int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
-                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st);
+                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready = false);
 // Subtree finish of every local root: split decisions, tree order, and the moments and
 // walk records of all nodes below the local roots.
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
