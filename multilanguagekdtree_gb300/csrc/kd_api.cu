@@ -796,13 +796,32 @@ void kd_destroy(kd_ctx *c) {
     delete c;
 }
 
+// Device-accessible address of a page-locked host buffer (registered or allocated pinned),
+// 16-byte aligned as the transfer kernels' vector accesses need; nullptr for pageable or
+// device memory and for other alignments.
+static void *pinned_device_view(const void *p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // an address CUDA does not know: clear the (non-sticky) error
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    return (reinterpret_cast<uintptr_t>(at.devicePointer) & 15u) == 0 ? at.devicePointer
+                                                                      : nullptr;
+}
+
 int kd_set_bodies(kd_ctx *c, const kd_particle_c *bodies, size_t n) {
     if (!c) return KD_EINVAL;
     if (!bodies || n != c->n) return c->fail(KD_EINVAL, "expected %zu bodies", c->n);
     KD_CHECK(c, cudaSetDevice(c->prm.device));
-    KD_CHECK(c, cudaMemcpyAsync(c->aos, bodies, n * sizeof(kd_particle_c),
-                                cudaMemcpyHostToDevice, c->st));
-    launch_aos_to_soa(c->aos, c->bodies, (uint32_t)n, c->dev_err, c->st);
+    // pinned records are read in place by the converting kernel; others are staged
+    if (const void *view = pinned_device_view(bodies)) {
+        launch_host_to_soa(view, c->bodies, (uint32_t)n, c->dev_err, c->st);
+    } else {
+        KD_CHECK(c, cudaMemcpyAsync(c->aos, bodies, n * sizeof(kd_particle_c),
+                                    cudaMemcpyHostToDevice, c->st));
+        launch_aos_to_soa(c->aos, c->bodies, (uint32_t)n, c->dev_err, c->st);
+    }
     return accept_bodies(c);
 }
 
@@ -821,9 +840,13 @@ int kd_get_bodies(kd_ctx *c, kd_particle_c *bodies, size_t n) {
     if (!bodies || n != c->n) return c->fail(KD_EINVAL, "expected %zu bodies", c->n);
     if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
     KD_CHECK(c, cudaSetDevice(c->prm.device));
-    launch_soa_to_aos(c->bodies, c->aos, (uint32_t)n, c->st);
-    KD_CHECK(c, cudaMemcpyAsync(bodies, c->aos, n * sizeof(kd_particle_c),
-                                cudaMemcpyDeviceToHost, c->st));
+    if (void *view = pinned_device_view(bodies)) {
+        launch_soa_to_host(c->bodies, view, (uint32_t)n, c->st);
+    } else {
+        launch_soa_to_aos(c->bodies, c->aos, (uint32_t)n, c->st);
+        KD_CHECK(c, cudaMemcpyAsync(bodies, c->aos, n * sizeof(kd_particle_c),
+                                    cudaMemcpyDeviceToHost, c->st));
+    }
     KD_CHECK(c, cudaStreamSynchronize(c->st));
     return KD_OK;
 }

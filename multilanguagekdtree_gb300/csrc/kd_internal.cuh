@@ -266,6 +266,10 @@ void launch_energy_partial(const Bodies &b, const double *phi, uint32_t n, doubl
 void launch_kick_drift(Bodies &b, double *acc, uint32_t n, double dt, cudaStream_t st);
 void launch_aos_to_soa(const void *aos, Bodies &b, uint32_t n, uint32_t *err, cudaStream_t st);
 void launch_soa_to_aos(const Bodies &b, void *aos, uint32_t n, cudaStream_t st);
+// The same conversions reading or writing pinned host records directly (a device-accessible
+// address of page-locked host memory), at the host link's rate, with no device staging copy.
+void launch_host_to_soa(const void *host, Bodies &b, uint32_t n, uint32_t *err, cudaStream_t st);
+void launch_soa_to_host(const Bodies &b, void *host, uint32_t n, cudaStream_t st);
 // FP64 direct sum for ns sinks; `partial` holds ns * ceil(n / kDirectChunk) * 3 doubles
 constexpr uint32_t kDirectChunk = 1u << 18;
 constexpr int kDirectThreads = 128;

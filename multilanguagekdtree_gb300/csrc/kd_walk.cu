@@ -295,6 +295,77 @@ void launch_soa_to_aos(const Bodies &b, void *aos, uint32_t n, cudaStream_t st) 
     k_soa_to_aos<<<blocks, 256, 0, st>>>(b, static_cast<double *>(aos), n);
 }
 
+// Direct transfers between pinned host records and the device's SoA state: a block moves 256
+// records (16 KB) through shared memory, so the host side is read or written as consecutive
+// 16-byte chunks by consecutive threads, and the conversion costs no pass of its own.
+constexpr int kXferRecords = 256;
+
+__global__ __launch_bounds__(kXferRecords) void k_host_to_soa(const float4 *__restrict__ host,
+                                                              Bodies b, uint32_t n,
+                                                              uint32_t *err) {
+    __shared__ float4 buf[4 * kXferRecords];
+    bool bad = false;
+    for (uint32_t r0 = blockIdx.x * kXferRecords; r0 < n; r0 += gridDim.x * kXferRecords) {
+        const uint32_t cnt = min((uint32_t)kXferRecords, n - r0);
+        const float4 *src = host + 4 * (size_t)r0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t q = threadIdx.x + k * kXferRecords;
+            if (q < 4 * cnt) buf[q] = src[q];
+        }
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            const double2 *p = reinterpret_cast<const double2 *>(buf + 4 * threadIdx.x);
+            const double2 a0 = p[0], a1 = p[1], a2 = p[2], a3 = p[3];
+            const uint32_t i = r0 + threadIdx.x;
+            b.x[i] = a0.x; b.y[i] = a0.y; b.z[i] = a1.x;
+            b.vx[i] = a1.y; b.vy[i] = a2.x; b.vz[i] = a2.y;
+            b.r[i] = a3.x; b.m[i] = a3.y;
+            bad |= !(isfinite(a0.x) && isfinite(a0.y) && isfinite(a1.x) && isfinite(a1.y) &&
+                     isfinite(a2.x) && isfinite(a2.y) && isfinite(a3.y) && a3.y >= 0.0);
+        }
+        __syncthreads();
+    }
+    if (bad) atomicOr(err, kErrNumeric);
+}
+
+__global__ __launch_bounds__(kXferRecords) void k_soa_to_host(Bodies b, float4 *__restrict__ host,
+                                                              uint32_t n) {
+    __shared__ float4 buf[4 * kXferRecords];
+    for (uint32_t r0 = blockIdx.x * kXferRecords; r0 < n; r0 += gridDim.x * kXferRecords) {
+        const uint32_t cnt = min((uint32_t)kXferRecords, n - r0);
+        if (threadIdx.x < cnt) {
+            const uint32_t i = r0 + threadIdx.x;
+            double2 *p = reinterpret_cast<double2 *>(buf + 4 * threadIdx.x);
+            p[0] = make_double2(b.x[i], b.y[i]);
+            p[1] = make_double2(b.z[i], b.vx[i]);
+            p[2] = make_double2(b.vy[i], b.vz[i]);
+            p[3] = make_double2(b.r[i], b.m[i]);
+        }
+        __syncthreads();
+        float4 *dst = host + 4 * (size_t)r0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t q = threadIdx.x + k * kXferRecords;
+            if (q < 4 * cnt) dst[q] = buf[q];
+        }
+        __syncthreads();
+    }
+}
+
+void launch_host_to_soa(const void *host, Bodies &b, uint32_t n, uint32_t *err,
+                        cudaStream_t st) {
+    int blocks = (int)((n + kXferRecords - 1) / kXferRecords);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_host_to_soa<<<blocks, kXferRecords, 0, st>>>(static_cast<const float4 *>(host), b, n, err);
+}
+
+void launch_soa_to_host(const Bodies &b, void *host, uint32_t n, cudaStream_t st) {
+    int blocks = (int)((n + kXferRecords - 1) / kXferRecords);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_soa_to_host<<<blocks, kXferRecords, 0, st>>>(b, static_cast<float4 *>(host), n);
+}
+
 // ------------------------------------------------------------------ direct sum
 
 // Sinks are spread one per thread; sources are swept in chunks of kDirectChunk bodies, one
