@@ -320,9 +320,9 @@ def run_ours(a, ws, rank, local):
     line["phases_ms_per_step"] = {k: ph[k] / 2 for k in ("build_ms", "moments_ms", "walk_ms",
                                                          "kick_ms")}
     line["interactions_per_body"] = {k: v / n for k, v in cnt.items()}
-    # DRAM bytes per launch: one-pass ncu capture of the 10M-body walk (4.28 GB read +
-    # 0.475 GB written, 476 B per body), scaled by the number of bodies
-    walk_traffic = 476.0 * n
+    # DRAM bytes per launch: one-pass ncu capture of the 10M-body walk (4.31 GB read +
+    # 0.475 GB written, 479 B per body), scaled by the number of bodies
+    walk_traffic = 479.0 * n
     line["roofline"] = {
         "kernel": "k_walk_group", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
         "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": walk_traffic,

@@ -435,7 +435,7 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
         lv.med_pos = nullptr;
         const uint32_t G_next = l + 1 < p.glevels.size() ? (uint32_t)p.glevels[l + 1].size() : 0u;
         c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, (int)l, G_next,
-                                    c->st, true);
+                                    c->st, true, p.gmax[l]);
         cur ^= 1;
     }
     LocalOut o;

@@ -834,8 +834,18 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
     }
 }
 
+// Levels whose segments hold at most kWarpSelMax bodies choose their splits and medians in
+// k_split_select_warp (one warp per segment; defined with the subtree finish below).
+constexpr uint32_t kWarpSelMax = 4096;
+constexpr int kWarpSelWarps = 8;
+__global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
+    Topology t, LevelArgs lv, const unsigned long long *bmin, const unsigned long long *bmax,
+    const double *wx, const double *wy, const double *wz, const uint32_t *wid, SegSel *sel,
+    NodeOut no, uint32_t *err);
+
 int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
-                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready) {
+                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready,
+                 uint32_t seg_max) {
     const int nxt = cur ^ 1;
     const uint32_t G = lv.G;
     const uint32_t grid = G * lv.tiles;
@@ -853,7 +863,14 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
         cudaMemsetAsync(nbmin, 0xff, sizeof(unsigned long long) * 3 * G_next, st);
         cudaMemsetAsync(nbmax, 0x00, sizeof(unsigned long long) * 3 * G_next, st);
     }
-    k_split<<<(G + 127) / 128, 128, 0, st>>>(t, lv, bmin, bmax, s.sel, no);
+    if (!lv.multi && seg_max <= kWarpSelMax) {
+        k_split_select_warp<<<(G + kWarpSelWarps - 1) / kWarpSelWarps, kWarpSelWarps * 32, 0,
+                              st>>>(t, lv, bmin, bmax, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
+                                    s.sel, no, s.err);
+        --launched;
+    } else {
+        k_split<<<(G + 127) / 128, 128, 0, st>>>(t, lv, bmin, bmax, s.sel, no);
+    }
     if (lv.multi) {
         cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * kHistBins * (size_t)G, st);
         cudaMemsetAsync(s.cand_cnt, 0, sizeof(uint32_t) * G, st);
@@ -864,8 +881,9 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
                                                  s.cand_cnt, s.ckey[0], s.cpos[0]);
         launched += 3;
     }
-    k_select<<<G, kSelThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur], s.sel,
-                                        s, no);
+    if (lv.multi || seg_max > kWarpSelMax)
+        k_select<<<G, kSelThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
+                                            s.sel, s, no);
     k_part_count<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
                                                 s.sel, s.tile_cnt);
     k_tile_scan<<<G, 256, 0, st>>>(t, lv, s.tile_cnt, s.tile_off, s.err);
@@ -935,6 +953,159 @@ struct RadixState {
         }
     }
 };
+
+// Split choice and exact median of a level's segments when they are small (at most
+// kWarpSelMax bodies): one warp per segment, no block barrier.  Lane 0 chooses the split as
+// k_split does; the warp then narrows the (key, id) candidates with 8-bit radix passes over a
+// warp-private histogram, as the subtree finish does for its larger nodes, until at most 32
+// remain, and ranks those by comparison.  Writes the segment's SegSel and node fields.
+__global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
+    Topology t, LevelArgs lv, const unsigned long long *bmin, const unsigned long long *bmax,
+    const double *wx, const double *wy, const double *wz, const uint32_t *wid, SegSel *sel,
+    NodeOut no, uint32_t *err) {
+    __shared__ uint32_t hist[kWarpSelWarps][256];
+    __shared__ unsigned long long ckey[kWarpSelWarps][32];
+    __shared__ uint32_t cid[kWarpSelWarps][32], cpos[kWarpSelWarps][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t seg = blockIdx.x * kWarpSelWarps + warp;
+    if (seg >= lv.G) return;  // warp-uniform; no block barrier below
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t nid = lv.ids[seg];
+    const uint32_t start = t.start[nid], cn = t.count[nid];
+    uint32_t sd = 0;
+    if (lane == 0) {
+        double mn[3], mx[3];
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = ord_val(bmin[seg * 3 + d]);
+            mx[d] = ord_val(bmax[seg * 3 + d]);
+        }
+        double size;
+        choose_split(mn, mx, sd, size);
+        no.split_dim[nid] = (uint8_t)sd;
+        no.size[nid] = size;
+    }
+    sd = __shfl_sync(kFull, sd, 0);
+    const double *w = pick(wx, wy, wz, sd) + start;
+    const uint32_t *ids = wid + start;
+    const unsigned long long kmin = bmin[seg * 3 + sd], kmax = bmax[seg * 3 + sd];
+    const uint32_t rank0 = split_rank(lv, cn);
+    uint32_t r = rank0, ccount = cn;
+    RadixState rs;
+    rs.kb = __clzll((long long)(kmin ^ kmax));
+    rs.kp = rs.kb == 0 ? 0ull : (rs.kb == 64 ? kmin : (kmin >> (64 - rs.kb)));
+    rs.ib = 0;
+    rs.ip = 0;
+    uint32_t *h = hist[warp];
+    while (ccount > 32) {
+        if (rs.kb == 64 && rs.ib == 32) {  // cannot happen with distinct ids
+            if (lane == 0) atomicOr(err, kErrSelect);
+            break;
+        }
+        const int wd = rs.width();
+#pragma unroll
+        for (int q = 0; q < 8; ++q) h[lane * 8 + q] = 0u;
+        __syncwarp();
+        for (uint32_t k = lane; k < cn; k += 32) {
+            const unsigned long long key = ord_key(w[k]);
+            const uint32_t id = ids[k];
+            if (rs.match(key, id)) atomicAdd(&h[rs.digit(key, id, wd)], 1u);
+        }
+        __syncwarp();
+        uint32_t mine = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) mine += h[lane * 8 + q];
+        uint32_t inc = mine;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(kFull, inc, off);
+            if (lane >= off) inc += v;
+        }
+        const uint32_t before = inc - mine;
+        uint32_t dsel = 0, below = 0, cnt = 0;
+        const bool owner = r >= before && r < inc;
+        if (owner) {
+            uint32_t cum = before;
+            for (int q = 0; q < 8; ++q) {
+                const uint32_t c = h[lane * 8 + q];
+                if (r < cum + c) {
+                    dsel = (uint32_t)(lane * 8 + q);
+                    below = cum;
+                    cnt = c;
+                    break;
+                }
+                cum += c;
+            }
+        }
+        const uint32_t om = __ballot_sync(kFull, owner);
+        if (!om) {  // the wanted rank is not among the candidates: a failed select
+            if (lane == 0) atomicOr(err, kErrSelect);
+            break;
+        }
+        const int src = __ffs(om) - 1;
+        dsel = __shfl_sync(kFull, dsel, src);
+        below = __shfl_sync(kFull, below, src);
+        cnt = __shfl_sync(kFull, cnt, src);
+        rs.fix(dsel, wd);
+        r -= below;
+        ccount = cnt;
+        __syncwarp();
+    }
+    // gather the <= 32 candidates, then rank them by comparison
+    uint32_t ng = 0;
+    for (uint32_t base = 0; base < cn; base += 32) {
+        const uint32_t k = base + lane;
+        bool hit = false;
+        unsigned long long key = 0;
+        uint32_t id = 0;
+        if (k < cn) {
+            key = ord_key(w[k]);
+            id = ids[k];
+            hit = rs.match(key, id);
+        }
+        const uint32_t m = __ballot_sync(kFull, hit);
+        if (hit) {
+            const uint32_t off = ng + __popc(m & lt);
+            if (off < 32) {
+                ckey[warp][off] = key;
+                cid[warp][off] = id;
+                cpos[warp][off] = k;
+            }
+        }
+        ng += __popc(m);
+    }
+    __syncwarp();
+    const bool have = (uint32_t)lane < min(ng, 32u);
+    const unsigned long long mk = have ? ckey[warp][lane] : ~0ull;
+    const uint32_t mi = have ? cid[warp][lane] : kFull;
+    uint32_t rank = 0;
+    for (int q = 0; q < 32; ++q) {
+        const unsigned long long ok = __shfl_sync(kFull, mk, q);
+        const uint32_t oi = __shfl_sync(kFull, mi, q);
+        rank += (ok < mk || (ok == mk && oi < mi)) ? 1u : 0u;
+    }
+    const uint32_t wm = __ballot_sync(kFull, have && rank == r);
+    if (!wm) {
+        if (lane == 0) atomicOr(err, kErrSelect);
+        return;
+    }
+    if (lane == __ffs(wm) - 1) {
+        const uint32_t pos = cpos[warp][lane];
+        SegSel s;
+        s.sd = sd;
+        s.scale = 0.0f;
+        s.digit = 0;
+        s.c = cn;
+        s.r = rank0;
+        s.pad = 0;
+        s.kmed = mk;
+        s.idmed = mi;
+        s.posmed = pos;
+        s.lo = 0.0f;
+        s.pad2 = 0;
+        sel[seg] = s;
+        no.split_val[nid] = w[pos];
+    }
+}
 
 __device__ __forceinline__ double coord(const LocalSmem &S, uint32_t sd, uint32_t l) {
     return sd == 0 ? S.x[l] : (sd == 1 ? S.y[l] : S.z[l]);

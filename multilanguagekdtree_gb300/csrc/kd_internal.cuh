@@ -224,9 +224,11 @@ void launch_place_selected(uint32_t *id, const uint32_t *med_pos, uint32_t goal,
 // One multi-block level.  `lvl` selects the bounding-box buffers (lvl & 1); the boxes of
 // level 0 are computed here unless `box0_ready` (launch_init_work made them), deeper levels
 // receive theirs from the previous level's scatter (`G_next` > 0 when the next level is a
-// multi-block level too).  Returns the number of kernels launched.
+// multi-block level too).  `seg_max`: the level's largest segment (small segments take a
+// warp each for split and median).  Returns the number of kernels launched.
 int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
-                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready = false);
+                 Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready = false,
+                 uint32_t seg_max = 0xffffffffu);
 // Subtree finish of every local root: split decisions, tree order, and the moments and
 // walk records of all nodes below the local roots.
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
