@@ -557,19 +557,19 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
         double ay = (double)sum[u][1] - (double)comp[u][1];
         double az = (double)sum[u][2] - (double)comp[u][2];
         double ph = (double)sum[u][3] - (double)comp[u][3];
-        // heavy bodies in FP64, pair kernel of array_particle.rs:67-76
+        // heavy bodies in FP64: the pair kernel of array_particle.rs:67-76 with 1/|d| from
+        // rsqrt64 (a few ulp) in place of the square root and division
         const double px64 = b.x[o], py64 = b.y[o], pz64 = b.z[o];
         for (int hh = 0; hh < n_heavy; ++hh) {
             if (heavy_ids[hh] == o) continue;
             const Heavy q = heavy[hh];
             const double dx = px64 - q.x, dy = py64 - q.y, dz = pz64 - q.z;
-            const double dp2 = dx * dx + dy * dy + dz * dz;
-            const double dist = sqrt(dp2);
-            const double magi = -q.m / (dist * dist * dist);
-            ax += magi * dx;
-            ay += magi * dy;
-            az += magi * dz;
-            if (kPot) ph -= q.m / dist;
+            const double ri = inv_dist(fma(dx, dx, fma(dy, dy, dz * dz)));
+            const double magi = -q.m * (ri * ri * ri);
+            ax = fma(magi, dx, ax);
+            ay = fma(magi, dy, ay);
+            az = fma(magi, dz, az);
+            if (kPot) ph -= q.m * ri;
         }
         acc[3 * (size_t)o] = ax;
         acc[3 * (size_t)o + 1] = ay;
@@ -729,9 +729,9 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
                 if (h >= n_heavy || heavy_ids[h] == o) continue;
                 const Heavy q = heavy[h];
                 const double dx = X - q.x, dy = Y - q.y, dz = Z - q.z;
-                const double d2 = dx * dx + dy * dy + dz * dz;
-                const double inv2 = 1.0 / d2;
-                const double inv3 = inv2 * sqrt(inv2);
+                const double ri = inv_dist(fma(dx, dx, fma(dy, dy, dz * dz)));
+                const double inv2 = ri * ri;
+                const double inv3 = inv2 * ri;
                 const double dm = dx * mux + dy * muy + dz * muz;
                 const double c3 = 3.0 * dm * inv2;
                 const double wx = inv3 * (mux - c3 * dx), wy = inv3 * (muy - c3 * dy),

@@ -75,6 +75,24 @@ struct __align__(16) NodeF {
     uint32_t a, b, pad0, pad1;
 };
 
+// 1/sqrt(x) for x in [1e-30, 1e30]: the FP32 hardware estimate, then two Newton steps in
+// FP64 (quadratic convergence from ~2^-23 to a few ulp).
+__device__ __forceinline__ double rsqrt64(double x) {
+    float f;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"((float)x));
+    const double h = 0.5 * x;
+    double y = (double)f;
+    y = y * fma(-h * y, y, 1.5);
+    y = y * fma(-h * y, y, 1.5);
+    return y;
+}
+
+// 1/sqrt(x) by rsqrt64 inside its range, else by the rounded square root and division
+// (x = 0 gives inf, as the reference's coincident bodies do).
+__device__ __forceinline__ double inv_dist(double x) {
+    return (x >= 1e-30 && x <= 1e30) ? rsqrt64(x) : __ddiv_rn(1.0, __dsqrt_rn(x));
+}
+
 // Per-segment state of the median select at one level of the multi-block build.
 struct SegSel {
     uint32_t sd;      // split dimension

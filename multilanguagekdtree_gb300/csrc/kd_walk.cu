@@ -27,20 +27,9 @@ __device__ __forceinline__ void load_noded(const NodeD *rec, uint32_t node, doub
     b = ab.y;
 }
 
-// 1/sqrt(x) for x in [1e-30, 1e30]: the FP32 hardware estimate, then two Newton steps in
-// FP64 (quadratic convergence from ~2^-23 to a few ulp), in place of the reference's
-// sqrt and division: the interaction magnitude m / (d^2 sqrt(d^2)) = m r^3 differs from the
-// IEEE-rounded one by a few ulp.
-__device__ __forceinline__ double rsqrt64(double x) {
-    float f;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"((float)x));
-    const double h = 0.5 * x;
-    double y = (double)f;
-    y = y * fma(-h * y, y, 1.5);
-    y = y * fma(-h * y, y, 1.5);
-    return y;
-}
-
+// (rsqrt64, in kd_internal.cuh, stands in for the reference's sqrt and division: the
+// interaction magnitude m / (d^2 sqrt(d^2)) = m r^3 differs from the IEEE-rounded one by a
+// few ulp.)
 // m / |d|^3 as the reference forms it (array_kd_tree.rs:607, array_particle.rs:72-73), or
 // by rsqrt64 when d2 is in its range; d2 = 0 keeps the reference's inf.
 __device__ __forceinline__ double inv_cube(double d2) {
