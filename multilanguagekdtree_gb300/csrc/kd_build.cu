@@ -237,9 +237,10 @@ struct TileRef {
     uint32_t seg, tile, id, start, cnt, lo, hi;
 };
 
-__device__ __forceinline__ bool tile_of(const Topology &t, const LevelArgs &lv, TileRef &r) {
-    r.seg = blockIdx.x / lv.tiles;
-    r.tile = blockIdx.x - r.seg * lv.tiles;
+__device__ __forceinline__ bool tile_at(const Topology &t, const LevelArgs &lv, uint32_t idx,
+                                        TileRef &r) {
+    r.seg = idx / lv.tiles;
+    r.tile = idx - r.seg * lv.tiles;
     r.id = lv.ids[r.seg];
     r.start = t.start[r.id];
     r.cnt = t.count[r.id];
@@ -247,6 +248,10 @@ __device__ __forceinline__ bool tile_of(const Topology &t, const LevelArgs &lv, 
     if (r.lo >= r.cnt) return false;
     r.hi = min(r.cnt, r.lo + (uint32_t)kTile);
     return true;
+}
+
+__device__ __forceinline__ bool tile_of(const Topology &t, const LevelArgs &lv, TileRef &r) {
+    return tile_at(t, lv, blockIdx.x, r);
 }
 
 __device__ __forceinline__ double warp_fmin(double v) {
@@ -344,19 +349,38 @@ __global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin
 }
 
 // First pass over big segments: histogram of linear bins of the split coordinate.
+// A block takes kHistTiles consecutive tiles of one segment, so that zeroing its
+// kHistBins shared bins and merging them into the segment's histogram is paid once per
+// kHistTiles * kTile bodies.
+constexpr uint32_t kHistTiles = 4;
+
 __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
                                                        const double *wx, const double *wy,
                                                        const double *wz, const SegSel *sel,
                                                        uint32_t *hist) {
+    const uint32_t per_seg = (lv.tiles + kHistTiles - 1) / kHistTiles;
+    const uint32_t seg = blockIdx.x / per_seg;
+    const uint32_t t0 = (blockIdx.x - seg * per_seg) * kHistTiles;
     TileRef r;
-    if (!tile_of(t, lv, r)) return;
+    if (!tile_at(t, lv, seg * lv.tiles + t0, r)) return;  // block-uniform
+    const uint32_t hi = min(r.cnt, r.lo + kHistTiles * (uint32_t)kTile);
     __shared__ uint32_t h[kHistBins];
     for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) h[b] = 0;
     __syncthreads();
     const SegSel s = sel[r.seg];
     const double *w = pick(wx, wy, wz, s.sd) + r.start;
-    for (uint32_t k = r.lo + threadIdx.x; k < r.hi; k += blockDim.x) {
-        atomicAdd(&h[lin_bin(w[k], s.lo, s.scale)], 1u);
+    constexpr int kRows = kTile / kTileThreads;
+    for (uint32_t base = r.lo; base < hi; base += kTile) {
+        double v[kRows];
+#pragma unroll
+        for (int i = 0; i < kRows; ++i) {
+            const uint32_t k = base + (uint32_t)i * kTileThreads + threadIdx.x;
+            v[i] = k < hi ? w[k] : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < kRows; ++i)
+            if (base + (uint32_t)i * kTileThreads + threadIdx.x < hi)
+                atomicAdd(&h[lin_bin(v[i], s.lo, s.scale)], 1u);
     }
     __syncthreads();
     uint32_t *gh = hist + (size_t)r.seg * kHistBins;
@@ -437,10 +461,18 @@ __global__ __launch_bounds__(kTileThreads) void k_collect(Topology t, LevelArgs 
     const SegSel s = sel[r.seg];
     const double *w = pick(wx, wy, wz, s.sd) + r.start;
     const int lane = threadIdx.x & 31;
-    for (uint32_t base = r.lo; base < r.hi; base += blockDim.x) {
-        uint32_t k = base + threadIdx.x;
+    constexpr int kRows = kTile / kTileThreads;
+    double vr[kRows];
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+        const uint32_t k = r.lo + (uint32_t)i * kTileThreads + threadIdx.x;
+        vr[i] = k < r.hi ? w[k] : 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+        const uint32_t k = r.lo + (uint32_t)i * kTileThreads + threadIdx.x;
         bool in = k < r.hi;
-        const double v = in ? w[k] : 0.0;
+        const double v = vr[i];
         const unsigned long long key = ord_key(v);
         bool hit = in && lin_bin(v, s.lo, s.scale) == s.digit;
         uint32_t m = __ballot_sync(kFull, hit);
@@ -646,9 +678,20 @@ __global__ __launch_bounds__(kTileThreads) void k_part_count(Topology t, LevelAr
     const SegSel s = sel[r.seg];
     const double *w = pick(wx, wy, wz, s.sd) + r.start;
     const uint32_t *ids = wid + r.start;
+    constexpr int kRows = kTile / kTileThreads;
+    double v[kRows];
+    uint32_t q[kRows];
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+        const uint32_t k = r.lo + (uint32_t)i * kTileThreads + threadIdx.x;
+        v[i] = k < r.hi ? w[k] : 0.0;
+        q[i] = k < r.hi ? ids[k] : 0u;
+    }
     uint32_t cnt = 0;
-    for (uint32_t k = r.lo + threadIdx.x; k < r.hi; k += blockDim.x)
-        cnt += goes_left(ord_key(w[k]), ids[k], s.kmed, s.idmed) ? 1u : 0u;
+#pragma unroll
+    for (int i = 0; i < kRows; ++i)
+        if (r.lo + (uint32_t)i * kTileThreads + threadIdx.x < r.hi)
+            cnt += goes_left(ord_key(v[i]), q[i], s.kmed, s.idmed) ? 1u : 0u;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
     __shared__ uint32_t ws[kTileThreads / 32];
@@ -874,8 +917,8 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
     if (lv.multi) {
         cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * kHistBins * (size_t)G, st);
         cudaMemsetAsync(s.cand_cnt, 0, sizeof(uint32_t) * G, st);
-        k_hist<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], s.sel,
-                                              s.hist);
+        k_hist<<<G * ((lv.tiles + kHistTiles - 1) / kHistTiles), kTileThreads, 0, st>>>(
+            t, lv, w.x[cur], w.y[cur], w.z[cur], s.sel, s.hist);
         k_find<<<G, kTileThreads, 0, st>>>(s.hist, s.sel);
         k_collect<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], s.sel,
                                                  s.cand_cnt, s.ckey[0], s.cpos[0]);
