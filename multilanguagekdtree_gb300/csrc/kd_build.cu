@@ -352,7 +352,10 @@ __global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin
 // A block takes kHistTiles consecutive tiles of one segment, so that zeroing its
 // kHistBins shared bins and merging them into the segment's histogram is paid once per
 // kHistTiles * kTile bodies.
-constexpr uint32_t kHistTiles = 4;
+#ifndef KD_HIST_TILES
+#define KD_HIST_TILES 8
+#endif
+constexpr uint32_t kHistTiles = KD_HIST_TILES;
 
 __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
                                                        const double *wx, const double *wy,

@@ -36,7 +36,10 @@ constexpr int kSelCap = 2048;       // capacity of the select's shared-memory so
 #define KD_SEL_THREADS 512
 #endif
 constexpr int kSelThreads = KD_SEL_THREADS;
-constexpr uint32_t kMultiMin = 32768;  // segments above this use multi-block histograms
+#ifndef KD_MULTI_MIN
+#define KD_MULTI_MIN 8192
+#endif
+constexpr uint32_t kMultiMin = KD_MULTI_MIN;  // segments above this use multi-block histograms
 constexpr int kSelMaxIters = 16;    // radix refinement passes before giving up (error)
 constexpr int kWalkWarps = 4;       // warps per walk block
 constexpr int kStackMax = 32;       // traversal stack entries: one per lane of a warp
