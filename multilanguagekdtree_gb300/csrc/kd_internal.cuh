@@ -269,7 +269,10 @@ void launch_walk_fp64(const NodeD *rec, const NodeP *recp, const float4 *thi,
 // per-warp stack entries (a multiple of 32).
 constexpr int kGroupSinks = 64;
 constexpr int kGroupWarps = 4;
-constexpr int kGroupFlush = 128;
+#ifndef KD_GROUP_FLUSH
+#define KD_GROUP_FLUSH 128
+#endif
+constexpr int kGroupFlush = KD_GROUP_FLUSH;  // list entries that trigger a sum
 constexpr int kGroupListCap = kGroupFlush + 32 * 8;
 // shared memory of one warp: interaction list, own-leaf list (two float4 per body: split
 // positions), stack
