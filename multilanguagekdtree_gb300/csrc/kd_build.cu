@@ -15,9 +15,11 @@
 // depends on its random pivots.
 //
 // Structure: levels whose segments exceed kLocalMax bodies run as multi-block passes
-// (bounding box -> split -> radix select -> stable partition into the other ping-pong
-// buffer); below that, one thread block takes a whole segment into shared memory and
-// finishes its subtree there (bitonic sort per sub-segment per level).
+// (bounding box -> split -> exact median select -> stable partition into the other
+// ping-pong buffer, which also reduces the children's bounding boxes); below that, one
+// thread block takes a whole segment into shared memory and finishes its subtree there
+// (one warp per node: radix select on a warp-private histogram, ballot partition; nodes of
+// at most 32 bodies in one warp's registers).
 #include "kd_internal.cuh"
 
 namespace kd {

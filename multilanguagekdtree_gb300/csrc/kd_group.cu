@@ -9,7 +9,7 @@
 // group splits: a run of leaves that crosses a high-level split joins two far-apart corners
 // of the tree, and one box around both would open nearly every node for that group.
 // Accepted nodes and the bodies of reached leaves go to an interaction list in shared
-// memory; whenever the list holds kGroupFlush entries every lane sums it for its own body,
+// memory; whenever the list holds kGroupFlush entries every lane sums it for its two bodies,
 // so the force loop runs without divergence and without per-lane traversal state.  Two
 // sinks per lane halve the traversal per body against 32-body groups, for a group box that
 // accepts somewhat fewer nodes.
@@ -359,7 +359,7 @@ __device__ __forceinline__ void traverse(const NodeF *__restrict__ rec,
     __syncwarp();
 }
 
-// Two list entries (packed source coordinates and masses) on the lane's body (q, packed
+// Two list entries (packed source coordinates and masses) on one sink (q, packed
 // twice): the pair kernel of one entry per half.
 template <bool kPot>
 __device__ __forceinline__ void pair_term2(f2 ex, f2 ey, f2 ez, f2 em, f2 qx, f2 qy, f2 qz,
