@@ -117,7 +117,9 @@ void kd_destroy(kd_ctx *ctx);
 const char *kd_last_error(const kd_ctx *ctx);
 
 /* Copy n bodies host -> device (Vec<Particle> handed to simple_sim/build_tree).  Checks
- * that every p, v, m is finite and m >= 0. */
+ * that every p, v, m is finite and m >= 0.  A page-locked (pinned) 16-byte-aligned array is
+ * read in place by the converting kernel at the host link's rate; any other array is first
+ * copied to a device staging buffer.  Returns after the bodies are on the device. */
 int kd_set_bodies(kd_ctx *ctx, const kd_particle_c *bodies, size_t n);
 /* Generate n bodies on the device, straight into the context (no host arrays): the
  * initial conditions of array_particle.rs without the host-to-device copy.  KD_GEN_RING: body
@@ -130,7 +132,9 @@ int kd_set_bodies(kd_ctx *ctx, const kd_particle_c *bodies, size_t n);
 enum { KD_GEN_RING = 0, KD_GEN_PLUMMER = 1, KD_GEN_CIRCULAR = 2 };
 int kd_generate(kd_ctx *ctx, int32_t kind, uint64_t seed);
 
-/* Copy the bodies device -> host (the &mut Vec<Particle> after simple_sim returns). */
+/* Copy the bodies device -> host (the &mut Vec<Particle> after simple_sim returns); a
+ * page-locked 16-byte-aligned array is written in place, any other through a staging
+ * buffer.  Returns after the copy is complete. */
 int kd_get_bodies(kd_ctx *ctx, kd_particle_c *bodies, size_t n);
 
 /* build_tree (array_kd_tree.rs:63-130) / build_tree_par4 (:515-583) over the current
