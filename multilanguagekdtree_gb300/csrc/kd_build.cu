@@ -711,7 +711,7 @@ __global__ __launch_bounds__(kTileThreads) void k_part_count(Topology t, LevelAr
 
 // Exclusive scan of the left counts over the tiles of each segment; checks that exactly
 // len/2 bodies go left.
-__global__ __launch_bounds__(256) void k_tile_scan(Topology t, LevelArgs lv,
+__global__ __launch_bounds__(1024) void k_tile_scan(Topology t, LevelArgs lv,
                                                    const uint32_t *tile_cnt, uint32_t *tile_off,
                                                    uint32_t *err) {
     const uint32_t seg = blockIdx.x;
@@ -719,7 +719,7 @@ __global__ __launch_bounds__(256) void k_tile_scan(Topology t, LevelArgs lv,
     const uint32_t ntiles = (cnt + kTile - 1) / kTile;
     const uint32_t *tc = tile_cnt + (size_t)seg * lv.tiles;
     uint32_t *to = tile_off + (size_t)seg * lv.tiles;
-    __shared__ uint32_t wsum[8];
+    __shared__ uint32_t wsum[32];
     __shared__ uint32_t carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -934,7 +934,9 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
                                             s.sel, s, no);
     k_part_count<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
                                                 s.sel, s.tile_cnt);
-    k_tile_scan<<<G, 256, 0, st>>>(t, lv, s.tile_cnt, s.tile_off, s.err);
+    // one block per segment, a thread per tile up to 1024
+    const uint32_t scan_threads = min(1024u, max(32u, (lv.tiles + 31u) & ~31u));
+    k_tile_scan<<<G, scan_threads, 0, st>>>(t, lv, s.tile_cnt, s.tile_off, s.err);
     k_part_scatter<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur],
                                                   w.id[cur], w.x[nxt], w.y[nxt], w.z[nxt],
                                                   w.id[nxt], s.sel, s.tile_off, nbmin, nbmax);

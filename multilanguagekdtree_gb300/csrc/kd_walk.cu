@@ -225,15 +225,20 @@ void launch_energy_partial(const Bodies &b, const double *phi, uint32_t n, doubl
 __global__ void k_kick_drift(Bodies b, const double *__restrict__ acc, uint32_t n, double dt) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += gridDim.x * blockDim.x) {
-        const double vx = __dadd_rn(b.vx[i], __dmul_rn(dt, acc[3 * (size_t)i]));
-        const double vy = __dadd_rn(b.vy[i], __dmul_rn(dt, acc[3 * (size_t)i + 1]));
-        const double vz = __dadd_rn(b.vz[i], __dmul_rn(dt, acc[3 * (size_t)i + 2]));
+        // every load first: the state arrays may alias as far as the compiler knows
+        const double ax = acc[3 * (size_t)i], ay = acc[3 * (size_t)i + 1],
+                     az = acc[3 * (size_t)i + 2];
+        const double vx0 = b.vx[i], vy0 = b.vy[i], vz0 = b.vz[i];
+        const double x0 = b.x[i], y0 = b.y[i], z0 = b.z[i];
+        const double vx = __dadd_rn(vx0, __dmul_rn(dt, ax));
+        const double vy = __dadd_rn(vy0, __dmul_rn(dt, ay));
+        const double vz = __dadd_rn(vz0, __dmul_rn(dt, az));
         b.vx[i] = vx;
         b.vy[i] = vy;
         b.vz[i] = vz;
-        b.x[i] = __dadd_rn(b.x[i], __dmul_rn(dt, vx));
-        b.y[i] = __dadd_rn(b.y[i], __dmul_rn(dt, vy));
-        b.z[i] = __dadd_rn(b.z[i], __dmul_rn(dt, vz));
+        b.x[i] = __dadd_rn(x0, __dmul_rn(dt, vx));
+        b.y[i] = __dadd_rn(y0, __dmul_rn(dt, vy));
+        b.z[i] = __dadd_rn(z0, __dmul_rn(dt, vz));
     }
 }
 
