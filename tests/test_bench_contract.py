@@ -48,3 +48,12 @@ def test_tree_levels(n, leaf, expect):
     sys.path.insert(0, str(ROOT))
     import bench
     assert bench.tree_levels(n, leaf) == expect
+
+
+@pytest.mark.parametrize("n,exceeds", [(10_000_000, True), (4_000_000, True), (20_000, False)])
+def test_l2_note_states_how_the_inputs_stand_against_the_l2(n, exceeds):
+    sys.path.insert(0, str(ROOT))
+    import bench
+    note = bench.l2_note(n)
+    assert ("exceed the 129 MB L2" in note) == exceeds
+    assert f"{64.0 * n / 1e6:.0f}" in note or f"{64.0 * n / 1e6:.1f}" in note
