@@ -1657,12 +1657,10 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
                   const NodeOut &no, const Work &w, int cur, const LocalOut &out, uint32_t *err,
                   cudaStream_t st) {
-    static bool attr_set = false;
+    // set on every launch: the attribute belongs to the current device's context, and a
+    // process may hold contexts on several devices
     const size_t smem = sizeof(LocalSmem);
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr_set = true;
-    }
+    cudaFuncSetAttribute(k_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_local<<<n_roots, kLocalThreads, smem, st>>>(t, roots, no, w.x[cur], w.y[cur], w.z[cur],
                                                   w.id[cur], out, err);
 }
