@@ -751,7 +751,8 @@ __global__ __launch_bounds__(1024) void k_tile_scan(Topology t, LevelArgs lv,
 __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
     Topology t, LevelArgs lv, const double *sx, const double *sy, const double *sz,
     const uint32_t *sid, double *dx, double *dy, double *dz, uint32_t *did, const SegSel *sel,
-    const uint32_t *tile_off, unsigned long long *nbmin, unsigned long long *nbmax) {
+    const uint32_t *tile_off, unsigned long long *nbmin, unsigned long long *nbmax,
+    uint32_t *err) {
     TileRef r;
     if (!tile_of(t, lv, r)) return;
     // [child][dim] running bounds of this thread, as ordered keys
@@ -759,7 +760,8 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
     unsigned long long cmx[2][3] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
     const SegSel s = sel[r.seg];
     const uint32_t mid = split_rank(lv, r.cnt);
-    const uint32_t lbase = tile_off[(size_t)r.seg * lv.tiles + r.tile];
+    // without tile offsets every segment is one tile: nothing goes left before it
+    const uint32_t lbase = tile_off ? tile_off[(size_t)r.seg * lv.tiles + r.tile] : 0u;
     const uint32_t rbase = r.lo - lbase;
     // The tile as kRows rows of one element per thread: all loads first, then one ballot
     // per row, one table of per-(row, warp) counts and its row-major exclusive scan, so the
@@ -827,6 +829,9 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
             if (lane >= o) { sa += ua; sb += ub; }
         }
         const uint32_t ea = sa - a0 - a1, eb = sb - b0 - b1;
+        // a one-tile segment checks here what k_tile_scan checks otherwise: exactly the
+        // wanted rank went left
+        if (!tile_off && lane == 31 && sa != mid) atomicOr(err, kErrSelect);
         __syncwarp();
         if (c0 < kCells) { cntL[c0 / kWarps][c0 % kWarps] = ea; cntR[c0 / kWarps][c0 % kWarps] = eb; }
         if (c1 < kCells) { cntL[c1 / kWarps][c1 % kWarps] = ea + a0; cntR[c1 / kWarps][c1 % kWarps] = eb + b0; }
@@ -932,14 +937,20 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
     if (lv.multi || seg_max > kWarpSelMax)
         k_select<<<G, kSelThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
                                             s.sel, s, no);
-    k_part_count<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
-                                                s.sel, s.tile_cnt);
-    // one block per segment, a thread per tile up to 1024
-    const uint32_t scan_threads = min(1024u, max(32u, (lv.tiles + 31u) & ~31u));
-    k_tile_scan<<<G, scan_threads, 0, st>>>(t, lv, s.tile_cnt, s.tile_off, s.err);
+    if (lv.tiles > 1) {
+        k_part_count<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur],
+                                                    w.id[cur], s.sel, s.tile_cnt);
+        // one block per segment, a thread per tile up to 1024
+        const uint32_t scan_threads = min(1024u, max(32u, (lv.tiles + 31u) & ~31u));
+        k_tile_scan<<<G, scan_threads, 0, st>>>(t, lv, s.tile_cnt, s.tile_off, s.err);
+    } else {
+        launched -= 2;  // one tile per segment: the scatter counts and checks by itself
+    }
     k_part_scatter<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur],
                                                   w.id[cur], w.x[nxt], w.y[nxt], w.z[nxt],
-                                                  w.id[nxt], s.sel, s.tile_off, nbmin, nbmax);
+                                                  w.id[nxt], s.sel,
+                                                  lv.tiles > 1 ? s.tile_off : nullptr, nbmin,
+                                                  nbmax, s.err);
     return launched;
 }
 
