@@ -35,7 +35,8 @@ def gpu_grad(kd, bodies, dt, steps, target, theta=0.3, ckpt=32):
             gx, gv = tape.backward(dLdx)
             gx2, gv2 = tape.backward(dLdx)
             after = s.get_bodies()["p"].copy()
-    # the source-side sums are FP32 atomics: repeated sweeps agree to their rounding
+    # the source-side sums are FP64 atomics in no fixed order: repeated sweeps agree to their
+    # rounding, not bit for bit
     assert np.allclose(gv, gv2, rtol=1e-6, atol=1e-6 * np.abs(gv).max())
     assert np.allclose(gx, gx2, rtol=1e-6, atol=1e-6 * np.abs(gx).max())
     assert np.array_equal(after, xT), "backward must leave the final state in place"
