@@ -106,6 +106,14 @@ void kd_default_params(kd_params *params);
  * kd_build_tree reports the nodes actually used). */
 size_t kd_nodes_needed(size_t n, int32_t leaf_size, int32_t layout);
 
+/* The sink groups of the mixed (grouped) walk for n bodies (host computation, no device):
+ * whole leaves in tree order packed greedily up to 64 bodies; gstart[0..g] = first tree
+ * position of each group and n at the end, gsplit[0..g-1] = the split position of the
+ * deepest node holding each group (its end for a one-leaf group).  *n_groups = g is set
+ * even when cap < g + 1 (then KD_EINVAL and nothing is written). */
+int kd_group_plan(size_t n, int32_t leaf_size, uint32_t *gstart, uint32_t *gsplit, size_t cap,
+                  size_t *n_groups);
+
 /* Create a context for n bodies (1 <= n < 2^31).  Replaces the set-up half of
  * simple_sim (array_kd_tree.rs:624-630): node storage, index vector, accelerations.
  * Returns NULL on failure; kd_last_error(NULL) then says why. */

@@ -72,6 +72,8 @@ class KDError(RuntimeError):
 SIGNATURES = {
     "kd_default_params": (None, [C.POINTER(KdParams)]),
     "kd_nodes_needed": (C.c_size_t, [C.c_size_t, C.c_int32, C.c_int32]),
+    "kd_group_plan": (C.c_int, [C.c_size_t, C.c_int32, C.POINTER(C.c_uint32),
+                                C.POINTER(C.c_uint32), C.c_size_t, C.POINTER(C.c_size_t)]),
     "kd_create": (C.c_void_p, [C.c_size_t, C.POINTER(KdParams)]),
     "kd_destroy": (None, [C.c_void_p]),
     "kd_last_error": (C.c_char_p, [C.c_void_p]),

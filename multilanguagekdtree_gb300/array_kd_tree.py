@@ -41,6 +41,24 @@ def _precision(v) -> int:
     return PRECISIONS[v] if isinstance(v, str) else int(v)
 
 
+def group_plan(n: int, leaf_size: int = 7):
+    """Sink groups of the mixed walk for n bodies (host computation): (gstart, gsplit) in tree
+    positions, see kd_group_plan."""
+    lib = _lib.load()
+    ng = C.c_size_t(0)
+    lib.kd_group_plan(n, leaf_size, None, None, 0, C.byref(ng))
+    if ng.value == 0:
+        raise ValueError("n must be >= 1 and leaf_size in [2, 8]")
+    gstart = np.zeros(ng.value + 1, dtype=np.uint32)
+    gsplit = np.zeros(ng.value, dtype=np.uint32)
+    rc = lib.kd_group_plan(n, leaf_size, gstart.ctypes.data_as(C.POINTER(C.c_uint32)),
+                           gsplit.ctypes.data_as(C.POINTER(C.c_uint32)), ng.value + 1,
+                           C.byref(ng))
+    if rc != 0:
+        raise ValueError(f"kd_group_plan failed ({rc})")
+    return gstart, gsplit
+
+
 def nodes_needed(n: int, leaf_size: int = 8, layout="par4") -> int:
     """nodes_needed_for_particles: PAR4 array_kd_tree.rs:45-53 (Parallel), DFS
     Sequential/RustVersion/src/array_kd_tree.rs:37-39."""

@@ -725,6 +725,21 @@ size_t kd_nodes_needed(size_t n, int32_t leaf_size, int32_t layout) {
                                     : (size_t)needed_seq(n, (uint32_t)leaf_size);
 }
 
+int kd_group_plan(size_t n, int32_t leaf_size, uint32_t *gstart, uint32_t *gsplit, size_t cap,
+                  size_t *n_groups) {
+    if (n < 1 || n >= (size_t)1 << 31 || leaf_size < 2 || leaf_size > KD_MAX_LEAF || !n_groups)
+        return KD_EINVAL;
+    Plan p;
+    std::string err;
+    if (!make_plan((uint32_t)n, (uint32_t)leaf_size, p, err)) return KD_EINVAL;
+    const size_t ng = p.gstart.size() - 1;
+    *n_groups = ng;
+    if (!gstart || !gsplit || cap < ng + 1) return KD_EINVAL;
+    std::copy(p.gstart.begin(), p.gstart.end(), gstart);
+    std::copy(p.gsplit.begin(), p.gsplit.end(), gsplit);
+    return KD_OK;
+}
+
 const char *kd_last_error(const kd_ctx *ctx) {
     return ctx ? ctx->err.c_str() : g_create_error.c_str();
 }

@@ -69,6 +69,7 @@ class Oracle:
                                             _vp]),
             "orc_calc_accel_group": (C.c_int, [_vp, C.c_size_t, _vp, C.c_size_t, C.c_double, _vp,
                                                _vp]),
+            "orc_groups": (C.c_size_t, [_vp, C.c_size_t, C.c_size_t, _vp, _vp, C.c_size_t]),
             "orc_omp_threads": (C.c_int, []),
             "orc_set_threads": (None, [C.c_int]),
         }
@@ -148,6 +149,17 @@ class Oracle:
         self.lib.orc_walk_counts(_p(b), _p(nodes), theta, _p(s), len(s), _p(out))
         return {"p2p": int(out[0]), "opened": int(out[1]), "m2p": int(out[2]),
                 "visits": int(out[3])}
+
+    def groups(self, nodes, n: int):
+        """The grouped walk's sink groups over a DFS tree of n bodies: (gstart, gsplit),
+        depth-first body positions (make_groups / group_split of kdoracle.c)."""
+        nodes = np.ascontiguousarray(nodes, dtype=NODE)
+        gstart = np.zeros(n + 1, dtype=np.uint64)
+        gsplit = np.zeros(n + 1, dtype=np.uint64)
+        ng = self.lib.orc_groups(_p(nodes), len(nodes), n, _p(gstart), _p(gsplit), n + 1)
+        if ng == 2 ** 64 - 1:
+            raise RuntimeError("orc_groups failed")
+        return gstart[: ng + 1], gsplit[:ng]
 
     def calc_accel_group(self, bodies, nodes, theta: float = 0.3):
         """FP64 restatement of the grouped walk of the mixed path: sinks in groups of whole

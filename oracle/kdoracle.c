@@ -487,6 +487,31 @@ static size_t make_groups(const orc_node *nodes, size_t n_nodes, uint64_t *order
     return ng;
 }
 
+/* The groups of make_groups and their split positions, for the tests: gstart (ng + 1
+ * entries, depth-first body positions) and gsplit (ng entries, group_split).  Returns ng,
+ * or (size_t)-1 when cap < ng + 1 or on allocation failure. */
+size_t orc_groups(const orc_node *nodes, size_t n_nodes, size_t n, size_t *gstart_out,
+                  size_t *gsplit_out, size_t cap) {
+    uint64_t *order = (uint64_t *)malloc(sizeof(uint64_t) * (n ? n : 1));
+    size_t *gs = (size_t *)malloc(sizeof(size_t) * (n + 1));
+    size_t ng = (size_t)-1;
+    if (order && gs) {
+        ng = make_groups(nodes, n_nodes, order, gs);
+        if (ng + 1 > cap) {
+            ng = (size_t)-1;
+        } else {
+            for (size_t g = 0; g < ng; ++g) {
+                gstart_out[g] = gs[g];
+                gsplit_out[g] = group_split(nodes, n, gs[g], gs[g + 1]);
+            }
+            gstart_out[ng] = gs[ng];
+        }
+    }
+    free(order);
+    free(gs);
+    return ng;
+}
+
 /* acc (n*3, original body order); counts: p2p and m2p per sink, node tests per group,
  * internal nodes opened per group. */
 int orc_calc_accel_group(const orc_particle *P, size_t n, const orc_node *nodes, size_t n_nodes,
