@@ -28,3 +28,19 @@ def test_groups_are_whole_leaves_of_at_most_64_bodies(n):
     assert np.all(sp >= gs[:-1]) and np.all(sp <= gs[1:])
     # greedy packing: a group and its successor together exceed 64 bodies
     assert np.all(sizes[:-1] + sizes[1:] > 64)
+
+
+@pytest.mark.parametrize("n,leaf", [(0, 7), (100, 1), (100, 9)])
+def test_group_plan_rejects_bad_arguments(n, leaf):
+    with pytest.raises(ValueError):
+        group_plan(n, leaf)
+
+
+def test_group_plan_reports_the_count_when_the_buffer_is_short():
+    import ctypes as C
+
+    from multilanguagekdtree_gb300 import _lib
+    lib = _lib.load()
+    ng = C.c_size_t(0)
+    rc = lib.kd_group_plan(1000, 7, None, None, 0, C.byref(ng))
+    assert rc != 0 and ng.value == len(group_plan(1000, 7)[1])
