@@ -14,15 +14,23 @@ simulation step: tree build, centre-of-mass pass, force walk, kick-drift.
 * ``fp64``: the plain FP64 path on the same bodies (the reference's arithmetic), and the
   mixed/FP64 speed ratio.
 * ``accuracy``: max / RMS relative acceleration error of the mixed walk against an FP64
-  direct sum on 4,096 seeded bodies (body 0, whose acceleration is a near-cancelling
-  residual, is reported separately).
-* ``roofline``: the force walk (the dominant kernel) against the FP32 rate of the GPU;
+  direct sum on 4,096 seeded bodies, body 0 (the central mass) among them.
+* ``roofline``: the force walk (the dominant kernel) on the algorithmic flops of the
+  reference walk (18 per pair, 10 per opening test, 9 per accepted node, counted by the
+  oracle's instrumented walk on 20,000 seeded sinks) against the measured FP32 rate;
   ``roofline_build``: the build against measured HBM bandwidth.
-* ``cpu_baseline``: the CPU oracle's step loop (the reference's algorithm, OpenMP,
-  fork-join build) on one step of the same workload.
+* ``adjoint``: forward and reverse sweep over two checkpoint segments (recompute included).
+* ``plummer``: the 20,000,000-body Plummer stress case (theta 0.5, dt 1e-4, 20 steps, mixed
+  forward + adjoint, rooflines, error on 4,096 samples).
+* ``adjoint_check``: the 100,000-body ring gradient check (1,000 steps, checkpoints every 32,
+  central differences on 64 coordinates, and the 2,000-body FP64 direct-sum CPU adjoint).
+* ``cpu_baseline``: the CPU oracle's step (the reference's algorithm: fork-join PAR4 build,
+  parallel walk, all host threads) on sampled steps of the same workload.
 
 ``--impl reference`` times the reference's CPU algorithm (the oracle port, all host
-threads) on the same workload and prints the same line with ``"impl": "reference"``.
+threads) on the same workload -- each step the whole build and kick-drift, the walk on a
+seeded sample of sinks scaled to all bodies -- and prints the same line with
+``"impl": "reference"``.
 """
 from __future__ import annotations
 
@@ -58,8 +66,19 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--err-samples", type=int, default=4096)
-    ap.add_argument("--cpu-steps", type=int, default=1)
-    ap.add_argument("--adjoint-steps", type=int, default=4)
+    ap.add_argument("--cpu-steps", type=int, default=3,
+                    help="sampled steps of the cpu_baseline leg")
+    ap.add_argument("--ref-sample", type=float, default=0.02,
+                    help="fraction of the sinks the CPU walks in each sampled step")
+    ap.add_argument("--adjoint-steps", type=int, default=16)
+    ap.add_argument("--adjoint-ckpt", type=int, default=8,
+                    help="checkpoint interval of the headline adjoint (two segments)")
+    ap.add_argument("--flop-sinks", type=int, default=20_000,
+                    help="sinks of the oracle walk that counts the algorithmic flops")
+    ap.add_argument("--fd-threads", type=int, default=8,
+                    help="contexts stepping the finite-difference runs concurrently")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the Plummer and gradient-check blocks of the default line")
     ap.add_argument("--build-n", type=int, default=10_000_000,
                     help="bodies of the build-only measurement (circular_orbits, leaf 8, PAR4)")
     ap.add_argument("--select-n", type=int, default=100_000_000,
@@ -177,17 +196,29 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ CPU reference arm
 
-def cpu_step_rate(bodies, steps: int, leaf: int, theta: float, dt: float):
-    """The oracle's step loop (reference algorithm: fork-join PAR4 build, parallel walk)
-    on all host threads.  Returns (body-steps/s, threads, seconds)."""
+def sampled_cpu_rate(bodies, steps: int, warmup: int, leaf: int, theta: float, dt: float,
+                     frac: float, seed: int):
+    """The oracle's step (reference algorithm: fork-join PAR4 build, parallel walk, parallel
+    kick-drift) on all host threads, `warmup` untimed and `steps` timed sampled steps.  Each
+    sampled step builds the whole tree and kick-drifts every body, but walks only a seeded
+    `frac` of the sinks; its walk time is scaled by n / sinks.  Returns (body-steps/s,
+    threads, timed CPU seconds, per-part seconds of one full step)."""
     from oracle import Oracle
     orc = Oracle()
-    threads = orc.threads()
     b = bodies.copy()
-    t0 = time.perf_counter()
-    orc.simple_sim(b, dt, steps, leaf=leaf, layout="par4", theta=theta)
-    t = time.perf_counter() - t0
-    return len(b) * steps / t, threads, t
+    n = len(b)
+    ns = max(1, min(n, int(round(frac * n))))
+    rng = np.random.default_rng(seed)
+    total, cpu_s, parts = 0.0, 0.0, np.zeros(3)
+    for k in range(warmup + steps):
+        sinks = np.sort(rng.choice(n, ns, replace=False))
+        tb, tw, tk = orc.sampled_step(b, dt, sinks, leaf=leaf, theta=theta, seed=k + 1)
+        if k >= warmup:
+            full = np.array([tb, tw * n / ns, tk])
+            parts += full
+            total += full.sum()
+            cpu_s += tb + tw + tk
+    return n * steps / total, orc.threads(), cpu_s, parts / steps, ns
 
 
 def run_reference(a, ws, rank):
@@ -195,20 +226,22 @@ def run_reference(a, ws, rank):
         return
     import multilanguagekdtree_gb300.array_particle as ap
     bodies = ap.ring(a.n, seed=a.seed)
-    # one untimed step warms caches and page tables; each timed step is one full step of
-    # the same 10M-body workload, capped so the run stays within a few minutes
-    rate_w, threads, tw = cpu_step_rate(bodies, 1, a.leaf, a.theta, a.dt)
-    steps = max(1, min(a.steps, int(150.0 / max(tw, 1e-3))))
-    rate, threads, t = cpu_step_rate(bodies, steps, a.leaf, a.theta, a.dt)
+    rate, threads, cpu_s, parts, ns = sampled_cpu_rate(bodies, a.steps, a.warmup, a.leaf,
+                                                       a.theta, a.dt, a.ref_sample, a.seed)
+    sample = (f"{a.steps} sampled steps of the {a.n}-body ring ({cpu_s:.1f} s of CPU time): "
+              f"whole PAR4 build and kick-drift, walk of {ns} seeded sinks scaled by "
+              f"{a.n / ns:.0f}")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": a.gpus,
-        "steps": steps, "warmup": 1, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * a.n / rate,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
         "config": {"workload": f"ring N={a.n} theta={a.theta} leaf={a.leaf} dt={a.dt} "
                                "(reference algorithm: FP64, fork-join median build, "
                                "recursive walk)", "n_bodies": a.n},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{steps} full step(s) of the {a.n}-body ring"},
+                         "sample": sample},
+        "step_parts_s": {"build": parts[0], "walk": parts[1], "kick_drift": parts[2]},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -216,27 +249,38 @@ def run_reference(a, ws, rank):
 
 # ------------------------------------------------------------------ GPU arm
 
-def adjoint_timing(kd, bodies, a, dev):
-    """Forward sweep with checkpoints (every 32 steps) and the reverse sweep of the loss
-    mean |x_T - R_z(1 rad) x_0|^2, timed by the library's events."""
+ROT_Z1 = np.array([[np.cos(1.0), -np.sin(1.0), 0.0], [np.sin(1.0), np.cos(1.0), 0.0],
+                   [0.0, 0.0, 1.0]])
+
+
+def read_peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def adjoint_timing(kd, bodies, dt, theta, leaf, steps, every, dev):
+    """Forward sweep with checkpoints every `every` steps and the reverse sweep of the loss
+    mean |x_T - R_z(1 rad) x_0|^2, timed by the library's events.  With steps > every the
+    reverse sweep recomputes every segment but the last."""
     n = len(bodies)
-    adj = kd.KDTreeSim(n, leaf_size=a.leaf, layout="dfs", precision="mixed", theta=a.theta,
-                       dt=a.dt, device=dev)
+    adj = kd.KDTreeSim(n, leaf_size=leaf, layout="dfs", precision="mixed", theta=theta,
+                       dt=dt, device=dev)
     adj.set_bodies(bodies)
-    adj.simple_sim(a.dt, 1)
+    adj.simple_sim(dt, 1)
     adj.set_bodies(bodies)
-    with adj.forward(a.dt, a.adjoint_steps, 32) as tape:
+    with adj.forward(dt, steps, every) as tape:
         fwd_ms = adj.stats()["total_ms"]
         xT = adj.get_bodies()["p"]
-        tgt = bodies["p"] @ np.array([[np.cos(1.0), -np.sin(1.0), 0.0],
-                                      [np.sin(1.0), np.cos(1.0), 0.0], [0.0, 0.0, 1.0]]).T
+        tgt = bodies["p"] @ ROT_Z1.T
         tape.backward(2.0 * (xT - tgt) / n)
         bwd_ms = adj.stats()["total_ms"]
     adj.close()
-    return {"steps": a.adjoint_steps, "forward_ms_per_step": fwd_ms / a.adjoint_steps,
-            "backward_ms_per_step": bwd_ms / a.adjoint_steps,
+    return {"steps": steps, "ckpt_every": every, "segments": -(-steps // every),
+            "forward_ms_per_step": fwd_ms / steps, "backward_ms_per_step": bwd_ms / steps,
             "adjoint_over_forward": bwd_ms / fwd_ms,
-            "note": "backward = recompute of each checkpoint segment but the last (whose "
+            "note": "backward = recompute of every checkpoint segment but the last (whose "
                     "positions the forward keeps) + rebuild + transpose-Jacobian walk per "
                     "step; loss = mean |x_T - R_z(1) x_0|^2"}
 
@@ -246,6 +290,62 @@ def pinned_bodies(n):
     from multilanguagekdtree_gb300 import PARTICLE_DTYPE
     t = torch.empty(n * 64, dtype=torch.uint8, pin_memory=True)
     return t, t.numpy().view(PARTICLE_DTYPE)
+
+
+def reference_walk_flops(state, leaf, theta, sinks):
+    """Algorithmic flops per body-step of the reference walk (18 per pair, 10 per opening
+    test at an internal node, 9 per accepted node), from the oracle's instrumented walk
+    (array_kd_tree.rs:585-617) over a PAR4 tree of the same bodies on seeded sinks."""
+    from oracle import Oracle
+    orc = Oracle()
+    nodes = orc.build_tree_par4(state, leaf=leaf)
+    c = orc.walk_counts(state, nodes, sinks, theta)
+    k = len(sinks)
+    per = {key: c[key] / k for key in ("p2p", "opened", "m2p", "visits")}
+    return 18 * per["p2p"] + 10 * per["opened"] + 9 * per["m2p"], per
+
+
+def grouped_walk_flops(cnt):
+    """FP32 work the grouped walk itself does, from its device counts: 18 per interaction
+    (pair or accepted node) + 20 per group node test."""
+    return 18 * (cnt["p2p"] + cnt["m2p"]) + 20 * cnt["opened"]
+
+
+def walk_roofline(n, walk_s, alg_per_body, grouped_total, peak, peak_note):
+    achieved = alg_per_body * n / walk_s / 1e12
+    return {
+        "kernel": "k_walk_group", "bound": "fp32", "achieved": achieved, "peak": peak,
+        "unit": "TFLOP/s", "frac": achieved / peak,
+        "flops_per_body": alg_per_body, "launch_s": walk_s,
+        "grouped_set": {"achieved": grouped_total / walk_s / 1e12,
+                        "frac": grouped_total / walk_s / 1e12 / peak,
+                        "flops_per_body": grouped_total / n},
+        "note": "achieved = algorithmic flops of the reference walk (18 per pair, 10 per "
+                "opening test, 9 per accepted node; counts from the oracle's instrumented "
+                "walk on seeded sinks) x N / device time of the walk phase (CUDA events); "
+                "grouped_set = the flops of the grouped walk's own (larger) interaction set; "
+                + peak_note}
+
+
+def build_roofline(n, leaf, build_s, hbm, hbm_src):
+    levels = tree_levels(n, leaf)
+    build_bytes = n * (40 * levels + 32)
+    achieved = build_bytes / build_s / 1e9
+    traffic = BUILD_TRAFFIC_PER_BODY * n if BUILD_TRAFFIC_PER_BODY else None
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": traffic, "launch_s": build_s,
+            "note": f"algorithmic bytes N*(40 L + 32), L = {levels} internal levels; traffic "
+                    f"= {BUILD_TRAFFIC_NOTE}", "peak_source": hbm_src}
+
+
+def fp32_peak_tflops(kd, dev):
+    try:
+        r = kd.fp32_peak(dev)
+        return max(r["scalar"], r["packed"]), r
+    except Exception as e:  # measured figure unavailable: nominal rate instead, said so
+        import torch
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        return sms * 128 * 2 * 2070e6 / 1e12, {"error": str(e), "nominal_sms": sms}
 
 
 def run_ours(a, ws, rank, local):
@@ -259,7 +359,8 @@ def run_ours(a, ws, rank, local):
 
     if a.adjoint_only:
         line = {"metric": METRIC, "config": {"workload": f"adjoint ring N={n}"},
-                "adjoint": adjoint_timing(kd, bodies, a, dev)}
+                "adjoint": adjoint_timing(kd, bodies, a.dt, a.theta, a.leaf, a.adjoint_steps,
+                                          a.adjoint_ckpt, dev)}
         print(json.dumps(line))
         return
 
@@ -300,6 +401,13 @@ def run_ours(a, ws, rank, local):
             print(json.dumps(line))
         return
 
+    peaks = read_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    hbm_src = "MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6800 GB/s"
+    fp32, fp32_detail = fp32_peak_tflops(kd, dev)
+    peak_note = ("peak = the larger of the measured scalar and packed (f32x2) FP32 "
+                 "multiply-add rates (kd_fp32_peak: every SM, a few ms)")
+
     # ---- per-phase device times (events around every phase) and interaction counts
     sim.set_bodies(bodies)
     sim.set_timing(True)
@@ -311,41 +419,27 @@ def run_ours(a, ws, rank, local):
     sim.set_counting(True)
     sim.calc_accel()
     cnt = sim.counts()
+    sim.set_precision("fp64")  # the reference walk itself, every body, counted on the device
+    sim.calc_accel()
+    cnt64 = sim.counts()
+    sim.set_precision("mixed")
     sim.set_counting(False)
-    flops = walk_flops(cnt)
+    rng = np.random.default_rng(a.seed + 101)
+    flop_sinks = np.sort(rng.choice(n, min(n, a.flop_sinks), replace=False))
+    alg, per = reference_walk_flops(bodies, a.leaf, a.theta, flop_sinks)
     walk_s = ph["walk_ms"] / 2 / 1e3
-    sm_mhz = clk.get("sm_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s at the sampled clock
-    achieved = flops / walk_s / 1e12
     line["phases_ms_per_step"] = {k: ph[k] / 2 for k in ("build_ms", "moments_ms", "walk_ms",
                                                          "kick_ms")}
-    line["interactions_per_body"] = {k: v / n for k, v in cnt.items()}
-    # DRAM bytes per launch: one-pass ncu capture of the 10M-body walk (4.31 GB read +
-    # 0.475 GB written, 479 B per body), scaled by the number of bodies
-    walk_traffic = 479.0 * n
-    line["roofline"] = {
-        "kernel": "k_walk_group", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-        "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": walk_traffic,
-        "traffic_unit": "bytes per launch (ncu dram read + write of the 10M ring walk, scaled "
-                        "by N)",
-        "note": WALK_FLOPS_NOTE}
-    # build: algorithmic bytes per build = N*(40 L + 32), L = internal levels of the tree
-    # (each level reads x, y, z for the box, the split key and the index; a final gather of
-    # the leaves)
-    peaks = {}
-    try:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-    except (OSError, ValueError):
-        pass
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    levels = tree_levels(n, a.leaf)
-    build_bytes = n * (40 * levels + 32)
-    build_s = ph["build_ms"] / 2 / 1e3
-    line["roofline_build"] = {
-        "bound": "hbm", "achieved": build_bytes / build_s / 1e9, "peak": hbm, "unit": "GB/s",
-        "frac": build_bytes / build_s / 1e9 / hbm, "traffic": None,
-        "note": f"algorithmic bytes N*(40 L + 32), L = {levels} internal levels",
-        "peak_source": "MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6800 GB/s"}
+    line["interactions_per_body"] = {
+        "grouped_walk": {k: v / n for k, v in cnt.items()},
+        "reference_walk_oracle": dict(per, sinks=len(flop_sinks)),
+        "reference_walk_device_fp64": {k: v / n for k, v in cnt64.items()}}
+    line["roofline"] = walk_roofline(n, walk_s, alg, grouped_walk_flops(cnt), fp32, peak_note)
+    line["roofline"]["traffic"] = WALK_TRAFFIC_PER_BODY * n
+    line["roofline"]["traffic_unit"] = ("bytes per launch (ncu dram read + write of the 10M "
+                                        "ring walk, scaled by N)")
+    line["fp32_peak_tflops"] = fp32_detail
+    line["roofline_build"] = build_roofline(n, a.leaf, ph["build_ms"] / 2 / 1e3, hbm, hbm_src)
 
     # ---- energy drift over the timed run length
     sim.set_bodies(bodies)
@@ -354,33 +448,30 @@ def run_ours(a, ws, rank, local):
     e1 = sim.energy()
     line["energy"] = {"steps": a.steps, "start": e0, "end": e1,
                       "relative_drift": (sum(e1) - sum(e0)) / abs(sum(e0)),
-                      "potential": "mixed tree walk (theta as above), FP64 central-mass term"}
+                      "potential": "mixed tree walk (theta as above), FP64 heavy-body terms"}
 
-    # ---- accuracy of the mixed walk against the FP64 direct sum
+    # ---- accuracy of the mixed walk against the FP64 direct sum, body 0 included
     rng = np.random.default_rng(12345)
-    sinks = np.sort(rng.choice(np.arange(1, n), a.err_samples, replace=False))
+    sinks = np.sort(np.concatenate([[0], rng.choice(np.arange(1, n), a.err_samples - 1,
+                                                    replace=False)]))
     sim.set_bodies(bodies)
     sim.build_tree()
     macc = sim.calc_accel()
-    direct = sim.direct_accel(np.concatenate([[0], sinks]))
+    direct = sim.direct_accel(sinks)
     sim.set_precision("fp64")
     facc = sim.calc_accel()
     sim.set_precision("mixed")
-
-    def rel(x, y):
-        return np.linalg.norm(x - y, axis=1) / np.linalg.norm(y, axis=1)
-
-    e_mixed = rel(macc[sinks], direct[1:])
-    e_fp64 = rel(facc[sinks], direct[1:])
-    e_mix_vs_fp64 = rel(macc[sinks], facc[sinks])
+    e_mixed = rel_rows(macc[sinks], direct)
+    e_fp64 = rel_rows(facc[sinks], direct)
     line["accuracy"] = {
-        "samples": int(a.err_samples), "reference": "FP64 direct sum (GPU kernel, all N)",
-        "mixed_max_rel": float(e_mixed.max()), "mixed_rms_rel": float(np.sqrt(np.mean(e_mixed ** 2))),
-        "fp64_tree_max_rel": float(e_fp64.max()),
-        "mixed_vs_fp64_tree_max_rel": float(e_mix_vs_fp64.max()),
-        "body0_mixed_rel": float(rel(macc[:1], direct[:1])[0]),
-        "body0_fp64_tree_rel": float(rel(facc[:1], direct[:1])[0]),
-    }
+        "samples": int(len(sinks)), "reference": "FP64 direct sum (GPU kernel, all N)",
+        "mixed_max_rel": float(e_mixed.max()),
+        "mixed_rms_rel": float(np.sqrt(np.mean(e_mixed ** 2))),
+        "fp64_tree_max_rel": float(e_fp64[1:].max()),
+        "body0_mixed_rel": float(e_mixed[0]), "body0_fp64_tree_rel": float(e_fp64[0]),
+        "note": "body 0 (the central mass) is among the samples; the mixed path takes its "
+                "acceleration as an FP64 direct sum, the FP64 tree keeps the reference's "
+                "theta truncation of its cancelling sum (excluded from fp64_tree_max_rel)"}
     sim.close()
 
     # ---- FP64 plain path, same bodies
@@ -397,8 +488,9 @@ def run_ours(a, ws, rank, local):
     line["mixed_over_fp64"] = value / ws / fp64_rate
     f64.close()
 
-    # ---- adjoint: forward sweep with checkpoints, then the reverse sweep, same bodies
-    line["adjoint"] = adjoint_timing(kd, bodies, a, dev)
+    # ---- adjoint: two checkpoint segments, so the reverse sweep includes a recompute
+    line["adjoint"] = adjoint_timing(kd, bodies, a.dt, a.theta, a.leaf, a.adjoint_steps,
+                                     a.adjoint_ckpt, dev)
 
     # ---- build only: the reference's bench_build_tree input (circular_orbits, leaf 8, PAR4)
     cb = kd.circular_orbits(a.build_n - 1, seed=a.seed)
@@ -449,6 +541,11 @@ def run_ours(a, ws, rank, local):
                    "call": "kd_set_bodies(pinned host) + kd_simple_sim(1) + kd_get_bodies"}
     del keep
 
+    # ---- the Plummer stress case and the gradient check (the other GPU configurations)
+    if not a.no_configs:
+        line["plummer"] = plummer_block(kd, a, dev, fp32, peak_note, hbm, hbm_src)
+        line["adjoint_check"] = adjoint_check_block(kd, a, dev)
+
     # ---- CPU baseline (oracle port of the reference algorithm)
     if not a.no_cpu_baseline:
         from oracle import Oracle
@@ -461,17 +558,24 @@ def run_ours(a, ws, rank, local):
         orc.quickstat_index(sv, goal)
         line["select_only"]["cpu_ms"] = 1e3 * (time.perf_counter() - t0)
         line["select_only"]["cpu_kind"] = "oracle quickstat_index (sequential, as quickstat.rs)"
-        rate, threads, t = cpu_step_rate(bodies, a.cpu_steps, a.leaf, a.theta, a.dt)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{a.cpu_steps} full FP64 step(s) of the {n}-body "
-                                          f"ring ({t:.1f} s)"}
+        rate, threads, cpu_s, parts, ns = sampled_cpu_rate(bodies, a.cpu_steps, 1, a.leaf,
+                                                           a.theta, a.dt, a.ref_sample,
+                                                           a.seed)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{a.cpu_steps} sampled FP64 steps of the {n}-body ring ({cpu_s:.1f} s "
+                      f"of CPU time): whole PAR4 build and kick-drift, walk of {ns} seeded "
+                      f"sinks scaled by {n / ns:.0f}",
+            "step_parts_s": {"build": parts[0], "walk": parts[1], "kick_drift": parts[2]}}
     print(json.dumps(line))
 
 
-WALK_FLOPS_NOTE = ("walk flops = 18 per body interaction (P2P or accepted node, the "
-                   "reference's pair count) + 20 per group node test, counted on the device; "
-                   "peak = 152 SMs x 128 FP32 lanes x 2 x sampled SM clock (nominal rate; no "
-                   "measured FP32 figure exists)")
+# DRAM bytes per body of one launch, from one-pass ncu captures (see profiles/): the 10M-body
+# grouped walk (4.31 GB read + 0.475 GB written), and the build's kernels at 4M bodies
+# summed over the step's launch list, both scaled by the number of bodies
+WALK_TRAFFIC_PER_BODY = 479.0
+BUILD_TRAFFIC_PER_BODY = None
+BUILD_TRAFFIC_NOTE = "not captured"
 
 
 def tree_levels(n: int, leaf: int) -> int:
@@ -483,24 +587,17 @@ def tree_levels(n: int, leaf: int) -> int:
     return levels
 
 
-def walk_flops(cnt):
-    """Algorithmic FP32 work of one grouped walk from its device counts."""
-    return 18 * (cnt["p2p"] + cnt["m2p"]) + 20 * cnt["opened"]
-
-
 def rel_rows(x, y):
     return np.linalg.norm(x - y, axis=1) / np.linalg.norm(y, axis=1)
 
 
-def run_plummer(a, dev):
+def plummer_block(kd, a, dev, fp32, peak_note, hbm, hbm_src, n=20_000_000):
     """Clustered stress case: Plummer sphere (G = M = a = 1, equal masses, radii <= 20),
     theta 0.5, leaf 7, dt 1e-4, 20 mixed-precision steps, then a reverse sweep over the same
-    20 steps; error of the mixed walk against the FP64 direct sum on 4,096 bodies."""
+    20 steps in checkpoint segments of 8; error of the mixed walk against the FP64 direct sum
+    on 4,096 bodies; walk and build rooflines."""
     import torch
-
-    import multilanguagekdtree_gb300 as kd
-    n = a.n if a.n != 10_000_000 else 20_000_000
-    theta, dt, steps = 0.5, 1e-4, 20
+    theta, dt, steps, every = 0.5, 1e-4, 20, 8
     s = kd.KDTreeSim(n, leaf_size=a.leaf, precision="mixed", theta=theta, dt=dt, device=dev)
     s.generate("plummer", a.seed)
     e0 = s.energy()
@@ -514,106 +611,141 @@ def run_plummer(a, dev):
     clk = clocks.stop()
     fwd = s.stats()
     e1 = s.energy()
-    line = {"workload": f"plummer N={n} theta={theta} leaf={a.leaf} dt={dt} mixed",
-            "steps": steps, "value": n * steps / (fwd["total_ms"] / 1e3), "unit": UNIT,
-            "ms_per_step": fwd["total_ms"] / steps,
-            "energy": {"start": e0, "end": e1,
-                       "relative_drift": (sum(e1) - sum(e0)) / abs(sum(e0))},
-            "gpu_launches": int(fwd["launches"]), "clocks": clk}
+    out = {"workload": f"plummer N={n} theta={theta} leaf={a.leaf} dt={dt} mixed",
+           "steps": steps, "value": n * steps / (fwd["total_ms"] / 1e3), "unit": UNIT,
+           "ms_per_step": fwd["total_ms"] / steps,
+           "energy": {"start": e0, "end": e1,
+                      "relative_drift": (sum(e1) - sum(e0)) / abs(sum(e0))},
+           "gpu_launches": int(fwd["launches"]), "clocks": clk}
+    s.generate("plummer", a.seed)
+    state = s.get_bodies().copy()
     s.set_timing(True)
     s.simple_sim(dt, 2)
     ph = s.stats()
     s.set_timing(False)
-    line["phases_ms_per_step"] = {k: ph[k] / 2 for k in ("build_ms", "walk_ms", "kick_ms")}
+    out["phases_ms_per_step"] = {k: ph[k] / 2 for k in ("build_ms", "walk_ms", "kick_ms")}
+    s.set_bodies(state)
     s.build_tree()
     s.set_counting(True)
-    s.calc_accel()
+    acc = s.calc_accel()
     cnt = s.counts()
     s.set_counting(False)
-    flops = walk_flops(cnt)
-    peak = 152 * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12
-    walk_s = ph["walk_ms"] / 2 / 1e3
-    line["interactions_per_body"] = {k: v / n for k, v in cnt.items()}
-    line["roofline_walk"] = {"bound": "fp32", "achieved": flops / walk_s / 1e12, "peak": peak,
-                             "unit": "TFLOP/s", "frac": flops / walk_s / 1e12 / peak}
-    try:
-        hbm = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", 6800.0)
-    except (OSError, ValueError):
-        hbm = 6800.0
-    levels = tree_levels(n, a.leaf)
-    bb = n * (40 * levels + 32) / (ph["build_ms"] / 2 / 1e3) / 1e9
-    line["roofline_build"] = {"bound": "hbm", "achieved": bb, "peak": hbm, "unit": "GB/s",
-                              "frac": bb / hbm}
+    rng = np.random.default_rng(a.seed + 202)
+    flop_sinks = np.sort(rng.choice(n, a.flop_sinks, replace=False))
+    alg, per = reference_walk_flops(state, a.leaf, theta, flop_sinks)
+    out["interactions_per_body"] = {"grouped_walk": {k: v / n for k, v in cnt.items()},
+                                    "reference_walk_oracle": dict(per, sinks=len(flop_sinks))}
+    out["roofline_walk"] = walk_roofline(n, ph["walk_ms"] / 2 / 1e3, alg,
+                                         grouped_walk_flops(cnt), fp32, peak_note)
+    out["roofline_build"] = build_roofline(n, a.leaf, ph["build_ms"] / 2 / 1e3, hbm, hbm_src)
     rng = np.random.default_rng(12345)
     sinks = np.sort(rng.choice(n, a.err_samples, replace=False))
-    acc = s.calc_accel()
     ref = s.direct_accel(sinks)
     e = rel_rows(acc[sinks], ref)
-    line["accuracy"] = {"samples": int(a.err_samples), "reference": "FP64 direct sum",
-                        "mixed_max_rel": float(e.max()),
-                        "mixed_rms_rel": float(np.sqrt(np.mean(e ** 2))),
-                        "mixed_median_rel": float(np.median(e))}
-    s.generate("plummer", a.seed)
-    with s.forward(dt, steps, 32) as tape:
+    out["accuracy"] = {"samples": int(a.err_samples), "reference": "FP64 direct sum",
+                       "mixed_max_rel": float(e.max()),
+                       "mixed_rms_rel": float(np.sqrt(np.mean(e ** 2))),
+                       "mixed_median_rel": float(np.median(e)),
+                       "note": "theta = 0.5 truncation dominates (the FP64 tree has the same)"}
+    s.set_bodies(state)
+    with s.forward(dt, steps, every) as tape:
         f_ms = s.stats()["total_ms"]
         xT = s.get_bodies()["p"]
         tape.backward(np.zeros_like(xT), np.ones_like(xT) / n)
         b_ms = s.stats()["total_ms"]
-    line["adjoint"] = {"steps": steps, "forward_ms": f_ms, "backward_ms": b_ms,
-                       "adjoint_over_forward": b_ms / f_ms,
-                       "loss": "sum of final velocities / n (dL/dv_T = 1/n)"}
+    out["adjoint"] = {"steps": steps, "ckpt_every": every, "segments": -(-steps // every),
+                      "forward_ms": f_ms, "backward_ms": b_ms, "adjoint_over_forward": b_ms / f_ms,
+                      "loss": "sum of final velocities / n (dL/dv_T = 1/n)"}
     s.close()
-    print(json.dumps(line))
+    return out
 
 
-def run_adjoint_check(a, dev):
+def adjoint_check_block(kd, a, dev, n=100_000):
     """Gradient check: 100,000-body ring, theta 0.3, dt 1e-3, 1,000 steps, checkpoints every
     32 steps, loss = mean |x_T - R_z(1 rad) x_0|^2.  dL/dv0 from the reverse sweep against
-    central differences (h = 1e-6) of the forward on 64 seeded coordinates."""
-    import multilanguagekdtree_gb300 as kd
-    n = a.n if a.n != 10_000_000 else 100_000
-    steps, dt, h = 1000, 1e-3, 1e-6
-    R = np.array([[np.cos(1.0), -np.sin(1.0), 0.0], [np.sin(1.0), np.cos(1.0), 0.0],
-                  [0.0, 0.0, 1.0]])
+    central differences (h = 1e-6) of the forward on 64 seeded coordinates (the forward runs
+    of the differences step concurrently, one context per thread); and the 2,000-body,
+    1,000-step sweep against the oracle's FP64 direct-sum adjoint."""
+    from concurrent.futures import ThreadPoolExecutor
+    steps, dt, h, every = 1000, 1e-3, 1e-6, 32
 
-    def grad(bodies):
+    def sweep(bodies):
         m = len(bodies)
-        tgt = bodies["p"] @ R.T
+        tgt = bodies["p"] @ ROT_Z1.T
         with kd.KDTreeSim(m, leaf_size=a.leaf, precision="mixed", theta=a.theta,
                           device=dev) as s:
             s.set_bodies(bodies)
-            with s.forward(dt, steps, 32) as tape:
+            s.simple_sim(dt, 1)
+            s.set_bodies(bodies)
+            with s.forward(dt, steps, every) as tape:
                 fms = s.stats()["total_ms"]
                 xT = s.get_bodies()["p"]
                 gx, gv = tape.backward(2.0 * (xT - tgt) / m)
                 bms = s.stats()["total_ms"]
         return gx, gv, fms, bms, tgt
 
+    t0 = time.perf_counter()
     b = kd.ring(n, seed=a.seed)
-    gx, gv, fms, bms, tgt = grad(b)
+    gx, gv, fms, bms, tgt = sweep(b)
     rng = np.random.default_rng(77)
     coords = list(zip(rng.choice(np.arange(1, n), 64, replace=False).tolist(),
                       rng.integers(0, 2, 64).tolist()))
-    errs = []
-    with kd.KDTreeSim(n, leaf_size=a.leaf, precision="mixed", theta=a.theta, device=dev) as s:
-        def final(bb):
-            s.set_bodies(bb)
-            s.simple_sim(dt, steps)
-            return s.get_bodies()["p"].copy()
-        for i, d in coords:
-            bp = b.copy(); bp["v"][i, d] += h
-            bm = b.copy(); bm["v"][i, d] -= h
-            lp = np.sum((final(bp) - tgt) ** 2, axis=1)
-            lm = np.sum((final(bm) - tgt) ** 2, axis=1)
-            fd = np.sum(lp - lm) / n / (2 * h)
-            errs.append(abs(fd - gv[i, d]) / abs(gv[i, d]))
-    line = {"workload": f"adjoint-check ring N={n} theta={a.theta} dt={dt} steps={steps} ckpt=32",
+
+    def fd_share(share):
+        import torch
+        torch.cuda.set_device(dev)
+        res = []
+        with kd.KDTreeSim(n, leaf_size=a.leaf, precision="mixed", theta=a.theta,
+                          device=dev) as s:
+            def final(bb):
+                s.set_bodies(bb)
+                s.simple_sim(dt, steps)
+                return s.get_bodies()["p"].copy()
+            for i, d in share:
+                bp = b.copy(); bp["v"][i, d] += h
+                bm = b.copy(); bm["v"][i, d] -= h
+                lp = np.sum((final(bp) - tgt) ** 2, axis=1)
+                lm = np.sum((final(bm) - tgt) ** 2, axis=1)
+                fd = np.sum(lp - lm) / n / (2 * h)
+                res.append(abs(fd - gv[i, d]) / abs(gv[i, d]))
+        return res
+
+    k = max(1, a.fd_threads)
+    with ThreadPoolExecutor(k) as ex:
+        errs = [e for part in ex.map(fd_share, [coords[j::k] for j in range(k)]) for e in part]
+    fd_s = time.perf_counter() - t0
+    # the 2,000-body sweep against the FP64 direct-sum CPU adjoint
+    from oracle import Oracle
+    small = kd.ring(2000, seed=a.seed + 5)
+    sgx, sgv, _, _, stgt = sweep(small)
+    ref = Oracle().adjoint_direct(small, dt, steps, target=stgt)
+    ev = rel_rows(sgv, ref["g_v0"])
+    ex_ = rel_rows(sgx, ref["g_x0"])
+    return {"workload": f"ring N={n} theta={a.theta} dt={dt} steps={steps} ckpt={every}",
             "forward_ms": fms, "backward_ms": bms, "adjoint_over_forward": bms / fms,
             "fd": {"coords": 64, "h": h, "max_rel_err": float(max(errs)),
-                   "median_rel_err": float(np.median(errs))},
-            "cpu_direct_adjoint": "2,000-body, 1,000-step comparison with the FP64 direct-sum "
-                                  "adjoint: tests/test_gpu_adjoint.py"}
+                   "median_rel_err": float(np.median(errs)), "wall_s": fd_s},
+            "cpu_direct_adjoint": {"n": 2000, "steps": steps,
+                                   "dL_dv0_max_rel_err": float(ev.max()),
+                                   "dL_dv0_median_rel_err": float(np.median(ev)),
+                                   "dL_dx0_max_rel_err": float(ex_.max())}}
+
+
+def run_plummer(a, dev):
+    import multilanguagekdtree_gb300 as kd
+    fp32, _ = fp32_peak_tflops(kd, dev)
+    peaks = read_peaks()
+    line = plummer_block(kd, a, dev, fp32, "peak = measured FP32 multiply-add rate",
+                         peaks.get("hbm_gbs", 6800.0),
+                         "MEASURED_PEAKS.json" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+                         n=a.n if a.n != 10_000_000 else 20_000_000)
     print(json.dumps(line))
+
+
+def run_adjoint_check(a, dev):
+    import multilanguagekdtree_gb300 as kd
+    print(json.dumps(adjoint_check_block(kd, a, dev,
+                                         n=a.n if a.n != 10_000_000 else 100_000)))
 
 
 def main():

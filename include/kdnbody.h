@@ -67,7 +67,8 @@ enum { KD_LAYOUT_DFS = 0, KD_LAYOUT_PAR4 = 1 };
 
 /* FP64: the reference's arithmetic, every interaction of every body as the Rust walk makes
  * it.  MIXED: FP32 pairwise and multipole terms on split (hi+lo) coordinates with
- * compensated sums; FP64 for storage, tree splits, kick-drift and the heavy-body term. */
+ * compensated sums; FP64 for storage, tree splits, kick-drift and the heavy bodies (their
+ * pull on every body, and their own accelerations as direct sums over all bodies). */
 enum { KD_PREC_FP64 = 0, KD_PREC_MIXED = 1 };
 
 typedef struct {
@@ -77,8 +78,10 @@ typedef struct {
     int32_t device;     /* CUDA device ordinal */
     double theta;       /* THETA, array_kd_tree.rs:15 (0.3) */
     double dt;          /* time step used by kd_simple_sim when its dt argument is 0 */
-    double heavy_frac;  /* MIXED: bodies with m >= heavy_frac * total mass are summed
-                           directly in FP64 (the central-mass term); <= 0 disables */
+    double heavy_frac;  /* MIXED: bodies with m >= heavy_frac * total mass (at most 8) are
+                           summed directly in FP64 (the central-mass term), and their own
+                           accelerations are FP64 direct sums over all bodies; <= 0
+                           disables */
     uint64_t seed;      /* reserved for generators; the build itself is deterministic */
 } kd_params;
 
@@ -109,8 +112,9 @@ size_t kd_nodes_needed(size_t n, int32_t leaf_size, int32_t layout);
 /* The sink groups of the mixed (grouped) walk for n bodies (host computation, no device):
  * whole leaves in tree order packed greedily up to 64 bodies; gstart[0..g] = first tree
  * position of each group and n at the end, gsplit[0..g-1] = the split position of the
- * deepest node holding each group (its end for a one-leaf group).  *n_groups = g is set
- * even when cap < g + 1 (then KD_EINVAL and nothing is written). */
+ * deepest node holding each group (its end for a one-leaf group).  cap is the capacity of
+ * gstart (g + 1 entries needed; gsplit needs cap - 1).  *n_groups = g is set even when
+ * cap < g + 1 (then KD_EINVAL, nothing is written, and kd_last_error(NULL) says why). */
 int kd_group_plan(size_t n, int32_t leaf_size, uint32_t *gstart, uint32_t *gsplit, size_t cap,
                   size_t *n_groups);
 
@@ -121,7 +125,8 @@ kd_ctx *kd_create(size_t n, const kd_params *params);
 void kd_destroy(kd_ctx *ctx);
 
 /* Last error message of ctx (or of the calling thread's last failed kd_create,
- * kd_quickstat_index or kd_direct_accel_noalloc when ctx is NULL).  Never NULL. */
+ * kd_group_plan, kd_quickstat_index or kd_direct_accel_noalloc when ctx is NULL).  Never
+ * NULL. */
 const char *kd_last_error(const kd_ctx *ctx);
 
 /* Copy n bodies host -> device (Vec<Particle> handed to simple_sim/build_tree).  Checks
@@ -218,7 +223,9 @@ int kd_direct_accel(kd_ctx *ctx, const uint64_t *sinks, size_t ns, double *acc);
  * down to their bodies with weight m_i/M).  Device memory: 48 B per body per checkpoint
  * plus 24 B per body per step of one segment.  The bodies are left at the final state.  A
  * tape may be consumed by
- * several kd_backward calls; kd_tape_free releases it.  No counterpart in the reference
+ * several kd_backward calls; kd_tape_free releases it (before its context is destroyed).  The
+ * checkpoint buffers stay with the context and are reused by later kd_forward calls once
+ * their tape is freed; kd_destroy releases them.  No counterpart in the reference
  * (which has no derivatives); it differentiates simple_sim (array_kd_tree.rs:623-664). */
 int kd_forward(kd_ctx *ctx, double dt, int64_t steps, int64_t ckpt_every, kd_tape **tape);
 int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double *g_x0,
@@ -234,8 +241,11 @@ void kd_tape_free(kd_tape *tape);
  * acc[3k+d] for sinks[k]); an out-of-range sink index yields NaN.  Work is queued on
  * `stream` (a cudaStream_t; NULL = default stream) and not waited for.
  * Limit: ns <= 43690 -- the partial sums live in one 1 MiB __device__ array of the library
- * (131072 doubles, 3 per sink and source chunk; sources are chunked to fit), which every GPU
- * that loads the library holds until exit; larger ns returns KD_EINVAL and
+ * (131072 doubles, 3 per sink and source chunk), which every GPU that loads the library holds
+ * until exit.  The sources are cut into min(ceil(n / 4096), floor(131072 / (3 ns))) chunks,
+ * one grid column each, so a large ns with a large n makes one long launch on a grid of only
+ * ceil(ns / 128) x (1 or 2) blocks: callers sampling accuracy inside a step loop should keep
+ * ns small (a few thousand sinks give 10 or more chunks); larger ns returns KD_EINVAL and
  * kd_last_error(NULL) says why.  The first call on a device looks up that array's address
  * (cudaGetSymbolAddress) with the device current; make that first call before any stream
  * capture.  Every call overwrites all the partials it reads, so no clearing is needed, but
@@ -244,6 +254,24 @@ void kd_tape_free(kd_tape *tape);
 int kd_direct_accel_noalloc(const double *x, const double *y, const double *z,
                             const double *m, size_t n, const uint64_t *sinks, size_t ns,
                             double *acc, void *stream);
+
+/* Device-side guards, lowered for testing the failure path: the traversal stack of both
+ * walks is cut to stack_entries (at most 32 for the FP64 walk, whose stack is one entry per
+ * lane; at most 32 * (tree depth + 2) + 64 for the grouped walk and its adjoint) and the
+ * radix refinement passes of the block median select (segments above 4,096 bodies) to
+ * select_passes (at most 16).  A negative value restores the default.  A walk or select that
+ * runs out stops, sets a device flag, and the call returns KD_EDEVICE ("traversal stack
+ * overflow" / "median select failed to converge"); nothing traps or waits, the step's
+ * kick-drift is skipped (the bodies stay at the start of the failed step), and the context
+ * stays usable.  No counterpart in the reference, whose walk and quickselect panic on a
+ * bad index instead. */
+int kd_set_device_limits(kd_ctx *ctx, int32_t stack_entries, int32_t select_passes);
+
+/* Measured FP32 multiply-add rate of a device, TFLOP/s (2 flops per multiply-add): out[0]
+ * with scalar fma.rn.f32, out[1] with packed fma.rn.f32x2 (the form of the mixed walk's pair
+ * sums); every SM busy for a few milliseconds.  A measurement helper for roofline figures,
+ * with no counterpart in the reference; kd_last_error(NULL) reports failures. */
+int kd_fp32_peak(int32_t device, double out[2]);
 
 /* Interaction counts of the last walk, summed over bodies: out[0] = pair (P2P)
  * interactions, out[2] = accepted multipole (M2P) interactions.  FP64 walk: out[1] =

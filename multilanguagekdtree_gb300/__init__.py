@@ -8,9 +8,9 @@ ctypes binding and the reference's module surface (``array_kd_tree``, ``array_pa
 from . import array_particle
 from .quickstat import quickstat_index
 from .array_kd_tree import (KDError, KDTreeSim, allocate_node_vec, build_tree, calc_accel,
-                            nodes_needed, simple_sim)
+                            fp32_peak, nodes_needed, simple_sim)
 from .array_particle import PARTICLE_DTYPE, circular_orbits, plummer, ring, two_bodies
 
 __all__ = ["KDTreeSim", "KDError", "allocate_node_vec", "nodes_needed", "build_tree",
            "calc_accel", "simple_sim", "PARTICLE_DTYPE", "circular_orbits", "ring", "plummer",
-           "two_bodies", "array_particle", "quickstat_index"]
+           "two_bodies", "array_particle", "quickstat_index", "fp32_peak"]

@@ -99,6 +99,8 @@ SIGNATURES = {
     "kd_direct_accel_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
                                           C.c_void_p]),
+    "kd_set_device_limits": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "kd_fp32_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "kd_set_counting": (C.c_int, [C.c_void_p, C.c_int32]),
     "kd_get_counts": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
 }

@@ -27,7 +27,7 @@ from . import _lib
 from ._lib import NODE_DTYPE, PARTICLE_DTYPE, KDError
 
 __all__ = ["KDTreeSim", "Tape", "allocate_node_vec", "nodes_needed", "build_tree", "calc_accel",
-           "simple_sim", "KDError", "NODE_DTYPE", "LAYOUTS", "PRECISIONS"]
+           "simple_sim", "fp32_peak", "KDError", "NODE_DTYPE", "LAYOUTS", "PRECISIONS"]
 
 LAYOUTS = {"dfs": _lib.KD_LAYOUT_DFS, "par4": _lib.KD_LAYOUT_PAR4}
 PRECISIONS = {"fp64": _lib.KD_PREC_FP64, "mixed": _lib.KD_PREC_MIXED}
@@ -57,6 +57,17 @@ def group_plan(n: int, leaf_size: int = 7):
     if rc != 0:
         raise ValueError(f"kd_group_plan failed ({rc})")
     return gstart, gsplit
+
+
+def fp32_peak(device: int = 0) -> dict:
+    """Measured FP32 multiply-add rate of a device in TFLOP/s (kd_fp32_peak): scalar
+    fma.rn.f32 and packed fma.rn.f32x2."""
+    lib = _lib.load()
+    out = (C.c_double * 2)()
+    rc = lib.kd_fp32_peak(device, out)
+    if rc != 0:
+        raise KDError(rc, lib.kd_last_error(None).decode())
+    return {"scalar": float(out[0]), "packed": float(out[1])}
 
 
 def nodes_needed(n: int, leaf_size: int = 8, layout="par4") -> int:
@@ -200,6 +211,10 @@ class KDTreeSim:
         out = np.empty((len(s), 3), dtype=np.float64)
         self._check(self._lib.kd_direct_accel(self._ctx, _lib.ptr(s), len(s), _lib.ptr(out)))
         return out
+
+    def set_device_limits(self, stack_entries: int = -1, select_passes: int = -1) -> None:
+        """Lower the device-side guards (kd_set_device_limits; negative = the default)."""
+        self._check(self._lib.kd_set_device_limits(self._ctx, stack_entries, select_passes))
 
     def set_counting(self, on: bool) -> None:
         self._check(self._lib.kd_set_counting(self._ctx, 1 if on else 0))

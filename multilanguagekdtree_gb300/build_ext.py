@@ -18,7 +18,7 @@ INCLUDE = PKG.parent / "include"
 OBJDIR = PKG.parent / "_build" / "kdnbody"
 LIB = PKG / "libkdnbody.so"
 SOURCES = ["kd_build.cu", "kd_walk.cu", "kd_group.cu", "kd_adjoint.cu", "kd_generate.cu",
-           "kd_api.cu", "kd_noalloc.cu"]
+           "kd_api.cu", "kd_noalloc.cu", "kd_probe.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",

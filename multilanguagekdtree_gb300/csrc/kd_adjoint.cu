@@ -75,7 +75,7 @@ __global__ void k_adj_combine(Topology t, const NodeF *__restrict__ rec,
 int launch_adjoint_step(const AdjArgs &a, cudaStream_t st) {
     const uint32_t n3 = 3 * a.n;
     int grid = (int)((n3 + 255) / 256);
-    if (grid > 152 * 16) grid = 152 * 16;
+    if (grid > sm_count() * 16) grid = sm_count() * 16;
     k_adj_mu<<<grid, 256, 0, st>>>(a.lx, a.lv, a.mu, n3, a.dt);
     cudaMemsetAsync(a.U, 0, sizeof(double) * 3 * (size_t)a.n, st);
     cudaMemsetAsync(a.G, 0, sizeof(double) * 3 * (size_t)a.topo.n_nodes, st);

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <charconv>
 #include <cmath>
 #include <cstdarg>
@@ -195,6 +196,12 @@ struct kd_ctx {
              *d_leaves = nullptr, *d_ttab = nullptr, *d_local_roots = nullptr,
              *d_gstart = nullptr, *d_gsplit = nullptr;
     uint32_t n_groups = 0, group_stack = 0;
+    // device-side limits (kd_set_device_limits): 0 = the defaults
+    uint32_t stack_limit = 0;
+    int select_passes = kSelMaxIters;
+    uint32_t walk_stack() const {  // stack entries of the grouped walk (and its adjoint)
+        return stack_limit && stack_limit < group_stack ? stack_limit : group_stack;
+    }
     std::vector<uint32_t *> d_glevels;
     Topology topo{};
 
@@ -215,6 +222,7 @@ struct kd_ctx {
     unsigned long long *d_counts = nullptr;
     uint32_t *d_heavy = nullptr, *d_nheavy = nullptr;
     double *d_total = nullptr;
+    double *d_hpart = nullptr;  // per-block partial direct sums of the heavy bodies
     double *gen_scratch = nullptr;
     double *phi = nullptr;  // potentials, allocated by the first kd_energy
     int n_heavy = 0;
@@ -252,6 +260,10 @@ struct kd_ctx {
     // forward sweep left them), or nothing (0)
     uint64_t tapes = 0, seg_owner = 0;
     double *aU = nullptr, *aG = nullptr;
+    // state buffers (6n doubles) of checkpoints, kept by the context and reused by later
+    // forward sweeps once their tape is freed: no cudaMalloc (and its device-wide
+    // synchronisation) in front of every sweep
+    std::vector<double *> ck_free;
 
     int fail(int code, const char *fmt, ...) {
         char buf[512];
@@ -383,6 +395,7 @@ int setup(kd_ctx *c) {
     KD_CHECK(c, c->alloc(&c->d_heavy, kMaxHeavy));
     KD_CHECK(c, c->alloc(&c->d_nheavy, 1));
     KD_CHECK(c, c->alloc(&c->d_total, 1 + 304));  // total mass + per-block partials
+    KD_CHECK(c, c->alloc(&c->d_hpart, (size_t)walk_group_blocks(c->n_groups) * kMaxHeavy * 4));
     KD_CHECK(c, c->alloc(&c->gen_scratch, 6 * 256));
     KD_CHECK(c, cudaMemset(c->dev_err, 0, sizeof(uint32_t)));
     // the build's ping-pong buffers start as valid bodies (id 0 at the origin), so a slot a
@@ -433,6 +446,7 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
         lv.multi = p.gmax[l] > kMultiMin;
         lv.rank = kMedianRank;
         lv.med_pos = nullptr;
+        lv.max_iters = c->select_passes;
         const uint32_t G_next = l + 1 < p.glevels.size() ? (uint32_t)p.glevels[l + 1].size() : 0u;
         c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, (int)l, G_next,
                                     c->st, true, p.gmax[l]);
@@ -459,16 +473,18 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
 }
 
 void enqueue_walk(kd_ctx *c) {
-    c->launches += 1;
     unsigned long long *cnt = c->counting ? c->d_counts : nullptr;
-    if (c->prm.precision == KD_PREC_MIXED)
-        launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart, c->d_gsplit,
-                          c->n_groups, c->group_stack, c->prm.theta, c->bodies, c->d_heavy,
-                          c->n_heavy, c->acc, c->dev_err, cnt, c->st);
-    else
+    if (c->prm.precision == KD_PREC_MIXED) {
+        c->launches += launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart,
+                                         c->d_gsplit, c->n_groups, c->walk_stack(),
+                                         c->prm.theta, c->bodies, c->d_heavy, c->n_heavy,
+                                         c->acc, c->d_hpart, c->dev_err, cnt, c->st);
+    } else {
+        c->launches += 1;
         launch_walk_fp64(c->recd, c->recp, c->thi, c->tlo, c->tpos, c->tid, (uint32_t)c->n,
-                         c->prm.theta, c->acc,
-                         c->dev_err, cnt, c->st);
+                         c->prm.theta, c->acc, c->dev_err, cnt, c->st,
+                         c->stack_limit ? c->stack_limit : (uint32_t)kStackMax);
+    }
 }
 
 int fetch_counts(kd_ctx *c) {
@@ -583,7 +599,7 @@ void enqueue_step(kd_ctx *c, double dt) {
     const bool mixed = c->prm.precision == KD_PREC_MIXED;
     enqueue_build(c, !mixed, mixed);
     enqueue_walk(c);
-    launch_kick_drift(c->bodies, c->acc, (uint32_t)c->n, dt, c->st);
+    launch_kick_drift(c->bodies, c->acc, (uint32_t)c->n, dt, c->dev_err, c->st);
     c->launches += 1;
 }
 
@@ -671,6 +687,26 @@ void enqueue_adj_step(kd_ctx *c, const AdjArgs &a) {
 
 namespace kd {
 void set_thread_error(const char *msg) { g_create_error = msg ? msg : ""; }
+
+int sm_count() {
+    constexpr int kDevices = 64;
+    static std::atomic<int> cache[kDevices];  // 0: not queried yet
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevices) {
+        cudaGetLastError();
+        dev = -1;
+    }
+    int v = dev >= 0 ? cache[dev].load(std::memory_order_relaxed) : 0;
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev < 0 ? 0 : dev) !=
+            cudaSuccess ||
+        v <= 0) {
+        cudaGetLastError();
+        return 1;  // grid-stride kernels stay correct on any grid
+    }
+    if (dev >= 0) cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
 }  // namespace kd
 
 // Rust's `{}` for f64: the shortest digits that round-trip, written positionally (never in
@@ -727,14 +763,22 @@ size_t kd_nodes_needed(size_t n, int32_t leaf_size, int32_t layout) {
 
 int kd_group_plan(size_t n, int32_t leaf_size, uint32_t *gstart, uint32_t *gsplit, size_t cap,
                   size_t *n_groups) {
-    if (n < 1 || n >= (size_t)1 << 31 || leaf_size < 2 || leaf_size > KD_MAX_LEAF || !n_groups)
+    if (n < 1 || n >= (size_t)1 << 31 || leaf_size < 2 || leaf_size > KD_MAX_LEAF || !n_groups) {
+        g_create_error = "kd_group_plan: need 1 <= n < 2^31, leaf_size in [2, 8], n_groups";
         return KD_EINVAL;
+    }
     Plan p;
     std::string err;
-    if (!make_plan((uint32_t)n, (uint32_t)leaf_size, p, err)) return KD_EINVAL;
+    if (!make_plan((uint32_t)n, (uint32_t)leaf_size, p, err)) {
+        g_create_error = "kd_group_plan: " + err;
+        return KD_EINVAL;
+    }
     const size_t ng = p.gstart.size() - 1;
     *n_groups = ng;
-    if (!gstart || !gsplit || cap < ng + 1) return KD_EINVAL;
+    if (!gstart || !gsplit || cap < ng + 1) {
+        g_create_error = "kd_group_plan: gstart needs n_groups + 1 entries (gsplit n_groups)";
+        return KD_EINVAL;
+    }
     std::copy(p.gstart.begin(), p.gstart.end(), gstart);
     std::copy(p.gsplit.begin(), p.gsplit.end(), gsplit);
     return KD_OK;
@@ -870,6 +914,7 @@ int kd_build_tree(kd_ctx *c, size_t *last_node) {
     if (!c) return KD_EINVAL;
     if (!c->has_bodies) return c->fail(KD_ESTATE, "no bodies set");
     KD_CHECK(c, cudaSetDevice(c->prm.device));
+    c->has_tree = false;  // until this build has passed its device checks
     KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
     enqueue_build(c, true, true);
     KD_CHECK(c, cudaEventRecord(c->ev[1], c->st));
@@ -1053,9 +1098,9 @@ int kd_energy(kd_ctx *c, double out[2]) {
     if (!c->phi) KD_CHECK(c, c->alloc(&c->phi, c->n));
     constexpr int kBlocks = 256;
     enqueue_build(c, false, true);
-    launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart, c->d_gsplit, c->n_groups,
-                      c->group_stack, c->prm.theta, c->bodies, c->d_heavy, c->n_heavy, c->acc,
-                      c->dev_err, nullptr, c->st, c->phi);
+    launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart, c->d_gsplit,
+                      c->n_groups, c->walk_stack(), c->prm.theta, c->bodies, c->d_heavy,
+                      c->n_heavy, c->acc, c->d_hpart, c->dev_err, nullptr, c->st, c->phi);
     launch_energy_partial(c->bodies, c->phi, (uint32_t)c->n, c->gen_scratch, kBlocks, c->st);
     double part[2 * kBlocks];
     KD_CHECK(c, cudaMemcpyAsync(part, c->gen_scratch, sizeof part, cudaMemcpyDeviceToHost,
@@ -1165,7 +1210,7 @@ int kd_simple_sim(kd_ctx *c, double dt, int64_t steps) {
         if (e) KD_CHECK(c, cudaEventRecord(e[2], c->st));
         enqueue_walk(c);
         if (e) KD_CHECK(c, cudaEventRecord(e[3], c->st));
-        launch_kick_drift(c->bodies, c->acc, (uint32_t)c->n, dt, c->st);
+        launch_kick_drift(c->bodies, c->acc, (uint32_t)c->n, dt, c->dev_err, c->st);
         c->launches += 1;
         if (e) KD_CHECK(c, cudaEventRecord(e[4], c->st));
     }
@@ -1226,12 +1271,21 @@ int kd_forward(kd_ctx *c, double dt, int64_t steps, int64_t ckpt_every, kd_tape 
     t->final_state = nullptr;
     const size_t nck = (size_t)((steps + ckpt_every - 1) / ckpt_every);
     cudaError_t e = cudaSuccess;
-    for (size_t k = 0; k < nck && e == cudaSuccess; ++k) {
+    auto take = [&]() -> double * {
+        if (!c->ck_free.empty()) {
+            double *p = c->ck_free.back();
+            c->ck_free.pop_back();
+            return p;
+        }
         double *p = nullptr;
-        e = cudaMalloc((void **)&p, 6 * c->n * sizeof(double));
-        if (e == cudaSuccess) t->ck.push_back(p);
+        e = c->alloc(&p, 6 * c->n);
+        return e == cudaSuccess ? p : nullptr;
+    };
+    for (size_t k = 0; k < nck && e == cudaSuccess; ++k) {
+        double *p = take();
+        if (p) t->ck.push_back(p);
     }
-    if (e == cudaSuccess) e = cudaMalloc((void **)&t->final_state, 6 * c->n * sizeof(double));
+    if (e == cudaSuccess) t->final_state = take();
     if (e != cudaSuccess) {
         kd_tape_free(reinterpret_cast<kd_tape *>(t));
         return c->cuda_fail(e, "checkpoint allocation");
@@ -1318,7 +1372,7 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
     a.gstart = c->d_gstart;
     a.gsplit = c->d_gsplit;
     a.n_groups = c->n_groups;
-    a.stk_cap = c->group_stack;
+    a.stk_cap = c->walk_stack();
     c->launches = 0;
     KD_CHECK(c, cudaEventRecord(c->ev[0], c->st));
     const int64_t nseg = (t->steps + t->every - 1) / t->every;
@@ -1366,12 +1420,11 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
 void kd_tape_free(kd_tape *tape) {
     if (!tape) return;
     kd_tape_impl *t = reinterpret_cast<kd_tape_impl *>(tape);
-    if (t->ctx) {
-        cudaSetDevice(t->ctx->prm.device);
-        cudaStreamSynchronize(t->ctx->st);
-    }
-    for (double *p : t->ck) cudaFree(p);
-    if (t->final_state) cudaFree(t->final_state);
+    // the checkpoint buffers belong to the context: back to its free list for the next
+    // forward sweep (kd_destroy releases them)
+    kd_ctx *c = t->ctx;
+    for (double *p : t->ck) c->ck_free.push_back(p);
+    if (t->final_state) c->ck_free.push_back(t->final_state);
     delete t;
 }
 
@@ -1408,6 +1461,23 @@ int kd_direct_accel(kd_ctx *c, const uint64_t *sinks, size_t ns, double *acc) {
     cudaFree(d_part);
     cudaFree(d_acc);
     if (e != cudaSuccess) return c->cuda_fail(e, "kd_direct_accel");
+    return KD_OK;
+}
+
+int kd_set_device_limits(kd_ctx *c, int32_t stack_entries, int32_t select_passes) {
+    if (!c) return KD_EINVAL;
+    if ((stack_entries >= 0 && stack_entries < 2) || select_passes > kSelMaxIters)
+        return c->fail(KD_EINVAL, "need stack_entries >= 2 and select_passes <= %d "
+                       "(negative: the default)", kSelMaxIters);
+    c->stack_limit = stack_entries < 0 ? 0u : (uint32_t)stack_entries;
+    c->select_passes = select_passes < 0 ? kSelMaxIters : (int)select_passes;
+    // the captured step graphs hold the old limits as kernel arguments
+    KD_CHECK(c, cudaSetDevice(c->prm.device));
+    KD_CHECK(c, cudaStreamSynchronize(c->st));
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    if (c->adj_graph) cudaGraphExecDestroy(c->adj_graph);
+    c->graph = nullptr;
+    c->adj_graph = nullptr;
     return KD_OK;
 }
 

@@ -192,7 +192,7 @@ __global__ __launch_bounds__(256) void k_init_work(Bodies b, double *wx, double 
 void launch_init_work(const Bodies &b, Work &w, uint32_t n, unsigned long long *bmin,
                       unsigned long long *bmax, cudaStream_t st) {
     int blocks = (int)((n + 255) / 256);
-    if (blocks > 2432) blocks = 2432;  // 16 per SM: a few thousand box atomics in all
+    if (blocks > sm_count() * 16) blocks = sm_count() * 16;  // a few thousand box atomics
     if (bmin) {
         cudaMemsetAsync(bmin, 0xff, sizeof(unsigned long long) * 3, st);
         cudaMemsetAsync(bmax, 0x00, sizeof(unsigned long long) * 3, st);
@@ -217,7 +217,7 @@ __global__ void k_gather_keys(const double *vals, uint64_t n_vals, const uint64_
 void launch_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx, uint32_t n,
                         double *key, uint32_t *id, uint32_t *err, cudaStream_t st) {
     int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > sm_count() * 16) blocks = sm_count() * 16;
     k_gather_keys<<<blocks, 256, 0, st>>>(vals, n_vals, idx, n, key, id, err);
 }
 
@@ -535,7 +535,7 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
     // refine until at most 32 candidates are left (ranked in one warp below); a pass that
     // cannot narrow any further (the error path) leaves up to kSelCap for the block sort
     for (int iter = 0; c > 32u; ++iter) {
-        if (iter >= kSelMaxIters) {
+        if (iter >= lv.max_iters) {
             if (threadIdx.x == 0) atomicOr(s.err, kErrSelect);
             c = min(c, (uint32_t)kSelCap);
             if (r >= c) r = c - 1;
@@ -1652,10 +1652,14 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
         o.tid[s0 + k] = id;
         {
             const float hx = (float)x, hy = (float)y, hz = (float)z;
-            const float fm = is_heavy(id, o.heavy, o.n_heavy) ? 0.0f : (float)mm;
+            const bool hv = is_heavy(id, o.heavy, o.n_heavy);
+            const float fm = hv ? 0.0f : (float)mm;
+            // light mass split hi (thi.w) + lo (tlo.w): the heavy bodies' direct sums read
+            // every light mass back to ~2^-48 relative
+            const float fml = hv ? 0.0f : (float)(mm - (double)fm);
             o.thi[s0 + k] = make_float4(hx, hy, hz, fm);
             o.tlo[s0 + k] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
-                                        (float)(z - (double)hz), 0.0f);
+                                        (float)(z - (double)hz), fml);
             if (o.recf) {
                 const uint32_t l0 = S.perm[S.perm2[k]];
                 o.trel[s0 + k] = make_float4((float)(x - S.x[l0]), (float)(y - S.y[l0]),

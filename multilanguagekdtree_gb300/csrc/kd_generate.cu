@@ -152,7 +152,7 @@ __global__ void k_mean_sub(Bodies b, uint32_t n, const double *part, int nblk) {
 int launch_generate(int kind, Bodies &b, uint32_t n, uint64_t seed, double *scratch,
                     cudaStream_t st) {
     int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks > sm_count() * 8) blocks = sm_count() * 8;
     switch (kind) {
         case 0:
             k_gen_ring<<<blocks, 256, 0, st>>>(b, n, seed);

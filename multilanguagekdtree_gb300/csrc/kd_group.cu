@@ -488,24 +488,35 @@ __device__ __forceinline__ void rotate32(int lane, const float (&mx)[2], const f
 
 }  // namespace
 
+// FP64 mass of the body at tree position s: the light mass as split hi + lo, or, for a heavy
+// body (light mass 0), its own mass.
+__device__ __forceinline__ double body_mass(const float4 &mh, const float4 &ml, uint32_t o,
+                                            const uint32_t *heavy_ids, const Heavy *heavy,
+                                            int n_heavy) {
+    double m = (double)mh.w + (double)ml.w;
+    for (int hh = 0; hh < n_heavy; ++hh)
+        if (heavy_ids[hh] == o) m = heavy[hh].m;
+    return m;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// One warp's group: the walk, the group's own leaves, the heavy bodies' FP64 terms on the
+// group's sinks, and the group's share (hred: [heavy][x, y, z, potential]) of the heavy
+// bodies' own direct sums.
 template <bool kCount, bool kPot>
-__global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
+__device__ __forceinline__ void walk_group_warp(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
     const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
     const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,
-    const uint32_t *__restrict__ gsplit, uint32_t n_groups, uint32_t stk_cap, float theta2,
-    Bodies b, const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
-    double *__restrict__ phi, uint32_t *err, unsigned long long *counts) {
-    extern __shared__ float4 smem[];
-    __shared__ Heavy heavy[kMaxHeavy];
-    if (threadIdx.x < n_heavy) {
-        const uint32_t h = heavy_ids[threadIdx.x];
-        heavy[threadIdx.x] = Heavy{b.x[h], b.y[h], b.z[h], b.m[h]};
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t g = blockIdx.x * kGroupWarps + warp;
-    if (g >= n_groups) return;  // no block-wide barrier follows
+    const uint32_t *__restrict__ gsplit, uint32_t g, uint32_t stk_cap, float theta2,
+    const Bodies &b, const uint32_t *__restrict__ heavy_ids, const Heavy *heavy, int n_heavy,
+    double *__restrict__ acc, double *__restrict__ phi, uint32_t *err,
+    unsigned long long *counts, float4 *smem, double (*hred)[4], int lane, int warp) {
     const WarpMem W = warp_mem(smem, warp, stk_cap, false);
     const Group G = make_group(thi, tlo, gstart[g], gstart[g + 1], gsplit[g], lane);
 
@@ -549,32 +560,66 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
         kahan(sum[u][2], comp[u][2], pz);
         if (kPot) kahan(sum[u][3], comp[u][3], -pp);
     }
+    double ax[2], ay[2], az[2], ph[2], px[2], py[2], pz[2], ms[2];
+    uint32_t o[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        o[u] = G.valid[u] ? tid[G.s[u]] : 0u;
+        ax[u] = (double)sum[u][0] - (double)comp[u][0];
+        ay[u] = (double)sum[u][1] - (double)comp[u][1];
+        az[u] = (double)sum[u][2] - (double)comp[u][2];
+        ph[u] = (double)sum[u][3] - (double)comp[u][3];
+        px[u] = py[u] = pz[u] = ms[u] = 0.0;
+        if (G.valid[u] && n_heavy > 0) {
+            px[u] = b.x[o[u]];
+            py[u] = b.y[o[u]];
+            pz[u] = b.z[o[u]];
+            ms[u] = body_mass(thi[G.s[u]], tlo[G.s[u]], o[u], heavy_ids, heavy, n_heavy);
+        }
+    }
+    // Heavy bodies in FP64, both ways of every (sink, heavy) pair: the heavy body's pull on
+    // the sink (the pair kernel of array_particle.rs:67-76 with 1/|d| from rsqrt64, a few ulp,
+    // in place of the square root and division), and the sink's pull on the heavy body, whose
+    // sum over all bodies is the heavy body's exact direct-sum acceleration (its grouped-walk
+    // value, a residual of FP32 terms that cancel, is replaced by k_heavy_finish).
+    for (int hh = 0; hh < n_heavy; ++hh) {  // warp-uniform
+        const Heavy q = heavy[hh];
+        double rx = 0.0, ry = 0.0, rz = 0.0, rp = 0.0;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (!G.valid[u] || heavy_ids[hh] == o[u]) continue;
+            const double dx = px[u] - q.x, dy = py[u] - q.y, dz = pz[u] - q.z;
+            const double ri = inv_dist(fma(dx, dx, fma(dy, dy, dz * dz)));
+            const double ri3 = ri * ri * ri;
+            const double magi = -q.m * ri3;
+            ax[u] = fma(magi, dx, ax[u]);
+            ay[u] = fma(magi, dy, ay[u]);
+            az[u] = fma(magi, dz, az[u]);
+            if (kPot) ph[u] -= q.m * ri;
+            const double mr = ms[u] * ri3;
+            rx = fma(mr, dx, rx);
+            ry = fma(mr, dy, ry);
+            rz = fma(mr, dz, rz);
+            if (kPot) rp -= ms[u] * ri;
+        }
+        rx = warp_sum(rx);
+        ry = warp_sum(ry);
+        rz = warp_sum(rz);
+        if (kPot) rp = warp_sum(rp);
+        if (lane == 0) {
+            hred[hh][0] = rx;
+            hred[hh][1] = ry;
+            hred[hh][2] = rz;
+            hred[hh][3] = rp;
+        }
+    }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
         if (!G.valid[u]) continue;
-        const uint32_t o = tid[G.s[u]];
-        double ax = (double)sum[u][0] - (double)comp[u][0];
-        double ay = (double)sum[u][1] - (double)comp[u][1];
-        double az = (double)sum[u][2] - (double)comp[u][2];
-        double ph = (double)sum[u][3] - (double)comp[u][3];
-        // heavy bodies in FP64: the pair kernel of array_particle.rs:67-76 with 1/|d| from
-        // rsqrt64 (a few ulp) in place of the square root and division
-        const double px64 = b.x[o], py64 = b.y[o], pz64 = b.z[o];
-        for (int hh = 0; hh < n_heavy; ++hh) {
-            if (heavy_ids[hh] == o) continue;
-            const Heavy q = heavy[hh];
-            const double dx = px64 - q.x, dy = py64 - q.y, dz = pz64 - q.z;
-            const double ri = inv_dist(fma(dx, dx, fma(dy, dy, dz * dz)));
-            const double magi = -q.m * (ri * ri * ri);
-            ax = fma(magi, dx, ax);
-            ay = fma(magi, dy, ay);
-            az = fma(magi, dz, az);
-            if (kPot) ph -= q.m * ri;
-        }
-        acc[3 * (size_t)o] = ax;
-        acc[3 * (size_t)o + 1] = ay;
-        acc[3 * (size_t)o + 2] = az;
-        if (kPot) phi[o] = ph;
+        acc[3 * (size_t)o[u]] = ax[u];
+        acc[3 * (size_t)o[u] + 1] = ay[u];
+        acc[3 * (size_t)o[u] + 2] = az[u];
+        if (kPot) phi[o[u]] = ph[u];
     }
     if (kCount && lane == 0) {
         const unsigned long long nv = G.g1 - G.g0;
@@ -584,6 +629,98 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
         atomicAdd(&counts[1], cnt[2]);
         atomicAdd(&counts[2], nv * cnt[1]);
         atomicAdd(&counts[3], nv * cnt[2]);
+    }
+}
+
+template <bool kCount, bool kPot>
+__global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
+    const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
+    const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
+    const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,
+    const uint32_t *__restrict__ gsplit, uint32_t n_groups, uint32_t stk_cap, float theta2,
+    Bodies b, const uint32_t *__restrict__ heavy_ids, int n_heavy, double *__restrict__ acc,
+    double *__restrict__ phi, double *__restrict__ hpart, uint32_t *err,
+    unsigned long long *counts) {
+    extern __shared__ float4 smem[];
+    __shared__ Heavy heavy[kMaxHeavy];
+    __shared__ double hred[kGroupWarps][kMaxHeavy][4];
+    if (threadIdx.x < n_heavy) {
+        const uint32_t h = heavy_ids[threadIdx.x];
+        heavy[threadIdx.x] = Heavy{b.x[h], b.y[h], b.z[h], b.m[h]};
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t g = blockIdx.x * kGroupWarps + warp;
+    if (g < n_groups)  // warp-uniform; every warp reaches the block barrier at the end
+        walk_group_warp<kCount, kPot>(rec, thi, tlo, trel, tid, gstart, gsplit, g, stk_cap,
+                                      theta2, b, heavy_ids, heavy, n_heavy, acc, phi, err,
+                                      counts, smem, hred[warp], lane, warp);
+    else if (lane == 0)
+        for (int hh = 0; hh < n_heavy; ++hh)
+            hred[warp][hh][0] = hred[warp][hh][1] = hred[warp][hh][2] = hred[warp][hh][3] = 0.0;
+    if (n_heavy == 0) return;  // block-uniform
+    // the block's share of the heavy bodies' direct sums, warps in order (deterministic)
+    __syncthreads();
+    if (threadIdx.x < 4u * (uint32_t)n_heavy) {
+        const int hh = threadIdx.x >> 2, c = threadIdx.x & 3;
+        double v = 0.0;
+        for (int w = 0; w < kGroupWarps; ++w) v += hred[w][hh][c];
+        hpart[((size_t)blockIdx.x * kMaxHeavy + hh) * 4 + c] = v;
+    }
+}
+
+// The heavy bodies' accelerations (and potentials) as FP64 direct sums over every other
+// body: the blocks' partial sums of k_walk_group added in a fixed order (each thread a fixed
+// strided subset, four blocks' partials in flight per round; then the warps' butterflies and
+// the warps in order), so the result is deterministic.  One block per heavy body; overwrites
+// what the grouped walk wrote for it.
+constexpr int kFinishThreads = 1024;
+
+__global__ __launch_bounds__(kFinishThreads) void k_heavy_finish(
+    const double *__restrict__ hpart, uint32_t n_blocks, const uint32_t *__restrict__ heavy_ids,
+    double *__restrict__ acc, double *__restrict__ phi) {
+    __shared__ double red[4][kFinishThreads / 32];
+    const int hh = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    uint32_t q = threadIdx.x;
+    for (; q + 3u * kFinishThreads < n_blocks; q += 4u * kFinishThreads) {
+        dbl4 t[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            t[r] = *reinterpret_cast<const dbl4 *>(
+                hpart + ((size_t)(q + r * kFinishThreads) * kMaxHeavy + hh) * 4);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            v[0] += t[r].x;
+            v[1] += t[r].y;
+            v[2] += t[r].z;
+            v[3] += t[r].w;
+        }
+    }
+    for (; q < n_blocks; q += kFinishThreads) {
+        const dbl4 t =
+            *reinterpret_cast<const dbl4 *>(hpart + ((size_t)q * kMaxHeavy + hh) * 4);
+        v[0] += t.x;
+        v[1] += t.y;
+        v[2] += t.z;
+        v[3] += t.w;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        v[c] = warp_sum(v[c]);
+        if (lane == 0) red[c][warp] = v[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        const int c = threadIdx.x;
+        double t = 0.0;
+        for (int w = 0; w < kFinishThreads / 32; ++w) t += red[c][w];
+        const size_t o = heavy_ids[hh];
+        if (c < 3)
+            acc[3 * o + c] = t;
+        else if (phi)
+            phi[o] = t;
     }
 }
 
@@ -601,10 +738,14 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
     double *__restrict__ Gn, double *__restrict__ yheavy, uint32_t *err) {
     extern __shared__ float4 smem[];
     __shared__ Heavy heavy[kMaxHeavy];
+    __shared__ double hmu[kMaxHeavy][3];
     __shared__ double hred[kGroupWarps][kMaxHeavy][3];
     if (threadIdx.x < n_heavy) {
         const uint32_t h = heavy_ids[threadIdx.x];
         heavy[threadIdx.x] = Heavy{b.x[h], b.y[h], b.z[h], b.m[h]};
+        hmu[threadIdx.x][0] = mu[3 * (size_t)h];
+        hmu[threadIdx.x][1] = mu[3 * (size_t)h + 1];
+        hmu[threadIdx.x][2] = mu[3 * (size_t)h + 2];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -615,12 +756,13 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
     if (g < n_groups) {  // warp-uniform; the block barrier below is reached by every warp
         const WarpMem W = warp_mem(smem, warp, stk_cap, true);
         const Group G = make_group(thi, tlo, gstart[g], gstart[g + 1], gsplit[g], lane);
-        // sinks without a body sit far away with mu = 0: every term they make is zero
+        // sinks without a body sit far away with mu = 0: every term they make is zero.  A
+        // heavy sink's row is its direct sum (below), so it takes no part in the rotation.
         float mx[2], my[2], mz[2], qx[2], qy[2], qz[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             mx[u] = my[u] = mz[u] = 0.f;
-            if (G.valid[u]) {
+            if (G.valid[u] && !is_heavy(tid[G.s[u]], heavy_ids, n_heavy)) {
                 const size_t o = tid[G.s[u]];
                 mx[u] = (float)mu[3 * o];
                 my[u] = (float)mu[3 * o + 1];
@@ -722,8 +864,14 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
             double ysx = (double)sum[u][0] - (double)comp[u][0];
             double ysy = (double)sum[u][1] - (double)comp[u][1];
             double ysz = (double)sum[u][2] - (double)comp[u][2];
-            // heavy bodies in FP64: sink side here, source side reduced over the block
+            // Heavy bodies in FP64, sink side here, source side reduced over the block.  Two
+            // rows meet in every (body o, heavy h) pair: o's row with source h (for a light o;
+            // a heavy o's row is its direct sum), and h's direct-sum row with source o.
             const double X = b.x[o], Y = b.y[o], Z = b.z[o];
+            const bool o_heavy = is_heavy((uint32_t)o, heavy_ids, n_heavy);
+            const double mo = n_heavy > 0 ? body_mass(thi[s], tlo[s], (uint32_t)o, heavy_ids,
+                                                      heavy, n_heavy)
+                                          : 0.0;
 #pragma unroll
             for (int h = 0; h < kMaxHeavy; ++h) {
                 if (h >= n_heavy || heavy_ids[h] == o) continue;
@@ -732,16 +880,29 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
                 const double ri = inv_dist(fma(dx, dx, fma(dy, dy, dz * dz)));
                 const double inv2 = ri * ri;
                 const double inv3 = inv2 * ri;
-                const double dm = dx * mux + dy * muy + dz * muz;
-                const double c3 = 3.0 * dm * inv2;
-                const double wx = inv3 * (mux - c3 * dx), wy = inv3 * (muy - c3 * dy),
-                             wz = inv3 * (muz - c3 * dz);
-                ysx -= q.m * wx;
-                ysy -= q.m * wy;
-                ysz -= q.m * wz;
-                hx[h][0] += q.m * wx;
-                hx[h][1] += q.m * wy;
-                hx[h][2] += q.m * wz;
+                if (!o_heavy) {
+                    const double dm = dx * mux + dy * muy + dz * muz;
+                    const double c3 = 3.0 * dm * inv2;
+                    const double wx = inv3 * (mux - c3 * dx), wy = inv3 * (muy - c3 * dy),
+                                 wz = inv3 * (muz - c3 * dz);
+                    ysx -= q.m * wx;
+                    ysy -= q.m * wy;
+                    ysz -= q.m * wz;
+                    hx[h][0] += q.m * wx;
+                    hx[h][1] += q.m * wy;
+                    hx[h][2] += q.m * wz;
+                }
+                const double hmx = hmu[h][0], hmy = hmu[h][1], hmz = hmu[h][2];
+                const double dh = dx * hmx + dy * hmy + dz * hmz;
+                const double ch = 3.0 * dh * inv2;
+                const double vx = inv3 * (hmx - ch * dx), vy = inv3 * (hmy - ch * dy),
+                             vz = inv3 * (hmz - ch * dz);
+                ysx += mo * vx;
+                ysy += mo * vy;
+                ysz += mo * vz;
+                hx[h][0] -= mo * vx;
+                hx[h][1] -= mo * vy;
+                hx[h][2] -= mo * vz;
             }
             ysink[3 * (size_t)s] = ysx;
             ysink[3 * (size_t)s + 1] = ysy;
@@ -768,34 +929,25 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
     }
 }
 
-void launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
-                       const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
-                       const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta,
-                       const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
-                       uint32_t *err, unsigned long long *counts, cudaStream_t st, double *phi) {
+int launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
+                      const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
+                      const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta,
+                      const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
+                      double *hpart, uint32_t *err, unsigned long long *counts, cudaStream_t st,
+                      double *phi) {
     const uint32_t threads = kGroupWarps * 32;
-    const uint32_t blocks = (n_groups + kGroupWarps - 1) / kGroupWarps;
+    const uint32_t blocks = walk_group_blocks(n_groups);
     const size_t smem = (size_t)kGroupWarps * group_warp_bytes(stk_cap);
     const float theta2 = (float)(theta * theta);
-    if (phi) {
-        auto k = k_walk_group<false, true>;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups,
-                                         stk_cap, theta2, b, heavy_ids, n_heavy, acc, phi, err,
-                                         nullptr);
-    } else if (counts) {
-        auto k = k_walk_group<true, false>;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups,
-                                         stk_cap, theta2, b, heavy_ids, n_heavy, acc, nullptr,
-                                         err, counts);
-    } else {
-        auto k = k_walk_group<false, false>;
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups,
-                                         stk_cap, theta2, b, heavy_ids, n_heavy, acc, nullptr,
-                                         err, nullptr);
-    }
+    auto k = phi ? k_walk_group<false, true>
+                 : (counts ? k_walk_group<true, false> : k_walk_group<false, false>);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<blocks, threads, smem, st>>>(rec, thi, tlo, trel, tid, gstart, gsplit, n_groups, stk_cap,
+                                     theta2, b, heavy_ids, n_heavy, acc, phi, hpart, err,
+                                     counts);
+    if (n_heavy <= 0) return 1;
+    k_heavy_finish<<<n_heavy, kFinishThreads, 0, st>>>(hpart, blocks, heavy_ids, acc, phi);
+    return 2;
 }
 
 void launch_adj_group(const AdjArgs &a, cudaStream_t st) {

@@ -51,6 +51,10 @@ constexpr uint32_t kErrStack = 2u;    // traversal stack overflow
 constexpr uint32_t kErrNumeric = 4u;  // non-finite or negative input
 constexpr uint32_t kErrHeavy = 8u;    // more heavy bodies than kMaxHeavy
 
+// Multiprocessors of the current device (queried once per device): the grid-stride
+// kernels size their grids by it.
+int sm_count();
+
 // ---------------------------------------------------------------- node records
 // Walk record of the FP64 path.  Internal: a = right child (DFS id), b = 0; the left child
 // is always id+1.  Leaf: a = first body in tree order, b = body count (>= 1).
@@ -135,6 +139,7 @@ struct LevelArgs {
     bool multi;              // multi-block select
     uint32_t rank;           // rank to select; kMedianRank = len/2 of every segment
     uint32_t *med_pos;       // if set: receives where the selected element was written
+    int max_iters = kSelMaxIters;  // radix refinement passes of k_select before it gives up
 };
 constexpr uint32_t kMedianRank = 0xffffffffu;
 
@@ -260,10 +265,12 @@ void launch_moments_top(const Topology &t, const uint32_t *roots, uint32_t n_roo
                         const NodeOut &no, const LocalOut &out, cudaStream_t st);
 
 // ---------------------------------------------------------------- launchers (kd_walk.cu)
+// stack_cap: traversal stack entries (at most kStackMax) before the walk reports kErrStack.
 void launch_walk_fp64(const NodeD *rec, const NodeP *recp, const float4 *thi,
                       const float4 *tlo, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
                       double theta, double *acc, uint32_t *err,
-                      unsigned long long *counts, cudaStream_t st);
+                      unsigned long long *counts, cudaStream_t st,
+                      uint32_t stack_cap = kStackMax);
 // Grouped mixed walk: groups of whole leaves, <= kGroupSinks bodies (two per lane of a warp),
 // gstart[g]..gstart[g+1] in tree order, boxed in two parts split at gsplit[g]; stk_cap =
 // per-warp stack entries (a multiple of 32).
@@ -280,16 +287,27 @@ __host__ __device__ inline uint32_t group_warp_bytes(uint32_t stk_cap) {
     return (uint32_t)((kGroupListCap + 2 * kGroupSinks) * sizeof(float4) +
                       stk_cap * sizeof(uint32_t));
 }
-void launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
-                       const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
-                       const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta, const Bodies &b,
-                       const uint32_t *heavy_ids, int n_heavy, double *acc, uint32_t *err,
-                       unsigned long long *counts, cudaStream_t st, double *phi = nullptr);
+// Thread blocks of the grouped walk (kGroupWarps groups each).
+__host__ __device__ inline uint32_t walk_group_blocks(uint32_t n_groups) {
+    return (n_groups + kGroupWarps - 1) / kGroupWarps;
+}
+// The walk, then (n_heavy > 0) the heavy bodies' own accelerations as FP64 direct sums over
+// all bodies: the walk leaves per-block partial sums in hpart (walk_group_blocks(n_groups) *
+// kMaxHeavy * 4 doubles) and k_heavy_finish adds them in block order.  With phi set, also the
+// potentials.  Returns the number of kernels launched.
+int launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
+                      const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
+                      const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta,
+                      const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
+                      double *hpart, uint32_t *err, unsigned long long *counts, cudaStream_t st,
+                      double *phi = nullptr);
 
 // per-block sums (kinetic, potential) of 0.5 m v^2 and 0.5 m phi into part[2*blocks]
 void launch_energy_partial(const Bodies &b, const double *phi, uint32_t n, double *part,
                            int blocks, cudaStream_t st);
-void launch_kick_drift(Bodies &b, double *acc, uint32_t n, double dt, cudaStream_t st);
+// No update once the device error word is set (the state stays at the failed step's start).
+void launch_kick_drift(Bodies &b, double *acc, uint32_t n, double dt, const uint32_t *err,
+                       cudaStream_t st);
 void launch_aos_to_soa(const void *aos, Bodies &b, uint32_t n, uint32_t *err, cudaStream_t st);
 void launch_soa_to_aos(const Bodies &b, void *aos, uint32_t n, cudaStream_t st);
 // The same conversions reading or writing pinned host records directly (a device-accessible

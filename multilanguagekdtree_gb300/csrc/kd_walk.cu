@@ -65,7 +65,7 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
     const float4 *__restrict__ thi, const float4 *__restrict__ tlo,
     const dbl4 *__restrict__ tpos, const uint32_t *__restrict__ tid, uint32_t n,
     double theta2, float theta2f, double *__restrict__ acc, uint32_t *err,
-    unsigned long long *counts) {
+    unsigned long long *counts, uint32_t stack_cap) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t s = (blockIdx.x * kWalkWarps + warp) * 32 + lane;
     const bool valid = s < n;
@@ -130,7 +130,7 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
             }
             const uint32_t open = mask & ~__ballot_sync(kFull, take);
             if (open) {
-                if (sp >= kStackMax) {
+                if (sp >= (int)stack_cap) {
                     if (lane == 0) atomicOr(err, kErrStack);
                     break;
                 }
@@ -176,17 +176,19 @@ __global__ __launch_bounds__(kWalkWarps * 32) void k_walk_fp64(
 void launch_walk_fp64(const NodeD *rec, const NodeP *recp, const float4 *thi,
                       const float4 *tlo, const dbl4 *tpos, const uint32_t *tid, uint32_t n,
                       double theta, double *acc, uint32_t *err, unsigned long long *counts,
-                      cudaStream_t st) {
+                      cudaStream_t st, uint32_t stack_cap) {
     const uint32_t threads = kWalkWarps * 32;
     const uint32_t blocks = (n + threads - 1) / threads;
     const double theta2 = theta * theta;  // THETA * THETA is formed first (array_kd_tree.rs:606)
     const float theta2f = (float)theta2;
+    // the stack lives in the lanes' registers: one entry per lane at most
+    stack_cap = stack_cap < (uint32_t)kStackMax ? stack_cap : (uint32_t)kStackMax;
     if (counts)
         k_walk_fp64<true><<<blocks, threads, 0, st>>>(rec, recp, thi, tlo, tpos, tid, n, theta2,
-                                                      theta2f, acc, err, counts);
+                                                      theta2f, acc, err, counts, stack_cap);
     else
         k_walk_fp64<false><<<blocks, threads, 0, st>>>(rec, recp, thi, tlo, tpos, tid, n, theta2,
-                                                       theta2f, acc, err, nullptr);
+                                                       theta2f, acc, err, nullptr, stack_cap);
 }
 
 // 0.5 m v^2 and 0.5 m phi summed per block in a fixed order (then on the host, in order).
@@ -222,7 +224,11 @@ void launch_energy_partial(const Bodies &b, const double *phi, uint32_t n, doubl
 // ------------------------------------------------------------------ kick-drift
 
 // v += dt*a; p += dt*v (array_kd_tree.rs:649-658), IEEE order without fused multiply-add.
-__global__ void k_kick_drift(Bodies b, const double *__restrict__ acc, uint32_t n, double dt) {
+// After a failed device check of this step (or an earlier one) the state is left as it is,
+// so a call that returns KD_EDEVICE leaves the bodies at the start of the failed step.
+__global__ void k_kick_drift(Bodies b, const double *__restrict__ acc, uint32_t n, double dt,
+                             const uint32_t *err) {
+    if (*(volatile const uint32_t *)err) return;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += gridDim.x * blockDim.x) {
         // every load first: the state arrays may alias as far as the compiler knows
@@ -242,10 +248,11 @@ __global__ void k_kick_drift(Bodies b, const double *__restrict__ acc, uint32_t 
     }
 }
 
-void launch_kick_drift(Bodies &b, double *acc, uint32_t n, double dt, cudaStream_t st) {
+void launch_kick_drift(Bodies &b, double *acc, uint32_t n, double dt, const uint32_t *err,
+                       cudaStream_t st) {
     int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    k_kick_drift<<<blocks, 256, 0, st>>>(b, acc, n, dt);
+    if (blocks > sm_count() * 16) blocks = sm_count() * 16;
+    k_kick_drift<<<blocks, 256, 0, st>>>(b, acc, n, dt, err);
 }
 
 // ------------------------------------------------------------------ body transfer
@@ -268,7 +275,7 @@ __global__ void k_aos_to_soa(const double *__restrict__ aos, Bodies b, uint32_t 
 
 void launch_aos_to_soa(const void *aos, Bodies &b, uint32_t n, uint32_t *err, cudaStream_t st) {
     int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > sm_count() * 16) blocks = sm_count() * 16;
     k_aos_to_soa<<<blocks, 256, 0, st>>>(static_cast<const double *>(aos), b, n, err);
 }
 
@@ -285,7 +292,7 @@ __global__ void k_soa_to_aos(Bodies b, double *__restrict__ aos, uint32_t n) {
 
 void launch_soa_to_aos(const Bodies &b, void *aos, uint32_t n, cudaStream_t st) {
     int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks > sm_count() * 16) blocks = sm_count() * 16;
     k_soa_to_aos<<<blocks, 256, 0, st>>>(b, static_cast<double *>(aos), n);
 }
 
@@ -350,13 +357,13 @@ __global__ __launch_bounds__(kXferRecords) void k_soa_to_host(Bodies b, float4 *
 void launch_host_to_soa(const void *host, Bodies &b, uint32_t n, uint32_t *err,
                         cudaStream_t st) {
     int blocks = (int)((n + kXferRecords - 1) / kXferRecords);
-    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks > sm_count() * 8) blocks = sm_count() * 8;
     k_host_to_soa<<<blocks, kXferRecords, 0, st>>>(static_cast<const float4 *>(host), b, n, err);
 }
 
 void launch_soa_to_host(const Bodies &b, void *host, uint32_t n, cudaStream_t st) {
     int blocks = (int)((n + kXferRecords - 1) / kXferRecords);
-    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks > sm_count() * 8) blocks = sm_count() * 8;
     k_soa_to_host<<<blocks, kXferRecords, 0, st>>>(b, static_cast<float4 *>(host), n);
 }
 
@@ -485,7 +492,7 @@ void launch_find_heavy(const Bodies &b, uint32_t n, double frac, double *scratch
     k_mass_partial<<<kMassBlocks, 256, 0, st>>>(b.m, n, scratch_total + 1);
     k_mass_total<<<1, 32, 0, st>>>(scratch_total + 1, kMassBlocks, scratch_total);
     int blocks = (int)((n + 255) / 256);
-    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks > sm_count() * 8) blocks = sm_count() * 8;
     k_heavy<<<blocks, 256, 0, st>>>(b.m, n, frac, scratch_total, heavy_ids, n_heavy);
 }
 

@@ -58,6 +58,10 @@ class Oracle:
             "orc_calc_accel_all": (None, [_vp, C.c_size_t, _vp, C.c_double, _vp]),
             "orc_calc_accel_abs": (None, [_vp, C.c_size_t, _vp, C.c_double, _vp, _vp]),
             "orc_walk_counts": (None, [_vp, _vp, C.c_double, _vp, C.c_size_t, _vp]),
+            "orc_calc_accel_sinks": (None, [_vp, _vp, C.c_double, _vp, C.c_size_t, _vp, _vp]),
+            "orc_direct_accel_abs": (None, [_vp, C.c_size_t, _vp, C.c_size_t, _vp, _vp]),
+            "orc_sampled_step": (C.c_int, [_vp, C.c_size_t, C.c_double, C.c_int, C.c_double,
+                                           C.c_uint64, _vp, C.c_size_t, _vp]),
             "orc_simple_sim": (C.c_int, [_vp, C.c_size_t, C.c_double, C.c_int64, C.c_int, C.c_int,
                                          C.c_double, C.c_uint64, _vp]),
             "orc_direct_accel": (None, [_vp, C.c_size_t, _vp, C.c_size_t, _vp]),
@@ -141,6 +145,16 @@ class Oracle:
         self.lib.orc_calc_accel_abs(_p(b), len(b), _p(nodes), theta, _p(acc), _p(ab))
         return acc, ab
 
+    def calc_accel_sinks(self, bodies, nodes, sinks, theta: float = 0.3):
+        """The reference walk for the listed sinks only: (acc, sum of |term|) per sink."""
+        b = self._bodies(bodies)
+        nodes = np.ascontiguousarray(nodes, dtype=NODE)
+        s = np.ascontiguousarray(sinks, dtype=np.uint64)
+        acc = np.zeros((len(s), 3))
+        ab = np.zeros(len(s))
+        self.lib.orc_calc_accel_sinks(_p(b), _p(nodes), theta, _p(s), len(s), _p(acc), _p(ab))
+        return acc, ab
+
     def walk_counts(self, bodies, nodes, sinks, theta: float = 0.3) -> dict:
         b = self._bodies(bodies)
         nodes = np.ascontiguousarray(nodes, dtype=NODE)
@@ -196,6 +210,31 @@ class Oracle:
         acc = np.zeros((len(s), 3))
         self.lib.orc_direct_accel(_p(b), len(b), _p(s), len(s), _p(acc))
         return acc
+
+    def sampled_step(self, bodies, dt: float, sinks, leaf: int = 7, theta: float = 0.3,
+                     seed: int = 1):
+        """One timing sample of a simple_sim step on all host threads (advances ``bodies``
+        in place): the whole PAR4 build, the walk for ``sinks`` only, the kick-drift of every
+        body.  Returns the wall seconds (build, sampled walk, kick-drift)."""
+        b = bodies.view(PARTICLE)
+        if not b.flags.c_contiguous:
+            raise ValueError("bodies must be contiguous")
+        s = np.ascontiguousarray(sinks, dtype=np.uint64)
+        t = np.zeros(3)
+        rc = self.lib.orc_sampled_step(_p(b), len(b), dt, leaf, theta, seed, _p(s), len(s),
+                                       _p(t))
+        if rc != 0:
+            raise RuntimeError(f"orc_sampled_step failed ({rc})")
+        return float(t[0]), float(t[1]), float(t[2])
+
+    def direct_accel_abs(self, bodies, sinks):
+        """FP64 direct sum for the sinks and, per sink, the sum of its terms' magnitudes."""
+        b = self._bodies(bodies)
+        s = np.ascontiguousarray(sinks, dtype=np.uint64)
+        acc = np.zeros((len(s), 3))
+        ab = np.zeros(len(s))
+        self.lib.orc_direct_accel_abs(_p(b), len(b), _p(s), len(s), _p(acc), _p(ab))
+        return acc, ab
 
     def adjoint_direct(self, bodies, dt: float, steps: int, target=None, dL_dx=None,
                        dL_dv=None):

@@ -3,7 +3,8 @@
 * ``liboracle.so`` -- the C restatement in ``kdoracle.c``.
 * ``_ref/libkdref.so`` -- the reference's own C port of the path
   (MarkCLewis/MultiLanguageKDTree Parallel/CVersion/src/kdtree.c and particle.c), compiled
-  straight from the reference checkout when it is present.  It is used only to pin the
+  straight from the reference checkout when it is present (its root is taken from the
+  ``KD_REFERENCE_DIR`` environment variable).  It is used only to pin the
   restatement (tests/test_oracle.py, tests/golden/make_golden.py) and as an optional CPU
   baseline.  Nothing is copied from the reference; gcc reads the sources where they lie.
 
@@ -12,6 +13,7 @@ arithmetic (Rust, and C without -ffast-math) rounds every operation.
 """
 from __future__ import annotations
 
+import os
 import shutil
 import subprocess
 import sys
@@ -19,7 +21,9 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "liboracle.so"
-REF_DIR = Path("/root/reference/Parallel/CVersion/src")
+# the reference checkout: KD_REFERENCE_DIR, else where this build's sources mount it
+REF_ROOT = Path(os.environ.get("KD_REFERENCE_DIR", "/root/reference"))
+REF_DIR = REF_ROOT / "Parallel" / "CVersion" / "src"
 REF_LIB = HERE / "_ref" / "libkdref.so"
 CFLAGS = ["-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"]
 

@@ -363,16 +363,31 @@ void orc_calc_accel_abs(const orc_particle *P, size_t n, const orc_node *nodes, 
     }
 }
 
+/* The walk for a list of sinks only (acc[3k..] and absum[k] for sinks[k]): the per-step
+ * sampled checks of large runs, where walking every body each step would take minutes. */
+void orc_calc_accel_sinks(const orc_particle *P, const orc_node *nodes, double theta,
+                          const uint64_t *sinks, size_t ns, double *acc, double *absum) {
+    double theta2 = theta * theta;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (size_t k = 0; k < ns; ++k) {
+        absum[k] = 0.0;
+        accel_recur(0, (size_t)sinks[k], P, nodes, theta2, &acc[3 * k], NULL, &absum[k]);
+    }
+}
+
 /* Instrumented walk over a list of sinks: interaction counts per the reference's walk. */
 void orc_walk_counts(const orc_particle *P, const orc_node *nodes, double theta,
                      const uint64_t *sinks, size_t ns, uint64_t out[4]) {
     double theta2 = theta * theta;
-    orc_counts tot = {0, 0, 0, 0};
+    uint64_t p2p = 0, opened = 0, m2p = 0, visits = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : p2p, opened, m2p, visits)
     for (size_t k = 0; k < ns; ++k) {
         double a[3];
-        accel_recur(0, (size_t)sinks[k], P, nodes, theta2, a, &tot, NULL);
+        orc_counts c = {0, 0, 0, 0};
+        accel_recur(0, (size_t)sinks[k], P, nodes, theta2, a, &c, NULL);
+        p2p += c.p2p; opened += c.opened; m2p += c.m2p; visits += c.visits;
     }
-    out[0] = tot.p2p; out[1] = tot.opened; out[2] = tot.m2p; out[3] = tot.visits;
+    out[0] = p2p; out[1] = opened; out[2] = m2p; out[3] = visits;
 }
 
 /* ---------------------------------------------------------------- grouped walk */
@@ -609,6 +624,51 @@ int orc_simple_sim(orc_particle *P, size_t n, double dt, int64_t steps, int leaf
     return rc;
 }
 
+/* One timing sample of a simple_sim step (array_kd_tree.rs:640-662) on all host threads:
+ * the whole PAR4 build, the walk for the `ns` listed sinks only, and the kick-drift of every
+ * body (the bodies that were not walked keep a zero acceleration and only drift).  t[0..2]
+ * receive the wall seconds of the three parts; the caller scales the walk by n / ns.  Returns
+ * 0, -1 when the node slice overflowed, -2 when out of memory. */
+int orc_sampled_step(orc_particle *P, size_t n, double dt, int leaf, double theta,
+                     uint64_t seed, const uint64_t *sinks, size_t ns, double t[3]) {
+    size_t cap = (size_t)orc_nodes_needed_par(n, leaf);
+    orc_node *nodes = (orc_node *)malloc(cap * sizeof(orc_node));
+    uint64_t *idx = (uint64_t *)malloc(n * sizeof(uint64_t));
+    double *acc = (double *)calloc(3 * n, sizeof(double));
+    double *sa = (double *)malloc(3 * (ns ? ns : 1) * sizeof(double));
+    if (!nodes || !idx || !acc || !sa) { free(nodes); free(idx); free(acc); free(sa); return -2; }
+    double theta2 = theta * theta;
+    double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < n; ++i) idx[i] = i;
+    int rc = orc_build_tree_par4(idx, n, P, nodes, cap, leaf, seed);
+    double t1 = omp_get_wtime();
+#pragma omp parallel for schedule(dynamic, 16)
+    for (size_t k = 0; k < ns; ++k)
+        accel_recur(0, (size_t)sinks[k], P, nodes, theta2, &sa[3 * k], NULL, NULL);
+    double t2 = omp_get_wtime();
+    for (size_t k = 0; k < ns; ++k) memcpy(&acc[3 * (size_t)sinks[k]], &sa[3 * k], 24);
+    double t3 = omp_get_wtime();
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < n; ++i) {
+        orc_particle *b = &P[i];
+        double *a = &acc[3 * i];
+        b->v[0] += dt * a[0];
+        b->v[1] += dt * a[1];
+        b->v[2] += dt * a[2];
+        b->p[0] += dt * b->v[0];
+        b->p[1] += dt * b->v[1];
+        b->p[2] += dt * b->v[2];
+        a[0] = 0.0; a[1] = 0.0; a[2] = 0.0;
+    }
+    double t4 = omp_get_wtime();
+    t[0] = t1 - t0;
+    t[1] = t2 - t1;
+    t[2] = t4 - t3;
+    free(nodes); free(idx); free(acc); free(sa);
+    return rc;
+}
+
 /* ---------------------------------------------------------------- direct sum */
 
 /* FP64 direct sum for a set of sinks: one-sided form of the all-pairs kernel of
@@ -627,6 +687,26 @@ void orc_direct_accel(const orc_particle *P, size_t n, const uint64_t *sinks, si
             a0 += pa[0]; a1 += pa[1]; a2 += pa[2];
         }
         acc[3 * k] = a0; acc[3 * k + 1] = a1; acc[3 * k + 2] = a2;
+    }
+}
+
+/* The same direct sum, also returning per sink the sum of the magnitudes of its terms (the
+ * scale of the rounding error of any other summation order of the same terms). */
+void orc_direct_accel_abs(const orc_particle *P, size_t n, const uint64_t *sinks, size_t ns,
+                          double *acc, double *absum) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (size_t k = 0; k < ns; ++k) {
+        size_t i = (size_t)sinks[k];
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, s = 0.0;
+        for (size_t j = 0; j < n; ++j) {
+            if (j == i) continue;
+            double pa[3];
+            pp_accel(&P[i], &P[j], pa);
+            a0 += pa[0]; a1 += pa[1]; a2 += pa[2];
+            s += sqrt(pa[0] * pa[0] + pa[1] * pa[1] + pa[2] * pa[2]);
+        }
+        acc[3 * k] = a0; acc[3 * k + 1] = a1; acc[3 * k + 2] = a2;
+        absum[k] = s;
     }
 }
 

@@ -44,3 +44,7 @@ def test_group_plan_reports_the_count_when_the_buffer_is_short():
     ng = C.c_size_t(0)
     rc = lib.kd_group_plan(1000, 7, None, None, 0, C.byref(ng))
     assert rc != 0 and ng.value == len(group_plan(1000, 7)[1])
+    # a stale message of an earlier call is replaced by this call's reason
+    assert b"kd_group_plan" in lib.kd_last_error(None)
+    rc = lib.kd_group_plan(0, 7, None, None, 0, C.byref(ng))
+    assert rc != 0 and b"n < 2^31" in lib.kd_last_error(None)

@@ -32,7 +32,9 @@ def test_noalloc_direct_sum_matches_allocating_entry_point(kd):
     mass = torch.from_numpy(np.ascontiguousarray(b["m"])).to(dev)
     with kd.KDTreeSim(n) as s:
         s.set_bodies(b)
-        for call, ns in enumerate((1500, 700)):
+        # 1500 and 700 sinks: the sources in 15 chunks of 4096 bodies; 20000 sinks: the
+        # scratch holds only floor(131072 / (3 * 20000)) = 2 chunks, so each is 30000 bodies
+        for call, ns in enumerate((1500, 700, 20_000)):
             sinks = np.sort(rng.choice(np.arange(1, n), ns, replace=False)).astype(np.uint64)
             ref = s.direct_accel(sinks)
             d_sinks = torch.from_numpy(sinks.view(np.int64)).to(dev)
@@ -47,6 +49,20 @@ def test_noalloc_direct_sum_matches_allocating_entry_point(kd):
             got = out.cpu().numpy()
             err = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
             assert err.max() <= RTOL, (call, err.max())
+
+    # a sink index out of range gives NaN in its row, the other rows are unaffected
+    sinks = np.array([5, n + 3, 17], dtype=np.uint64)
+    d_sinks = torch.from_numpy(sinks.view(np.int64)).to(dev)
+    out = torch.zeros((3, 3), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    rc = lib.kd_direct_accel_noalloc(
+        C.c_void_p(cols[0].data_ptr()), C.c_void_p(cols[1].data_ptr()),
+        C.c_void_p(cols[2].data_ptr()), C.c_void_p(mass.data_ptr()), n,
+        C.c_void_p(d_sinks.data_ptr()), 3, C.c_void_p(out.data_ptr()), None)
+    assert rc == 0, lib.kd_last_error(None)
+    got = out.cpu().numpy()
+    assert np.isnan(got[1]).all()
+    assert np.isfinite(got[[0, 2]]).all()
 
     # beyond the scratch limit: rejected with a message, nothing launched
     big = torch.zeros(43691, dtype=torch.int64, device=dev)
