@@ -51,6 +51,7 @@ struct Plan {
     std::vector<std::vector<uint32_t>> glevels;  // internal nodes of the multi-block levels
     std::vector<uint32_t> gmax;           // largest segment per multi-block level
     std::vector<uint32_t> local_roots;
+    uint32_t local_max = 0;               // bodies of the largest local root
     std::vector<uint32_t> ttab;
     uint64_t par4_slots = 0, par4_last = 0;
     bool par4_ok = true;
@@ -105,6 +106,7 @@ bool make_plan(uint32_t n, uint32_t leaf, Plan &p, std::string &err) {
         if (!local_found && mx <= (uint32_t)kLocalMax) {
             local_found = true;
             for (const E &e : cur) p.local_roots.push_back(e.id);
+            p.local_max = mx;
         }
         std::vector<uint32_t> internal;
         nxt.clear();
@@ -359,6 +361,8 @@ int setup(kd_ctx *c) {
         KD_CHECK(c, c->alloc(&c->work.y[k], n));
         KD_CHECK(c, c->alloc(&c->work.z[k], n));
         KD_CHECK(c, c->alloc(&c->work.id[k], n));
+    }
+    for (int k = 0; k < 3; ++k) {
         KD_CHECK(c, c->alloc(&c->scr.ckey[k], n));
         KD_CHECK(c, c->alloc(&c->scr.cpos[k], n));
     }
@@ -371,6 +375,8 @@ int setup(kd_ctx *c) {
     KD_CHECK(c, c->alloc(&c->scr.cand_cnt, maxG));
     KD_CHECK(c, c->alloc(&c->scr.tile_cnt, maxGT));
     KD_CHECK(c, c->alloc(&c->scr.tile_off, maxGT));
+    KD_CHECK(c, c->alloc(&c->scr.done, maxGmulti));
+    KD_CHECK(c, cudaMemset(c->scr.done, 0, maxGmulti * sizeof(uint32_t)));
     KD_CHECK(c, c->alloc(&c->dev_err, 1));
     c->scr.err = c->dev_err;
     const size_t nn = p.n_nodes;
@@ -467,7 +473,8 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     o.heavy = c->d_heavy;
     o.n_heavy = c->n_heavy;
     const uint32_t nr = (uint32_t)p.local_roots.size();
-    launch_local(c->topo, c->d_local_roots, nr, c->nout, c->work, cur, o, c->dev_err, c->st);
+    launch_local(c->topo, c->d_local_roots, nr, p.local_max, c->nout, c->work, cur, o,
+                 c->dev_err, c->st);
     launch_moments_top(c->topo, c->d_local_roots, nr, c->nout, o, c->st);
     c->final_buf = cur;
 }
@@ -1012,11 +1019,14 @@ int kd_quickstat_index(const double *vals, size_t n_vals, uint64_t *idx, size_t 
     for (int k = 0; k < 2; ++k) {
         w.x[k] = w.y[k] = w.z[k] = (double *)get(n * sizeof(double));
         w.id[k] = (uint32_t *)get(n * sizeof(uint32_t));
-        sc.ckey[k] = (unsigned long long *)get(n * sizeof(unsigned long long));
-        sc.cpos[k] = (uint32_t *)get(n * sizeof(uint32_t));
         sc.bmin[k] = (unsigned long long *)get(3 * sizeof(unsigned long long));
         sc.bmax[k] = (unsigned long long *)get(3 * sizeof(unsigned long long));
     }
+    for (int k = 0; k < 3; ++k) {
+        sc.ckey[k] = (unsigned long long *)get(n * sizeof(unsigned long long));
+        sc.cpos[k] = (uint32_t *)get(n * sizeof(uint32_t));
+    }
+    sc.done = (uint32_t *)get(sizeof(uint32_t));
     sc.sel = (SegSel *)get(sizeof(SegSel));
     sc.hist = (uint32_t *)get(kHistBins * sizeof(uint32_t));
     sc.cand_cnt = (uint32_t *)get(sizeof(uint32_t));
@@ -1040,6 +1050,7 @@ int kd_quickstat_index(const double *vals, size_t n_vals, uint64_t *idx, size_t 
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_idx, idx, n * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_seg, seg_h, sizeof seg_h, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(sc.err, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sc.done, 0, sizeof(uint32_t), st);
     if (e == cudaSuccess) {
         // one segment [0, n): its start / count live where a tree's node arrays would
         Topology t{};

@@ -317,23 +317,18 @@ __device__ __forceinline__ uint32_t lin_bin(double v, float lo, float scale) {
     return f >= (float)(kHistBins - 1) ? (uint32_t)(kHistBins - 1) : (uint32_t)f;
 }
 
-// Split dimension, size and the first-pass binning of every segment.
-__global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin,
-                        const unsigned long long *bmax, SegSel *sel, NodeOut no) {
-    uint32_t seg = blockIdx.x * blockDim.x + threadIdx.x;
-    if (seg >= lv.G) return;
-    uint32_t id = lv.ids[seg];
-    uint32_t cnt = t.count[id];
+// Split choice of a segment from its bounding box (ordered keys), as SegSel plus the node's
+// split_dim and size: the first-pass linear bins span [lo, hi] of the split coordinate.
+__device__ __forceinline__ SegSel make_segsel(const unsigned long long *bmin,
+                                              const unsigned long long *bmax, uint32_t seg,
+                                              uint32_t cnt, uint32_t rank, double &size) {
     double mn[3], mx[3];
     for (int d = 0; d < 3; ++d) {
         mn[d] = ord_val(bmin[seg * 3 + d]);
         mx[d] = ord_val(bmax[seg * 3 + d]);
     }
     uint32_t sd;
-    double size;
     choose_split(mn, mx, sd, size);
-    no.split_dim[id] = (uint8_t)sd;
-    no.size[id] = size;
     SegSel s;
     s.sd = sd;
     s.lo = trunc_float(sd == 0 ? mn[0] : (sd == 1 ? mn[1] : mn[2]));
@@ -342,55 +337,28 @@ __global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin
     s.scale = (range > 0.0f && isfinite(scale)) ? scale : 0.0f;
     s.digit = 0;
     s.c = cnt;
-    s.r = split_rank(lv, cnt);
+    s.r = rank;
     s.pad = 0;
     s.kmed = 0;
     s.idmed = 0;
     s.posmed = 0;
-    sel[seg] = s;
+    s.pad2 = 0;
+    return s;
 }
 
-// First pass over big segments: histogram of linear bins of the split coordinate.
-// A block takes kHistTiles consecutive tiles of one segment, so that zeroing its
-// kHistBins shared bins and merging them into the segment's histogram is paid once per
-// kHistTiles * kTile bodies.
-#ifndef KD_HIST_TILES
-#define KD_HIST_TILES 8
-#endif
-constexpr uint32_t kHistTiles = KD_HIST_TILES;
-
-__global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
-                                                       const double *wx, const double *wy,
-                                                       const double *wz, const SegSel *sel,
-                                                       uint32_t *hist) {
-    const uint32_t per_seg = (lv.tiles + kHistTiles - 1) / kHistTiles;
-    const uint32_t seg = blockIdx.x / per_seg;
-    const uint32_t t0 = (blockIdx.x - seg * per_seg) * kHistTiles;
-    TileRef r;
-    if (!tile_at(t, lv, seg * lv.tiles + t0, r)) return;  // block-uniform
-    const uint32_t hi = min(r.cnt, r.lo + kHistTiles * (uint32_t)kTile);
-    __shared__ uint32_t h[kHistBins];
-    for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) h[b] = 0;
-    __syncthreads();
-    const SegSel s = sel[r.seg];
-    const double *w = pick(wx, wy, wz, s.sd) + r.start;
-    constexpr int kRows = kTile / kTileThreads;
-    for (uint32_t base = r.lo; base < hi; base += kTile) {
-        double v[kRows];
-#pragma unroll
-        for (int i = 0; i < kRows; ++i) {
-            const uint32_t k = base + (uint32_t)i * kTileThreads + threadIdx.x;
-            v[i] = k < hi ? w[k] : 0.0;
-        }
-#pragma unroll
-        for (int i = 0; i < kRows; ++i)
-            if (base + (uint32_t)i * kTileThreads + threadIdx.x < hi)
-                atomicAdd(&h[lin_bin(v[i], s.lo, s.scale)], 1u);
-    }
-    __syncthreads();
-    uint32_t *gh = hist + (size_t)r.seg * kHistBins;
-    for (int b = threadIdx.x; b < kHistBins; b += blockDim.x)
-        if (h[b]) atomicAdd(&gh[b], h[b]);
+// Split dimension, size and the first-pass binning of every segment (levels whose medians
+// k_select finds over the whole segment).
+__global__ void k_split(Topology t, LevelArgs lv, const unsigned long long *bmin,
+                        const unsigned long long *bmax, SegSel *sel, NodeOut no) {
+    uint32_t seg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (seg >= lv.G) return;
+    uint32_t id = lv.ids[seg];
+    uint32_t cnt = t.count[id];
+    double size;
+    const SegSel s = make_segsel(bmin, bmax, seg, cnt, split_rank(lv, cnt), size);
+    no.split_dim[id] = (uint8_t)s.sd;
+    no.size[id] = size;
+    sel[seg] = s;
 }
 
 // Block-wide search of the histogram bin holding rank r.  Every thread owns
@@ -442,30 +410,97 @@ __device__ void find_bin(const uint32_t *h, uint32_t r, uint32_t *out3,
     __syncthreads();
 }
 
-__global__ __launch_bounds__(kTileThreads) void k_find(const uint32_t *hist, SegSel *sel) {
+// First pass over big segments: the split choice (every block of a segment makes the same
+// one from the segment's bounding box), a histogram of linear bins of the split coordinate,
+// and -- in the segment's last block to finish -- the bin holding the wanted rank.  A block
+// takes kHistTiles consecutive tiles of one segment, so that zeroing its kHistBins shared
+// bins and merging them into the segment's histogram is paid once per kHistTiles * kTile
+// bodies.  `done` counts the finished blocks of every segment (the last one resets it).
+#ifndef KD_HIST_TILES
+#define KD_HIST_TILES 8
+#endif
+constexpr uint32_t kHistTiles = KD_HIST_TILES;
+
+__global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
+                                                       const double *wx, const double *wy,
+                                                       const double *wz,
+                                                       const unsigned long long *bmin,
+                                                       const unsigned long long *bmax,
+                                                       SegSel *sel, NodeOut no, uint32_t *hist,
+                                                       uint32_t *done) {
+    const uint32_t per_seg = (lv.tiles + kHistTiles - 1) / kHistTiles;
+    const uint32_t seg = blockIdx.x / per_seg;
+    const uint32_t t0 = (blockIdx.x - seg * per_seg) * kHistTiles;
+    const uint32_t id = lv.ids[seg];
+    const uint32_t cnt = t.count[id];
+    double size;
+    const SegSel s = make_segsel(bmin, bmax, seg, cnt, split_rank(lv, cnt), size);
+    __shared__ uint32_t h[kHistBins];
     __shared__ uint32_t out3[3];
-    const uint32_t seg = blockIdx.x;
-    find_bin(hist + (size_t)seg * kHistBins, sel[seg].r, out3);
+    __shared__ bool last;
+    TileRef r;
+    const bool has = tile_at(t, lv, seg * lv.tiles + t0, r);  // block-uniform
+    uint32_t *gh = hist + (size_t)seg * kHistBins;
+    if (has) {
+        const uint32_t hi = min(r.cnt, r.lo + kHistTiles * (uint32_t)kTile);
+        for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) h[b] = 0;
+        __syncthreads();
+        const double *w = pick(wx, wy, wz, s.sd) + r.start;
+        constexpr int kRows = kTile / kTileThreads;
+        for (uint32_t base = r.lo; base < hi; base += kTile) {
+            double v[kRows];
+#pragma unroll
+            for (int i = 0; i < kRows; ++i) {
+                const uint32_t k = base + (uint32_t)i * kTileThreads + threadIdx.x;
+                v[i] = k < hi ? w[k] : 0.0;
+            }
+#pragma unroll
+            for (int i = 0; i < kRows; ++i)
+                if (base + (uint32_t)i * kTileThreads + threadIdx.x < hi)
+                    atomicAdd(&h[lin_bin(v[i], s.lo, s.scale)], 1u);
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < kHistBins; b += blockDim.x)
+            if (h[b]) atomicAdd(&gh[b], h[b]);
+    }
+    // the segment's last block sees every block's bins
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&done[seg], 1u) == per_seg - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) h[b] = __ldcg(&gh[b]);
+    __syncthreads();
+    find_bin(h, s.r, out3);
     if (threadIdx.x == 0) {
-        sel[seg].digit = out3[0];
-        sel[seg].r -= out3[1];
-        sel[seg].c = out3[2];
+        SegSel o = s;
+        o.digit = out3[0];
+        o.r = s.r - out3[1];
+        o.c = out3[2];
+        sel[seg] = o;
+        no.split_dim[id] = (uint8_t)s.sd;
+        no.size[id] = size;
+        done[seg] = 0u;
     }
 }
 
 // Gather the keys of the selected first-pass bin as candidates (unordered; the exact
-// select below does not depend on their order).
+// select below does not depend on their order), and count per tile the bodies of lower bins:
+// they go left whatever the median inside the bin (bins order the bodies as their keys do),
+// so tile_cnt starts as that count and k_select adds the candidates that go left.
 __global__ __launch_bounds__(kTileThreads) void k_collect(Topology t, LevelArgs lv,
                                                           const double *wx, const double *wy,
                                                           const double *wz, const SegSel *sel,
                                                           uint32_t *cand_cnt,
                                                           unsigned long long *ckey,
-                                                          uint32_t *cpos) {
+                                                          uint32_t *cpos, uint32_t *tile_cnt) {
     TileRef r;
     if (!tile_of(t, lv, r)) return;
     const SegSel s = sel[r.seg];
     const double *w = pick(wx, wy, wz, s.sd) + r.start;
     const int lane = threadIdx.x & 31;
+    uint32_t below = 0;
     constexpr int kRows = kTile / kTileThreads;
     double vr[kRows];
 #pragma unroll
@@ -479,7 +514,9 @@ __global__ __launch_bounds__(kTileThreads) void k_collect(Topology t, LevelArgs 
         bool in = k < r.hi;
         const double v = vr[i];
         const unsigned long long key = ord_key(v);
-        bool hit = in && lin_bin(v, s.lo, s.scale) == s.digit;
+        const uint32_t bin = lin_bin(v, s.lo, s.scale);
+        below += (in && bin < s.digit) ? 1u : 0u;
+        bool hit = in && bin == s.digit;
         uint32_t m = __ballot_sync(kFull, hit);
         if (m) {
             uint32_t leader = __ffs(m) - 1, slot = 0;
@@ -492,11 +529,121 @@ __global__ __launch_bounds__(kTileThreads) void k_collect(Topology t, LevelArgs 
             }
         }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) below += __shfl_xor_sync(kFull, below, o);
+    __shared__ uint32_t ws[kTileThreads / 32];
+    if (lane == 0) ws[threadIdx.x >> 5] = below;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (int i = 0; i < kTileThreads / 32; ++i) tot += ws[i];
+        tile_cnt[(size_t)r.seg * lv.tiles + r.tile] = tot;
+    }
+}
+
+__device__ __forceinline__ bool goes_left(unsigned long long key, uint32_t id,
+                                          unsigned long long kmed, uint32_t idmed) {
+    return key < kmed || (key == kmed && id < idmed);
+}
+
+// The last step of k_select when more than 32 candidates are left (a refinement that could
+// not narrow them): a bitonic sort of (key, id) and a pick at the wanted rank.
+template <typename Get>
+__device__ __forceinline__ void select_sorted(unsigned long long *skey, unsigned long long *sval,
+                                              uint32_t c, uint32_t r, SegSel *sel, uint32_t seg,
+                                              NodeOut no, uint32_t nid, const double *w,
+                                              const uint32_t *ids, Get &get,
+                                              unsigned long long &s_kmed, uint32_t &s_idmed) {
+    const uint32_t P = next_pow2(c);
+    for (uint32_t j = threadIdx.x; j < P; j += blockDim.x) {
+        if (j < c) {
+            unsigned long long key;
+            uint32_t pos;
+            get(j, key, pos);
+            skey[j] = key;
+            sval[j] = ((unsigned long long)ids[pos] << 32) | pos;
+        } else {
+            skey[j] = ~0ull;
+            sval[j] = ~0ull;
+        }
+    }
+    __syncthreads();
+    if (P > 1) bitonic_blocks(skey, sval, P, P);
+    if (threadIdx.x == 0) {
+        unsigned long long v = sval[r];
+        uint32_t pos = (uint32_t)(v & 0xffffffffull);
+        sel[seg].kmed = skey[r];
+        sel[seg].idmed = (uint32_t)(v >> 32);
+        sel[seg].posmed = pos;
+        no.split_val[nid] = w[pos];
+        s_kmed = skey[r];
+        s_idmed = (uint32_t)(v >> 32);
+    }
+}
+
+// Tile offsets of the partition (see k_select), one block per segment.
+constexpr int kSmallSegTiles = 8;  // non-multi segments: at most kMultiMin / kTile tiles
+static_assert(kMultiMin <= (uint32_t)(kSmallSegTiles * kTile), "tile counters of a small segment");
+
+__device__ __forceinline__ void tile_offsets(const Topology &t, const LevelArgs &lv,
+                                             const Scratch &s, const SegSel &st, uint32_t seg,
+                                             uint32_t nid, uint32_t start, const double *w,
+                                             const uint32_t *ids, unsigned long long kmed,
+                                             uint32_t idmed) {
+    __shared__ uint32_t scnt[kSmallSegTiles];
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t cnt = t.count[nid];
+    const uint32_t ntiles = (cnt + kTile - 1) / kTile;
+    uint32_t *tc = s.tile_cnt + (size_t)seg * lv.tiles;
+    uint32_t *to = s.tile_off + (size_t)seg * lv.tiles;
+    if (lv.multi) {
+        // the candidates of the first-pass bin that go left, added to the lower-bin counts
+        for (uint32_t j = threadIdx.x; j < st.c; j += blockDim.x) {
+            const uint32_t pos = s.cpos[0][start + j];
+            if (goes_left(s.ckey[0][start + j], ids[pos], kmed, idmed))
+                atomicAdd(&tc[pos / kTile], 1u);
+        }
+    } else {
+        if (threadIdx.x < kSmallSegTiles) scnt[threadIdx.x] = 0u;
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x)
+            if (goes_left(ord_key(w[j]), ids[j], kmed, idmed)) atomicAdd(&scnt[j / kTile], 1u);
+        __syncthreads();
+        if (threadIdx.x < ntiles && threadIdx.x < kSmallSegTiles) tc[threadIdx.x] = scnt[threadIdx.x];
+        if (threadIdx.x == 0 && ntiles > kSmallSegTiles) atomicOr(s.err, kErrSelect);
+    }
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < ntiles; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < ntiles ? __ldcg(&tc[i]) : 0u;
+        uint32_t inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(kFull, inc, o);
+            if (lane >= o) inc += u;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        uint32_t wpre = 0;
+        for (int q = 0; q < warp; ++q) wpre += wsum[q];
+        if (i < ntiles) to[i] = carry + wpre + inc - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += wpre + inc;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && carry != split_rank(lv, cnt)) atomicOr(s.err, kErrSelect);
 }
 
 // Exact median of every segment: radix refinement until at most kSelCap candidates are
 // left, then a bitonic sort of (key, id) in shared memory and a pick at the wanted rank.
-// Candidates start as the collected first-pass bin (multi) or the whole segment.
+// Candidates start as the collected first-pass bin (multi: buffer 0, which the refinement
+// passes, alternating between buffers 1 and 2, leave intact) or the whole segment.  Then the
+// partition's tile offsets: the bodies going left per tile (multi: k_collect's lower-bin
+// counts plus the candidates that go left; else counted here over the segment), scanned
+// over the segment's tiles; a total other than the wanted rank is a failed select.
 __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv,
                                                         const double *wx, const double *wy,
                                                         const double *wz, const uint32_t *wid,
@@ -511,6 +658,8 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
     __shared__ uint32_t ncomp;
     __shared__ unsigned long long red_k[2][kSelThreads / 32];
     __shared__ uint32_t red_i[2][kSelThreads / 32];
+    __shared__ unsigned long long s_kmed;
+    __shared__ uint32_t s_idmed;
 
     const uint32_t seg = blockIdx.x;
     const uint32_t nid = lv.ids[seg];
@@ -521,14 +670,18 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
     uint32_t c = st.c, r = st.r;
     int src = lv.multi ? 0 : -1;  // -1: the candidates are the segment itself
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) {  // a failed select keeps the split's defaults
+        s_kmed = st.kmed;
+        s_idmed = st.idmed;
+    }
 
     auto get = [&](uint32_t j, unsigned long long &key, uint32_t &pos) {
         if (src < 0) {
             pos = j;
             key = ord_key(w[j]);
         } else {
-            pos = (src == 0 ? s.cpos[0] : s.cpos[1])[start + j];
-            key = (src == 0 ? s.ckey[0] : s.ckey[1])[start + j];
+            pos = (src == 0 ? s.cpos[0] : (src == 1 ? s.cpos[1] : s.cpos[2]))[start + j];
+            key = (src == 0 ? s.ckey[0] : (src == 1 ? s.ckey[1] : s.ckey[2]))[start + j];
         }
     };
 
@@ -591,7 +744,7 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
         __syncthreads();
         find_bin(h, r, out3, nb);
         const uint32_t dig = out3[0], below = out3[1], inbin = out3[2];
-        const int dst = src == 0 ? 1 : 0;
+        const int dst = src == 1 ? 2 : 1;
         for (uint32_t base = 0; base < c; base += blockDim.x) {
             uint32_t j = base + threadIdx.x;
             bool in = j < c;
@@ -606,8 +759,8 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
                 slot = __shfl_sync(kFull, slot, leader);
                 if (hit) {
                     uint32_t o = slot + __popc(m & ((1u << lane) - 1u));
-                    (dst == 0 ? s.ckey[0] : s.ckey[1])[start + o] = key;
-                    (dst == 0 ? s.cpos[0] : s.cpos[1])[start + o] = pos;
+                    (dst == 1 ? s.ckey[1] : s.ckey[2])[start + o] = key;
+                    (dst == 1 ? s.cpos[1] : s.cpos[2])[start + o] = pos;
                 }
             }
         }
@@ -638,111 +791,15 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
                 sel[seg].idmed = id;
                 sel[seg].posmed = pos;
                 no.split_val[nid] = w[pos];
+                s_kmed = key;
+                s_idmed = id;
             }
         }
-        return;
-    }
-    const uint32_t P = next_pow2(c);
-    for (uint32_t j = threadIdx.x; j < P; j += blockDim.x) {
-        if (j < c) {
-            unsigned long long key;
-            uint32_t pos;
-            get(j, key, pos);
-            skey[j] = key;
-            sval[j] = ((unsigned long long)ids[pos] << 32) | pos;
-        } else {
-            skey[j] = ~0ull;
-            sval[j] = ~0ull;
-        }
+    } else {
+        select_sorted(skey, sval, c, r, sel, seg, no, nid, w, ids, get, s_kmed, s_idmed);
     }
     __syncthreads();
-    if (P > 1) bitonic_blocks(skey, sval, P, P);
-    if (threadIdx.x == 0) {
-        unsigned long long v = sval[r];
-        uint32_t pos = (uint32_t)(v & 0xffffffffull);
-        sel[seg].kmed = skey[r];
-        sel[seg].idmed = (uint32_t)(v >> 32);
-        sel[seg].posmed = pos;
-        no.split_val[nid] = w[pos];
-    }
-}
-
-__device__ __forceinline__ bool goes_left(unsigned long long key, uint32_t id,
-                                          unsigned long long kmed, uint32_t idmed) {
-    return key < kmed || (key == kmed && id < idmed);
-}
-
-__global__ __launch_bounds__(kTileThreads) void k_part_count(Topology t, LevelArgs lv,
-                                                             const double *wx, const double *wy,
-                                                             const double *wz,
-                                                             const uint32_t *wid,
-                                                             const SegSel *sel,
-                                                             uint32_t *tile_cnt) {
-    TileRef r;
-    if (!tile_of(t, lv, r)) return;
-    const SegSel s = sel[r.seg];
-    const double *w = pick(wx, wy, wz, s.sd) + r.start;
-    const uint32_t *ids = wid + r.start;
-    constexpr int kRows = kTile / kTileThreads;
-    double v[kRows];
-    uint32_t q[kRows];
-#pragma unroll
-    for (int i = 0; i < kRows; ++i) {
-        const uint32_t k = r.lo + (uint32_t)i * kTileThreads + threadIdx.x;
-        v[i] = k < r.hi ? w[k] : 0.0;
-        q[i] = k < r.hi ? ids[k] : 0u;
-    }
-    uint32_t cnt = 0;
-#pragma unroll
-    for (int i = 0; i < kRows; ++i)
-        if (r.lo + (uint32_t)i * kTileThreads + threadIdx.x < r.hi)
-            cnt += goes_left(ord_key(v[i]), q[i], s.kmed, s.idmed) ? 1u : 0u;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
-    __shared__ uint32_t ws[kTileThreads / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t tot = 0;
-        for (int i = 0; i < kTileThreads / 32; ++i) tot += ws[i];
-        tile_cnt[(size_t)r.seg * lv.tiles + r.tile] = tot;
-    }
-}
-
-// Exclusive scan of the left counts over the tiles of each segment; checks that exactly
-// len/2 bodies go left.
-__global__ __launch_bounds__(1024) void k_tile_scan(Topology t, LevelArgs lv,
-                                                   const uint32_t *tile_cnt, uint32_t *tile_off,
-                                                   uint32_t *err) {
-    const uint32_t seg = blockIdx.x;
-    const uint32_t cnt = t.count[lv.ids[seg]];
-    const uint32_t ntiles = (cnt + kTile - 1) / kTile;
-    const uint32_t *tc = tile_cnt + (size_t)seg * lv.tiles;
-    uint32_t *to = tile_off + (size_t)seg * lv.tiles;
-    __shared__ uint32_t wsum[32];
-    __shared__ uint32_t carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint32_t base = 0; base < ntiles; base += blockDim.x) {
-        uint32_t i = base + threadIdx.x;
-        uint32_t v = i < ntiles ? tc[i] : 0u;
-        uint32_t inc = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t u = __shfl_up_sync(kFull, inc, o);
-            if (lane >= o) inc += u;
-        }
-        if (lane == 31) wsum[warp] = inc;
-        __syncthreads();
-        uint32_t wpre = 0;
-        for (int q = 0; q < warp; ++q) wpre += wsum[q];
-        if (i < ntiles) to[i] = carry + wpre + inc - v;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry += wpre + inc;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0 && carry != split_rank(lv, cnt)) atomicOr(err, kErrSelect);
+    if (lv.tiles > 1) tile_offsets(t, lv, s, st, seg, nid, start, w, ids, s_kmed, s_idmed);
 }
 
 // Stable partition: bodies keep their relative order inside each child.  With `nbmin`
@@ -894,7 +951,7 @@ constexpr int kWarpSelWarps = 8;
 __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
     Topology t, LevelArgs lv, const unsigned long long *bmin, const unsigned long long *bmax,
     const double *wx, const double *wy, const double *wz, const uint32_t *wid, SegSel *sel,
-    NodeOut no, uint32_t *err);
+    NodeOut no, uint32_t *tile_off, uint32_t *err);
 
 int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
                  Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready,
@@ -905,7 +962,7 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
     unsigned long long *bmin = s.bmin[lvl & 1], *bmax = s.bmax[lvl & 1];
     unsigned long long *nbmin = G_next ? s.bmin[(lvl + 1) & 1] : nullptr;
     unsigned long long *nbmax = G_next ? s.bmax[(lvl + 1) & 1] : nullptr;
-    int launched = 5;
+    int launched = 0;
     if (lvl == 0 && !box0_ready) {
         cudaMemsetAsync(bmin, 0xff, sizeof(unsigned long long) * 3 * G, st);
         cudaMemsetAsync(bmax, 0x00, sizeof(unsigned long long) * 3 * G, st);
@@ -916,42 +973,37 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
         cudaMemsetAsync(nbmin, 0xff, sizeof(unsigned long long) * 3 * G_next, st);
         cudaMemsetAsync(nbmax, 0x00, sizeof(unsigned long long) * 3 * G_next, st);
     }
-    if (!lv.multi && seg_max <= kWarpSelMax) {
-        k_split_select_warp<<<(G + kWarpSelWarps - 1) / kWarpSelWarps, kWarpSelWarps * 32, 0,
-                              st>>>(t, lv, bmin, bmax, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
-                                    s.sel, no, s.err);
-        --launched;
-    } else {
-        k_split<<<(G + 127) / 128, 128, 0, st>>>(t, lv, bmin, bmax, s.sel, no);
-    }
+    // tile offsets of the partition: written by the select kernels when a segment spans
+    // several tiles; a one-tile segment's scatter counts and checks by itself
+    uint32_t *tile_off = lv.tiles > 1 ? s.tile_off : nullptr;
     if (lv.multi) {
+        // split + histogram (+ bin search), candidates (+ lower-bin counts), exact median
+        // (+ tile offsets)
         cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * kHistBins * (size_t)G, st);
         cudaMemsetAsync(s.cand_cnt, 0, sizeof(uint32_t) * G, st);
         k_hist<<<G * ((lv.tiles + kHistTiles - 1) / kHistTiles), kTileThreads, 0, st>>>(
-            t, lv, w.x[cur], w.y[cur], w.z[cur], s.sel, s.hist);
-        k_find<<<G, kTileThreads, 0, st>>>(s.hist, s.sel);
+            t, lv, w.x[cur], w.y[cur], w.z[cur], bmin, bmax, s.sel, no, s.hist, s.done);
         k_collect<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], s.sel,
-                                                 s.cand_cnt, s.ckey[0], s.cpos[0]);
-        launched += 3;
-    }
-    if (lv.multi || seg_max > kWarpSelMax)
+                                                 s.cand_cnt, s.ckey[0], s.cpos[0], s.tile_cnt);
         k_select<<<G, kSelThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
                                             s.sel, s, no);
-    if (lv.tiles > 1) {
-        k_part_count<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur],
-                                                    w.id[cur], s.sel, s.tile_cnt);
-        // one block per segment, a thread per tile up to 1024
-        const uint32_t scan_threads = min(1024u, max(32u, (lv.tiles + 31u) & ~31u));
-        k_tile_scan<<<G, scan_threads, 0, st>>>(t, lv, s.tile_cnt, s.tile_off, s.err);
+        launched += 3;
+    } else if (seg_max > kWarpSelMax) {
+        k_split<<<(G + 127) / 128, 128, 0, st>>>(t, lv, bmin, bmax, s.sel, no);
+        k_select<<<G, kSelThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
+                                            s.sel, s, no);
+        launched += 2;
     } else {
-        launched -= 2;  // one tile per segment: the scatter counts and checks by itself
+        k_split_select_warp<<<(G + kWarpSelWarps - 1) / kWarpSelWarps, kWarpSelWarps * 32, 0,
+                              st>>>(t, lv, bmin, bmax, w.x[cur], w.y[cur], w.z[cur], w.id[cur],
+                                    s.sel, no, tile_off, s.err);
+        launched += 1;
     }
     k_part_scatter<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur],
                                                   w.id[cur], w.x[nxt], w.y[nxt], w.z[nxt],
-                                                  w.id[nxt], s.sel,
-                                                  lv.tiles > 1 ? s.tile_off : nullptr, nbmin,
-                                                  nbmax, s.err);
-    return launched;
+                                                  w.id[nxt], s.sel, tile_off, nbmin, nbmax,
+                                                  s.err);
+    return launched + 1;
 }
 
 // ------------------------------------------------------------------ local subtree finish
@@ -969,21 +1021,27 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
 constexpr int kLocalWarps = kLocalThreads / 32;
 constexpr int kLocalLevels = 16;
 
+// Shared memory of one block, for segments of at most kCap bodies.  The kernel is built for
+// two capacities: kLocalMax, and kLocalSmallCap for trees whose local segments are all at
+// most that big (at 1e7 and 2e7 bodies they hold ~610): ~44 KB instead of ~62 KB, so four
+// blocks share an SM instead of three.
+template <int kCap>
 struct LocalSmem {
-    double x[kLocalMax], y[kLocalMax], z[kLocalMax], m[kLocalMax];
-    uint32_t id[kLocalMax];
+    double x[kCap], y[kCap], z[kCap], m[kCap];
+    uint32_t id[kCap];
     uint32_t hist[kLocalWarps][256];
     unsigned long long ckey[kLocalWarps][32];
     uint32_t cid[kLocalWarps][32];
     // internal sub-segments of every level, appended level after level
-    uint32_t tab_id[kLocalMax];
-    uint16_t tab_st[kLocalMax], tab_cn[kLocalMax], tab_pcn[kLocalMax];
-    uint16_t perm[kLocalMax], perm2[kLocalMax];
+    uint32_t tab_id[kCap];
+    uint16_t tab_st[kCap], tab_cn[kCap], tab_pcn[kCap];
+    uint16_t perm[kCap], perm2[kCap];
     uint16_t clid[kLocalWarps][32];
     uint32_t lvl_off[kLocalLevels + 1];
     uint32_t nlvl;
     uint32_t wcnt[kLocalWarps];
 };
+constexpr int kLocalSmallCap = 640;
 
 // Candidate filter of the radix select: the top `kb` bits of the key and the top `ib` bits of
 // the id are fixed to kp / ip.
@@ -1019,11 +1077,13 @@ struct RadixState {
 // kWarpSelMax bodies): one warp per segment, no block barrier.  Lane 0 chooses the split as
 // k_split does; the warp then narrows the (key, id) candidates with 8-bit radix passes over a
 // warp-private histogram, as the subtree finish does for its larger nodes, until at most 32
-// remain, and ranks those by comparison.  Writes the segment's SegSel and node fields.
+// remain, and ranks those by comparison.  Writes the segment's SegSel and node fields, and
+// with tile_off set (segments of two tiles) the partition's tile offsets, checking that
+// exactly the wanted rank goes left.
 __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
     Topology t, LevelArgs lv, const unsigned long long *bmin, const unsigned long long *bmax,
     const double *wx, const double *wy, const double *wz, const uint32_t *wid, SegSel *sel,
-    NodeOut no, uint32_t *err) {
+    NodeOut no, uint32_t *tile_off, uint32_t *err) {
     __shared__ uint32_t hist[kWarpSelWarps][256];
     __shared__ unsigned long long ckey[kWarpSelWarps][32];
     __shared__ uint32_t cid[kWarpSelWarps][32], cpos[kWarpSelWarps][32];
@@ -1166,16 +1226,40 @@ __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
         sel[seg] = s;
         no.split_val[nid] = w[pos];
     }
+    if (!tile_off) return;  // one tile: the scatter counts and checks by itself
+    // the bodies going left in each of the segment's (at most two) tiles
+    const int ml = __ffs(wm) - 1;
+    const unsigned long long kmed = __shfl_sync(kFull, mk, ml);
+    const uint32_t idmed = __shfl_sync(kFull, mi, ml);
+    uint32_t c0 = 0, c1 = 0;
+    for (uint32_t k = lane; k < cn; k += 32) {
+        const bool L = goes_left(ord_key(w[k]), ids[k], kmed, idmed);
+        c0 += (L && k < (uint32_t)kTile) ? 1u : 0u;
+        c1 += (L && k >= (uint32_t)kTile) ? 1u : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        c0 += __shfl_xor_sync(kFull, c0, o);
+        c1 += __shfl_xor_sync(kFull, c1, o);
+    }
+    if (lane == 0) {
+        uint32_t *to = tile_off + (size_t)seg * lv.tiles;
+        to[0] = 0u;
+        if (cn > (uint32_t)kTile) to[1] = c0;
+        if (c0 + c1 != rank0) atomicOr(err, kErrSelect);
+    }
 }
 
-__device__ __forceinline__ double coord(const LocalSmem &S, uint32_t sd, uint32_t l) {
+template <class Smem>
+__device__ __forceinline__ double coord(const Smem &S, uint32_t sd, uint32_t l) {
     return sd == 0 ? S.x[l] : (sd == 1 ? S.y[l] : S.z[l]);
 }
 
 // Mixed leaf record: origin o = position of the leaf's first body, as hi + lo floats.  The
 // leaf's first position is noted in perm2 for every body of the leaf, whose offset from o
 // goes to trel with the tree-ordered bodies.
-__device__ __forceinline__ NodeF leaf_nodef(LocalSmem &S, uint32_t st, uint32_t cn,
+template <class Smem>
+__device__ __forceinline__ NodeF leaf_nodef(Smem &S, uint32_t st, uint32_t cn,
                                             uint32_t s0, const LocalOut &o) {
     const uint32_t l0 = S.perm[st];
     const double ox = S.x[l0], oy = S.y[l0], oz = S.z[l0];
@@ -1193,7 +1277,8 @@ __device__ __forceinline__ NodeF leaf_nodef(LocalSmem &S, uint32_t st, uint32_t 
 
 // Sums of a leaf's bodies (tree positions [st, st+cn) of this block): full mass (f, for the
 // FP64 records) and light mass (g, for the mixed records), each only when wanted.
-__device__ __forceinline__ void leaf_sums(const LocalSmem &S, uint32_t st, uint32_t cn,
+template <class Smem>
+__device__ __forceinline__ void leaf_sums(const Smem &S, uint32_t st, uint32_t cn,
                                           const LocalOut &o, double f[4], double g[4]) {
     f[0] = f[1] = f[2] = f[3] = 0.0;
     g[0] = g[1] = g[2] = g[3] = 0.0;
@@ -1238,7 +1323,8 @@ __device__ __forceinline__ void load_moments(const Moments &mo, uint32_t id, dou
 // members' positions in rank order of the split dimension (the left half below the median,
 // as the exact select and partition of the larger nodes give).  Writes split_dim, size,
 // split_val of the internal nodes and the subtree's final order into perm.
-__device__ __forceinline__ void small_subtree(LocalSmem &S, const Topology &t, const NodeOut &no,
+template <class Smem>
+__device__ __forceinline__ void small_subtree(Smem &S, const Topology &t, const NodeOut &no,
                                            uint32_t st, uint32_t cn, uint32_t nid,
                                            uint32_t leaf, int lane, uint32_t *err) {
     const bool valid = (uint32_t)lane < cn;
@@ -1321,13 +1407,15 @@ __device__ __forceinline__ void small_subtree(LocalSmem &S, const Topology &t, c
     __syncwarp();
 }
 
-__global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const uint32_t *roots,
+template <int kCap>
+__global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void k_local(
+    Topology t, const uint32_t *roots,
                                                          NodeOut no, const double *wx,
                                                          const double *wy, const double *wz,
                                                          const uint32_t *wid, LocalOut o,
                                                          uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    LocalSmem &S = *reinterpret_cast<LocalSmem *>(smem_raw);
+    LocalSmem<kCap> &S = *reinterpret_cast<LocalSmem<kCap> *>(smem_raw);
     const uint32_t root = roots[blockIdx.x];
     const uint32_t s0 = t.start[root], c0 = t.count[root];
     const uint32_t leaf = t.leaf;
@@ -1559,7 +1647,7 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
             }
             if (keep) {
                 const uint32_t slot = off + __popc(m & lt);
-                if (slot < (uint32_t)kLocalMax) {
+                if (slot < (uint32_t)kCap) {
                     S.tab_st[slot] = (uint16_t)cst;
                     S.tab_cn[slot] = (uint16_t)ccn;
                     S.tab_pcn[slot] = (uint16_t)pcn;
@@ -1570,9 +1658,9 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
             __syncthreads();
         }
         if (threadIdx.x == 0) {
-            if (L + 2 > (uint32_t)kLocalLevels || fill > (uint32_t)kLocalMax) {
+            if (L + 2 > (uint32_t)kLocalLevels || fill > (uint32_t)kCap) {
                 atomicOr(err, kErrSelect);
-                fill = hi;  // stop: cannot happen for segments of <= kLocalMax bodies
+                fill = hi;  // stop: cannot happen for segments of <= kCap bodies
             }
             S.lvl_off[L + 2] = fill;
             if (fill > hi) S.nlvl = L + 2;
@@ -1669,15 +1757,25 @@ __global__ __launch_bounds__(kLocalThreads, 3) void k_local(Topology t, const ui
     }
 }
 
-void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
-                  const NodeOut &no, const Work &w, int cur, const LocalOut &out, uint32_t *err,
-                  cudaStream_t st) {
+template <int kCap>
+static void launch_local_cap(const Topology &t, const uint32_t *roots, uint32_t n_roots,
+                             const NodeOut &no, const Work &w, int cur, const LocalOut &out,
+                             uint32_t *err, cudaStream_t st) {
     // set on every launch: the attribute belongs to the current device's context, and a
     // process may hold contexts on several devices
-    const size_t smem = sizeof(LocalSmem);
-    cudaFuncSetAttribute(k_local, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_local<<<n_roots, kLocalThreads, smem, st>>>(t, roots, no, w.x[cur], w.y[cur], w.z[cur],
-                                                  w.id[cur], out, err);
+    const size_t smem = sizeof(LocalSmem<kCap>);
+    cudaFuncSetAttribute(k_local<kCap>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_local<kCap><<<n_roots, kLocalThreads, smem, st>>>(t, roots, no, w.x[cur], w.y[cur],
+                                                        w.z[cur], w.id[cur], out, err);
+}
+
+void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
+                  uint32_t max_count, const NodeOut &no, const Work &w, int cur,
+                  const LocalOut &out, uint32_t *err, cudaStream_t st) {
+    if (max_count <= (uint32_t)kLocalSmallCap)
+        launch_local_cap<kLocalSmallCap>(t, roots, n_roots, no, w, cur, out, err, st);
+    else
+        launch_local_cap<kLocalMax>(t, roots, n_roots, no, w, cur, out, err, st);
 }
 
 // ------------------------------------------------------------------ moments above the local roots

@@ -505,6 +505,93 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+constexpr uint32_t kNoBody = 0xffffffffu;
+
+// 1/sqrt(x) from the FP32 hardware estimate and one FP64 Newton step (relative error about
+// 1.5 * (2^-22.9)^2, ~3e-14): the mixed path's heavy-body terms, which the FP32 pair sums
+// around them bound far more loosely.  Outside [1e-30, 1e30] by square root and division.
+__device__ __forceinline__ double inv_dist1(double x) {
+    if (!(x >= 1e-30 && x <= 1e30)) return __ddiv_rn(1.0, __dsqrt_rn(x));
+    float f;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"((float)x));
+    const double y = (double)f;
+    return y * fma(-0.5 * x * y, y, 1.5);
+}
+
+// The end of a group's walk for the lane's two sinks (body o0 / o1 at tree positions s0 / s1,
+// kNoBody when the lane has none): the heavy bodies in FP64, both ways of every (sink,
+// heavy) pair -- the heavy body's pull on the sink (the pair kernel of array_particle.rs:67-76
+// with 1/|d| from inv_dist1 in place of the square root and division), and the sink's pull on
+// the heavy body, whose sum over all bodies is the heavy body's own direct-sum acceleration
+// (its grouped-walk value, a residual of cancelling FP32 terms, is replaced by
+// k_heavy_finish) -- the warp's share of those sums into hred, and the accelerations (and
+// potentials) out.
+template <bool kPot>
+__device__ __noinline__ void heavy_tail(uint32_t o0, uint32_t o1, uint32_t s0, uint32_t s1,
+                                        double ax0, double ay0, double az0, double ph0,
+                                        double ax1, double ay1, double az1, double ph1,
+                                        const float4 *__restrict__ thi,
+                                        const float4 *__restrict__ tlo,
+                                        const double *__restrict__ bx,
+                                        const double *__restrict__ by,
+                                        const double *__restrict__ bz,
+                                        const uint32_t *__restrict__ heavy_ids,
+                                        const Heavy *heavy, int n_heavy, double *__restrict__ acc,
+                                        double *__restrict__ phi, double (*hred)[4], int lane) {
+    const uint32_t o[2] = {o0, o1}, sp[2] = {s0, s1};
+    double ax[2] = {ax0, ax1}, ay[2] = {ay0, ay1}, az[2] = {az0, az1}, ph[2] = {ph0, ph1};
+    double px[2], py[2], pz[2], ms[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        px[u] = py[u] = pz[u] = ms[u] = 0.0;
+        if (o[u] != kNoBody && n_heavy > 0) {
+            px[u] = bx[o[u]];
+            py[u] = by[o[u]];
+            pz[u] = bz[o[u]];
+            ms[u] = body_mass(thi[sp[u]], tlo[sp[u]], o[u], heavy_ids, heavy, n_heavy);
+        }
+    }
+    for (int hh = 0; hh < n_heavy; ++hh) {  // warp-uniform
+        const Heavy q = heavy[hh];
+        double rx = 0.0, ry = 0.0, rz = 0.0, rp = 0.0;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            if (o[u] == kNoBody || heavy_ids[hh] == o[u]) continue;
+            const double dx = px[u] - q.x, dy = py[u] - q.y, dz = pz[u] - q.z;
+            const double ri = inv_dist1(fma(dx, dx, fma(dy, dy, dz * dz)));
+            const double ri3 = ri * ri * ri;
+            const double magi = -q.m * ri3;
+            ax[u] = fma(magi, dx, ax[u]);
+            ay[u] = fma(magi, dy, ay[u]);
+            az[u] = fma(magi, dz, az[u]);
+            if (kPot) ph[u] -= q.m * ri;
+            const double mr = ms[u] * ri3;
+            rx = fma(mr, dx, rx);
+            ry = fma(mr, dy, ry);
+            rz = fma(mr, dz, rz);
+            if (kPot) rp -= ms[u] * ri;
+        }
+        rx = warp_sum(rx);
+        ry = warp_sum(ry);
+        rz = warp_sum(rz);
+        if (kPot) rp = warp_sum(rp);
+        if (lane == 0) {
+            hred[hh][0] = rx;
+            hred[hh][1] = ry;
+            hred[hh][2] = rz;
+            hred[hh][3] = rp;
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        if (o[u] == kNoBody) continue;
+        acc[3 * (size_t)o[u]] = ax[u];
+        acc[3 * (size_t)o[u] + 1] = ay[u];
+        acc[3 * (size_t)o[u] + 2] = az[u];
+        if (kPot) phi[o[u]] = ph[u];
+    }
+}
+
 // One warp's group: the walk, the group's own leaves, the heavy bodies' FP64 terms on the
 // group's sinks, and the group's share (hred: [heavy][x, y, z, potential]) of the heavy
 // bodies' own direct sums.
@@ -560,67 +647,18 @@ __device__ __forceinline__ void walk_group_warp(
         kahan(sum[u][2], comp[u][2], pz);
         if (kPot) kahan(sum[u][3], comp[u][3], -pp);
     }
-    double ax[2], ay[2], az[2], ph[2], px[2], py[2], pz[2], ms[2];
-    uint32_t o[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        o[u] = G.valid[u] ? tid[G.s[u]] : 0u;
-        ax[u] = (double)sum[u][0] - (double)comp[u][0];
-        ay[u] = (double)sum[u][1] - (double)comp[u][1];
-        az[u] = (double)sum[u][2] - (double)comp[u][2];
-        ph[u] = (double)sum[u][3] - (double)comp[u][3];
-        px[u] = py[u] = pz[u] = ms[u] = 0.0;
-        if (G.valid[u] && n_heavy > 0) {
-            px[u] = b.x[o[u]];
-            py[u] = b.y[o[u]];
-            pz[u] = b.z[o[u]];
-            ms[u] = body_mass(thi[G.s[u]], tlo[G.s[u]], o[u], heavy_ids, heavy, n_heavy);
-        }
-    }
-    // Heavy bodies in FP64, both ways of every (sink, heavy) pair: the heavy body's pull on
-    // the sink (the pair kernel of array_particle.rs:67-76 with 1/|d| from rsqrt64, a few ulp,
-    // in place of the square root and division), and the sink's pull on the heavy body, whose
-    // sum over all bodies is the heavy body's exact direct-sum acceleration (its grouped-walk
-    // value, a residual of FP32 terms that cancel, is replaced by k_heavy_finish).
-    for (int hh = 0; hh < n_heavy; ++hh) {  // warp-uniform
-        const Heavy q = heavy[hh];
-        double rx = 0.0, ry = 0.0, rz = 0.0, rp = 0.0;
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            if (!G.valid[u] || heavy_ids[hh] == o[u]) continue;
-            const double dx = px[u] - q.x, dy = py[u] - q.y, dz = pz[u] - q.z;
-            const double ri = inv_dist(fma(dx, dx, fma(dy, dy, dz * dz)));
-            const double ri3 = ri * ri * ri;
-            const double magi = -q.m * ri3;
-            ax[u] = fma(magi, dx, ax[u]);
-            ay[u] = fma(magi, dy, ay[u]);
-            az[u] = fma(magi, dz, az[u]);
-            if (kPot) ph[u] -= q.m * ri;
-            const double mr = ms[u] * ri3;
-            rx = fma(mr, dx, rx);
-            ry = fma(mr, dy, ry);
-            rz = fma(mr, dz, rz);
-            if (kPot) rp -= ms[u] * ri;
-        }
-        rx = warp_sum(rx);
-        ry = warp_sum(ry);
-        rz = warp_sum(rz);
-        if (kPot) rp = warp_sum(rp);
-        if (lane == 0) {
-            hred[hh][0] = rx;
-            hred[hh][1] = ry;
-            hred[hh][2] = rz;
-            hred[hh][3] = rp;
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-        if (!G.valid[u]) continue;
-        acc[3 * (size_t)o[u]] = ax[u];
-        acc[3 * (size_t)o[u] + 1] = ay[u];
-        acc[3 * (size_t)o[u] + 2] = az[u];
-        if (kPot) phi[o[u]] = ph[u];
-    }
+    // the heavy-body terms and the result, in a separate (not inlined) function so that the
+    // walk's hot loops above are allocated registers without them
+    heavy_tail<kPot>(G.valid[0] ? tid[G.s[0]] : kNoBody, G.valid[1] ? tid[G.s[1]] : kNoBody,
+                     G.s[0], G.s[1], (double)sum[0][0] - (double)comp[0][0],
+                     (double)sum[0][1] - (double)comp[0][1],
+                     (double)sum[0][2] - (double)comp[0][2],
+                     (double)sum[0][3] - (double)comp[0][3],
+                     (double)sum[1][0] - (double)comp[1][0],
+                     (double)sum[1][1] - (double)comp[1][1],
+                     (double)sum[1][2] - (double)comp[1][2],
+                     (double)sum[1][3] - (double)comp[1][3], thi, tlo, b.x, b.y, b.z,
+                     heavy_ids, heavy, n_heavy, acc, phi, hred, lane);
     if (kCount && lane == 0) {
         const unsigned long long nv = G.g1 - G.g0;
         // the own leaves hold every body of the group (each reached once)

@@ -157,9 +157,10 @@ struct Scratch {
     SegSel *sel;
     uint32_t *hist;                   // [G*kHistBins]
     uint32_t *cand_cnt;               // [G]
-    unsigned long long *ckey[2];      // [n] candidate keys
-    uint32_t *cpos[2];                // [n] candidate positions
+    unsigned long long *ckey[3];      // [n] candidate keys: collected (0), refined (1, 2)
+    uint32_t *cpos[3];                // [n] candidate positions
     uint32_t *tile_cnt, *tile_off;    // [G*tiles]
+    uint32_t *done;                   // [G] finished histogram blocks per segment (zeroed)
     uint32_t *err;
 };
 
@@ -257,9 +258,10 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
                  uint32_t seg_max = 0xffffffffu);
 // Subtree finish of every local root: split decisions, tree order, and the moments and
 // walk records of all nodes below the local roots.
+// max_count: the largest local root's body count (the shared-memory layout is chosen by it).
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
-                  const NodeOut &no, const Work &w, int cur, const LocalOut &out, uint32_t *err,
-                  cudaStream_t st);
+                  uint32_t max_count, const NodeOut &no, const Work &w, int cur,
+                  const LocalOut &out, uint32_t *err, cudaStream_t st);
 // Moments and records of the nodes above the local roots (one thread per local root climbs).
 void launch_moments_top(const Topology &t, const uint32_t *roots, uint32_t n_roots,
                         const NodeOut &no, const LocalOut &out, cudaStream_t st);
