@@ -80,11 +80,11 @@ int launch_adjoint_step(const AdjArgs &a, cudaStream_t st) {
     cudaMemsetAsync(a.U, 0, sizeof(double) * 3 * (size_t)a.n, st);
     cudaMemsetAsync(a.G, 0, sizeof(double) * 3 * (size_t)a.topo.n_nodes, st);
     cudaMemsetAsync(a.yheavy, 0, sizeof(double) * 3 * kMaxHeavy, st);
-    launch_adj_group(a, st);
+    launch_adj_group(a, st);  // the walk and, with heavy bodies, their source sums
     k_adj_combine<<<(a.topo.n_leaves + 127) / 128, 128, 0, st>>>(
         a.topo, a.recf, a.trel, a.tid, a.ysink, a.U, a.G, a.heavy, a.n_heavy, a.yheavy, a.y);
     k_adj_update<<<grid, 256, 0, st>>>(a.lx, a.lv, a.mu, a.y, n3, a.dt);
-    return 4;
+    return a.n_heavy > 0 ? 5 : 4;
 }
 
 }  // namespace kd

@@ -224,7 +224,8 @@ struct kd_ctx {
     unsigned long long *d_counts = nullptr;
     uint32_t *d_heavy = nullptr, *d_nheavy = nullptr;
     double *d_total = nullptr;
-    double *d_hpart = nullptr;  // per-block partial direct sums of the heavy bodies
+    double *d_hpart = nullptr;   // per-group partial direct sums of the heavy bodies
+    uint32_t *d_hcount = nullptr;  // finished blocks of k_heavy_finish per heavy body
     double *gen_scratch = nullptr;
     double *phi = nullptr;  // potentials, allocated by the first kd_energy
     int n_heavy = 0;
@@ -401,7 +402,9 @@ int setup(kd_ctx *c) {
     KD_CHECK(c, c->alloc(&c->d_heavy, kMaxHeavy));
     KD_CHECK(c, c->alloc(&c->d_nheavy, 1));
     KD_CHECK(c, c->alloc(&c->d_total, 1 + 304));  // total mass + per-block partials
-    KD_CHECK(c, c->alloc(&c->d_hpart, (size_t)walk_group_blocks(c->n_groups) * kMaxHeavy * 4));
+    KD_CHECK(c, c->alloc(&c->d_hpart, heavy_partial_doubles(c->n_groups)));
+    KD_CHECK(c, c->alloc(&c->d_hcount, kMaxHeavy));
+    KD_CHECK(c, cudaMemset(c->d_hcount, 0, kMaxHeavy * sizeof(uint32_t)));
     KD_CHECK(c, c->alloc(&c->gen_scratch, 6 * 256));
     KD_CHECK(c, cudaMemset(c->dev_err, 0, sizeof(uint32_t)));
     // the build's ping-pong buffers start as valid bodies (id 0 at the origin), so a slot a
@@ -485,7 +488,8 @@ void enqueue_walk(kd_ctx *c) {
         c->launches += launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart,
                                          c->d_gsplit, c->n_groups, c->walk_stack(),
                                          c->prm.theta, c->bodies, c->d_heavy, c->n_heavy,
-                                         c->acc, c->d_hpart, c->dev_err, cnt, c->st);
+                                         c->acc, c->d_hpart, c->d_hcount, c->dev_err, cnt,
+                                         c->st);
     } else {
         c->launches += 1;
         launch_walk_fp64(c->recd, c->recp, c->thi, c->tlo, c->tpos, c->tid, (uint32_t)c->n,
@@ -1111,7 +1115,8 @@ int kd_energy(kd_ctx *c, double out[2]) {
     enqueue_build(c, false, true);
     launch_walk_group(c->recf, c->thi, c->tlo, c->trel, c->tid, c->d_gstart, c->d_gsplit,
                       c->n_groups, c->walk_stack(), c->prm.theta, c->bodies, c->d_heavy,
-                      c->n_heavy, c->acc, c->d_hpart, c->dev_err, nullptr, c->st, c->phi);
+                      c->n_heavy, c->acc, c->d_hpart, c->d_hcount, c->dev_err, nullptr, c->st,
+                      c->phi);
     launch_energy_partial(c->bodies, c->phi, (uint32_t)c->n, c->gen_scratch, kBlocks, c->st);
     double part[2 * kBlocks];
     KD_CHECK(c, cudaMemcpyAsync(part, c->gen_scratch, sizeof part, cudaMemcpyDeviceToHost,
@@ -1377,6 +1382,8 @@ int kd_backward(kd_tape *tape, const double *dL_dx, const double *dL_dv, double 
     a.y = c->ay;
     a.ysink = c->ysink;
     a.yheavy = c->yheavy;
+    a.hpart = c->d_hpart;
+    a.hcount = c->d_hcount;
     a.U = c->aU;
     a.G = c->aG;
     a.err = c->dev_err;

@@ -524,8 +524,8 @@ __device__ __forceinline__ double inv_dist1(double x) {
 // with 1/|d| from inv_dist1 in place of the square root and division), and the sink's pull on
 // the heavy body, whose sum over all bodies is the heavy body's own direct-sum acceleration
 // (its grouped-walk value, a residual of cancelling FP32 terms, is replaced by
-// k_heavy_finish) -- the warp's share of those sums into hred, and the accelerations (and
-// potentials) out.
+// k_heavy_finish) -- the warp's share of those sums into its own slot of hpart, and the
+// accelerations (and potentials) out.
 template <bool kPot>
 __device__ __noinline__ void heavy_tail(uint32_t o0, uint32_t o1, uint32_t s0, uint32_t s1,
                                         double ax0, double ay0, double az0, double ph0,
@@ -537,7 +537,8 @@ __device__ __noinline__ void heavy_tail(uint32_t o0, uint32_t o1, uint32_t s0, u
                                         const double *__restrict__ bz,
                                         const uint32_t *__restrict__ heavy_ids,
                                         const Heavy *heavy, int n_heavy, double *__restrict__ acc,
-                                        double *__restrict__ phi, double (*hred)[4], int lane) {
+                                        double *__restrict__ phi, double *__restrict__ hpart,
+                                        uint32_t g, uint32_t n_groups, int lane) {
     const uint32_t o[2] = {o0, o1}, sp[2] = {s0, s1};
     double ax[2] = {ax0, ax1}, ay[2] = {ay0, ay1}, az[2] = {az0, az1}, ph[2] = {ph0, ph1};
     double px[2], py[2], pz[2], ms[2];
@@ -576,10 +577,11 @@ __device__ __noinline__ void heavy_tail(uint32_t o0, uint32_t o1, uint32_t s0, u
         rz = warp_sum(rz);
         if (kPot) rp = warp_sum(rp);
         if (lane == 0) {
-            hred[hh][0] = rx;
-            hred[hh][1] = ry;
-            hred[hh][2] = rz;
-            hred[hh][3] = rp;
+            double *slot = hpart + ((size_t)hh * n_groups + g) * 4;
+            slot[0] = rx;
+            slot[1] = ry;
+            slot[2] = rz;
+            slot[3] = rp;
         }
     }
 #pragma unroll
@@ -593,8 +595,8 @@ __device__ __noinline__ void heavy_tail(uint32_t o0, uint32_t o1, uint32_t s0, u
 }
 
 // One warp's group: the walk, the group's own leaves, the heavy bodies' FP64 terms on the
-// group's sinks, and the group's share (hred: [heavy][x, y, z, potential]) of the heavy
-// bodies' own direct sums.
+// group's sinks, and the group's share (hpart[heavy][group][x, y, z, potential]) of the
+// heavy bodies' own direct sums.
 template <bool kCount, bool kPot>
 __device__ __forceinline__ void walk_group_warp(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
@@ -603,7 +605,8 @@ __device__ __forceinline__ void walk_group_warp(
     const uint32_t *__restrict__ gsplit, uint32_t g, uint32_t stk_cap, float theta2,
     const Bodies &b, const uint32_t *__restrict__ heavy_ids, const Heavy *heavy, int n_heavy,
     double *__restrict__ acc, double *__restrict__ phi, uint32_t *err,
-    unsigned long long *counts, float4 *smem, double (*hred)[4], int lane, int warp) {
+    unsigned long long *counts, float4 *smem, double *__restrict__ hpart, uint32_t n_groups,
+    int lane, int warp) {
     const WarpMem W = warp_mem(smem, warp, stk_cap, false);
     const Group G = make_group(thi, tlo, gstart[g], gstart[g + 1], gsplit[g], lane);
 
@@ -658,7 +661,7 @@ __device__ __forceinline__ void walk_group_warp(
                      (double)sum[1][1] - (double)comp[1][1],
                      (double)sum[1][2] - (double)comp[1][2],
                      (double)sum[1][3] - (double)comp[1][3], thi, tlo, b.x, b.y, b.z,
-                     heavy_ids, heavy, n_heavy, acc, phi, hred, lane);
+                     heavy_ids, heavy, n_heavy, acc, phi, hpart, g, n_groups, lane);
     if (kCount && lane == 0) {
         const unsigned long long nv = G.g1 - G.g0;
         // the own leaves hold every body of the group (each reached once)
@@ -681,7 +684,6 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
     unsigned long long *counts) {
     extern __shared__ float4 smem[];
     __shared__ Heavy heavy[kMaxHeavy];
-    __shared__ double hred[kGroupWarps][kMaxHeavy][4];
     if (threadIdx.x < n_heavy) {
         const uint32_t h = heavy_ids[threadIdx.x];
         heavy[threadIdx.x] = Heavy{b.x[h], b.y[h], b.z[h], b.m[h]};
@@ -689,56 +691,36 @@ __global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t g = blockIdx.x * kGroupWarps + warp;
-    if (g < n_groups)  // warp-uniform; every warp reaches the block barrier at the end
-        walk_group_warp<kCount, kPot>(rec, thi, tlo, trel, tid, gstart, gsplit, g, stk_cap,
-                                      theta2, b, heavy_ids, heavy, n_heavy, acc, phi, err,
-                                      counts, smem, hred[warp], lane, warp);
-    else if (lane == 0)
-        for (int hh = 0; hh < n_heavy; ++hh)
-            hred[warp][hh][0] = hred[warp][hh][1] = hred[warp][hh][2] = hred[warp][hh][3] = 0.0;
-    if (n_heavy == 0) return;  // block-uniform
-    // the block's share of the heavy bodies' direct sums, warps in order (deterministic)
-    __syncthreads();
-    if (threadIdx.x < 4u * (uint32_t)n_heavy) {
-        const int hh = threadIdx.x >> 2, c = threadIdx.x & 3;
-        double v = 0.0;
-        for (int w = 0; w < kGroupWarps; ++w) v += hred[w][hh][c];
-        hpart[((size_t)blockIdx.x * kMaxHeavy + hh) * 4 + c] = v;
-    }
+    // no block barrier follows: a warp whose group is done exits (a trailing barrier, which
+    // held finished warps until the block's slowest, cost 7% of the walk)
+    if (g >= n_groups) return;
+    walk_group_warp<kCount, kPot>(rec, thi, tlo, trel, tid, gstart, gsplit, g, stk_cap, theta2,
+                                  b, heavy_ids, heavy, n_heavy, acc, phi, err, counts, smem,
+                                  hpart, n_groups, lane, warp);
 }
 
 // The heavy bodies' accelerations (and potentials) as FP64 direct sums over every other
-// body: the blocks' partial sums of k_walk_group added in a fixed order (each thread a fixed
-// strided subset, four blocks' partials in flight per round; then the warps' butterflies and
-// the warps in order), so the result is deterministic.  One block per heavy body; overwrites
-// what the grouped walk wrote for it.
-constexpr int kFinishThreads = 1024;
-
+// body, from the groups' partial sums (hpart[heavy][group][4]): block q of heavy body h adds
+// groups [q * chunk, (q + 1) * chunk) in a fixed order (strided per thread, then the warps'
+// butterflies, then the warps in order) into hpart's block area; the last block of h to
+// finish adds the kFinishBlocks block sums in order.  Deterministic for a given n; overwrites
+// what the grouped walk wrote for the heavy body.  `count` (kMaxHeavy words, zero between
+// launches) counts the finished blocks of each heavy body.
 __global__ __launch_bounds__(kFinishThreads) void k_heavy_finish(
-    const double *__restrict__ hpart, uint32_t n_blocks, const uint32_t *__restrict__ heavy_ids,
-    double *__restrict__ acc, double *__restrict__ phi) {
+    double *__restrict__ hpart, uint32_t n_groups, const uint32_t *__restrict__ heavy_ids,
+    uint32_t *count, double *__restrict__ acc, double *__restrict__ phi,
+    double *__restrict__ out3) {
     __shared__ double red[4][kFinishThreads / 32];
-    const int hh = blockIdx.x;
+    __shared__ bool last;
+    const int hh = blockIdx.y, q = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double *src = hpart + (size_t)hh * n_groups * 4;
+    double *blk = hpart + (size_t)kMaxHeavy * n_groups * 4 + ((size_t)hh * kFinishBlocks) * 4;
+    const uint32_t chunk = (n_groups + kFinishBlocks - 1) / kFinishBlocks;
+    const uint32_t g0 = min(n_groups, (uint32_t)q * chunk), g1 = min(n_groups, g0 + chunk);
     double v[4] = {0.0, 0.0, 0.0, 0.0};
-    uint32_t q = threadIdx.x;
-    for (; q + 3u * kFinishThreads < n_blocks; q += 4u * kFinishThreads) {
-        dbl4 t[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-            t[r] = *reinterpret_cast<const dbl4 *>(
-                hpart + ((size_t)(q + r * kFinishThreads) * kMaxHeavy + hh) * 4);
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            v[0] += t[r].x;
-            v[1] += t[r].y;
-            v[2] += t[r].z;
-            v[3] += t[r].w;
-        }
-    }
-    for (; q < n_blocks; q += kFinishThreads) {
-        const dbl4 t =
-            *reinterpret_cast<const dbl4 *>(hpart + ((size_t)q * kMaxHeavy + hh) * 4);
+    for (uint32_t g = g0 + threadIdx.x; g < g1; g += kFinishThreads) {
+        const dbl4 t = *reinterpret_cast<const dbl4 *>(src + (size_t)g * 4);
         v[0] += t.x;
         v[1] += t.y;
         v[2] += t.z;
@@ -751,14 +733,28 @@ __global__ __launch_bounds__(kFinishThreads) void k_heavy_finish(
     }
     __syncthreads();
     if (threadIdx.x < 4) {
-        const int c = threadIdx.x;
         double t = 0.0;
-        for (int w = 0; w < kFinishThreads / 32; ++w) t += red[c][w];
+        for (int w = 0; w < kFinishThreads / 32; ++w) t += red[threadIdx.x][w];
+        blk[(size_t)q * 4 + threadIdx.x] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&count[hh], 1u) == kFinishBlocks - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int k = 0; k < kFinishBlocks; ++k) t += __ldcg(&blk[(size_t)k * 4 + threadIdx.x]);
         const size_t o = heavy_ids[hh];
-        if (c < 3)
-            acc[3 * o + c] = t;
-        else if (phi)
+        if (out3) {  // the adjoint's heavy source sums
+            if (threadIdx.x < 3) out3[3 * hh + threadIdx.x] = t;
+        } else if (threadIdx.x < 3) {
+            acc[3 * o + threadIdx.x] = t;
+        } else if (phi) {
             phi[o] = t;
+        }
+        if (threadIdx.x == 0) count[hh] = 0u;
     }
 }
 
@@ -773,11 +769,10 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
     const uint32_t *__restrict__ gsplit, uint32_t n_groups, uint32_t stk_cap, float theta2,
     Bodies b, const uint32_t *__restrict__ heavy_ids, int n_heavy,
     const double *__restrict__ mu, double *__restrict__ ysink, double *__restrict__ U,
-    double *__restrict__ Gn, double *__restrict__ yheavy, uint32_t *err) {
+    double *__restrict__ Gn, double *__restrict__ hpart, uint32_t *err) {
     extern __shared__ float4 smem[];
     __shared__ Heavy heavy[kMaxHeavy];
     __shared__ double hmu[kMaxHeavy][3];
-    __shared__ double hred[kGroupWarps][kMaxHeavy][3];
     if (threadIdx.x < n_heavy) {
         const uint32_t h = heavy_ids[threadIdx.x];
         heavy[threadIdx.x] = Heavy{b.x[h], b.y[h], b.z[h], b.m[h]};
@@ -791,7 +786,8 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
     double hx[kMaxHeavy][3];
 #pragma unroll
     for (int h = 0; h < kMaxHeavy; ++h) hx[h][0] = hx[h][1] = hx[h][2] = 0.0;
-    if (g < n_groups) {  // warp-uniform; the block barrier below is reached by every warp
+    if (g >= n_groups) return;  // warp-uniform; no block barrier follows
+    {
         const WarpMem W = warp_mem(smem, warp, stk_cap, true);
         const Group G = make_group(thi, tlo, gstart[g], gstart[g + 1], gsplit[g], lane);
         // sinks without a body sit far away with mu = 0: every term they make is zero.  A
@@ -947,23 +943,19 @@ __global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
             ysink[3 * (size_t)s + 2] = ysz;
         }
     }
-    if (n_heavy > 0) {
+    // the group's share of the heavy bodies' source sums, into its own slot of hpart (added up
+    // by k_heavy_finish: no block barrier, so a finished warp exits)
 #pragma unroll
-        for (int h = 0; h < kMaxHeavy; ++h)
+    for (int h = 0; h < kMaxHeavy; ++h) {
+        if (h >= n_heavy) break;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                double val = hx[h][d];
+        for (int d = 0; d < 3; ++d) {
+            double val = hx[h][d];
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) val += __shfl_xor_sync(kFull, val, off);
-                if (lane == 0) hred[warp][h][d] = val;
-            }
-        __syncthreads();
-        if (threadIdx.x < (unsigned)(3 * n_heavy)) {
-            const int h = threadIdx.x / 3, d = threadIdx.x % 3;
-            double val = 0.0;
-            for (int w = 0; w < kGroupWarps; ++w) val += hred[w][h][d];
-            atomicAdd(&yheavy[3 * h + d], val);
+            for (int off = 16; off > 0; off >>= 1) val += __shfl_xor_sync(kFull, val, off);
+            if (lane == 0) hpart[((size_t)h * n_groups + g) * 4 + d] = val;
         }
+        if (lane == 0) hpart[((size_t)h * n_groups + g) * 4 + 3] = 0.0;
     }
 }
 
@@ -971,8 +963,8 @@ int launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
                       const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
                       const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta,
                       const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
-                      double *hpart, uint32_t *err, unsigned long long *counts, cudaStream_t st,
-                      double *phi) {
+                      double *hpart, uint32_t *hcount, uint32_t *err,
+                      unsigned long long *counts, cudaStream_t st, double *phi) {
     const uint32_t threads = kGroupWarps * 32;
     const uint32_t blocks = walk_group_blocks(n_groups);
     const size_t smem = (size_t)kGroupWarps * group_warp_bytes(stk_cap);
@@ -984,7 +976,8 @@ int launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
                                      theta2, b, heavy_ids, n_heavy, acc, phi, hpart, err,
                                      counts);
     if (n_heavy <= 0) return 1;
-    k_heavy_finish<<<n_heavy, kFinishThreads, 0, st>>>(hpart, blocks, heavy_ids, acc, phi);
+    k_heavy_finish<<<dim3(kFinishBlocks, n_heavy), kFinishThreads, 0, st>>>(
+        hpart, n_groups, heavy_ids, hcount, acc, phi, nullptr);
     return 2;
 }
 
@@ -997,7 +990,10 @@ void launch_adj_group(const AdjArgs &a, cudaStream_t st) {
     k_adj_group<<<blocks, threads, smem, st>>>(
         a.recf, a.thi, a.tlo, a.trel, a.tid, a.gstart, a.gsplit, a.n_groups, a.stk_cap,
         (float)(a.theta * a.theta), a.bodies, a.heavy, a.n_heavy, a.mu, a.ysink, a.U, a.G,
-        a.yheavy, a.err);
+        a.hpart, a.err);
+    if (a.n_heavy > 0)
+        k_heavy_finish<<<dim3(kFinishBlocks, a.n_heavy), kFinishThreads, 0, st>>>(
+            a.hpart, a.n_groups, a.heavy, a.hcount, nullptr, nullptr, a.yheavy);
 }
 
 }  // namespace kd

@@ -294,15 +294,20 @@ __host__ __device__ inline uint32_t walk_group_blocks(uint32_t n_groups) {
     return (n_groups + kGroupWarps - 1) / kGroupWarps;
 }
 // The walk, then (n_heavy > 0) the heavy bodies' own accelerations as FP64 direct sums over
-// all bodies: the walk leaves per-block partial sums in hpart (walk_group_blocks(n_groups) *
-// kMaxHeavy * 4 doubles) and k_heavy_finish adds them in block order.  With phi set, also the
-// potentials.  Returns the number of kernels launched.
+// all bodies: every group's warp leaves its partial sums in hpart and k_heavy_finish adds
+// them in a fixed order (hpart: heavy_partial_doubles(n_groups); hcount: kMaxHeavy zeroed
+// words).  With phi set, also the potentials.  Returns the number of kernels launched.
+constexpr int kFinishBlocks = 64;
+constexpr int kFinishThreads = 256;
+__host__ __device__ inline size_t heavy_partial_doubles(uint32_t n_groups) {
+    return (size_t)kMaxHeavy * 4 * ((size_t)n_groups + kFinishBlocks);
+}
 int launch_walk_group(const NodeF *rec, const float4 *thi, const float4 *tlo,
                       const float4 *trel, const uint32_t *tid, const uint32_t *gstart,
                       const uint32_t *gsplit, uint32_t n_groups, uint32_t stk_cap, double theta,
                       const Bodies &b, const uint32_t *heavy_ids, int n_heavy, double *acc,
-                      double *hpart, uint32_t *err, unsigned long long *counts, cudaStream_t st,
-                      double *phi = nullptr);
+                      double *hpart, uint32_t *hcount, uint32_t *err,
+                      unsigned long long *counts, cudaStream_t st, double *phi = nullptr);
 
 // per-block sums (kinetic, potential) of 0.5 m v^2 and 0.5 m phi into part[2*blocks]
 void launch_energy_partial(const Bodies &b, const double *phi, uint32_t n, double *part,
@@ -346,7 +351,9 @@ struct AdjArgs {
     double *lx, *lv;        // adjoints of x and v, original order, 3n
     double *mu, *y;         // 3n scratch
     double *ysink;          // 3n, tree order
-    double *yheavy;         // 3 * kMaxHeavy
+    double *yheavy;         // 3 * kMaxHeavy: the heavy bodies' source sums
+    double *hpart;          // heavy_partial_doubles(n_groups): per-group parts of yheavy
+    uint32_t *hcount;       // kMaxHeavy zeroed words (k_heavy_finish)
     double *U;              // 3n, tree order: pair-source sums
     double *G;              // 3 * n_nodes: node-source sums
     uint32_t *err;
