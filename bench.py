@@ -570,12 +570,14 @@ def run_ours(a, ws, rank, local):
     print(json.dumps(line))
 
 
-# DRAM bytes per body of one launch, from one-pass ncu captures (see profiles/): the 10M-body
-# grouped walk (4.31 GB read + 0.475 GB written), and the build's kernels at 4M bodies
-# summed over the step's launch list, both scaled by the number of bodies
+# DRAM bytes per body of one launch, from one-pass ncu captures of the 10M-body step (the
+# launch list in profiles/): the grouped walk (4.79 GB), and the build's kernels summed over
+# the step (11.89 GB, every kernel starting with cold caches), both scaled by the number of
+# bodies
 WALK_TRAFFIC_PER_BODY = 479.0
-BUILD_TRAFFIC_PER_BODY = None
-BUILD_TRAFFIC_NOTE = "not captured"
+BUILD_TRAFFIC_PER_BODY = 1189.0
+BUILD_TRAFFIC_NOTE = ("ncu dram read + write of the build's kernels in one 10M-ring step "
+                      "(1,189 B/body, cold caches per kernel), scaled by N")
 
 
 def tree_levels(n: int, leaf: int) -> int:
