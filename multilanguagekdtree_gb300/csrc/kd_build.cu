@@ -802,66 +802,98 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
     if (lv.tiles > 1) tile_offsets(t, lv, s, st, seg, nid, start, w, ids, s_kmed, s_idmed);
 }
 
+// Asynchronous global -> shared copies (cp.async) of the partition's tile.  The wait is the
+// hardware's group count, not a spin loop.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// The partition's tile in shared memory: positions and ids as read, and the tile's bodies in
+// output order (left child first, then right) as indices into them.
+struct ScatTile {
+    double x[kTile], y[kTile], z[kTile];
+    uint32_t id[kTile];
+    uint16_t order[kTile];
+};
+
 // Stable partition: bodies keep their relative order inside each child.  With `nbmin`
 // set, the bounding boxes of the two children (segments 2*seg and 2*seg+1 of the next
-// level) are reduced on the way.
-__global__ __launch_bounds__(kTileThreads) void k_part_scatter(
+// level) are reduced on the way.  A block stages its tile in shared memory, ranks every body
+// inside its child (one ballot per row of the tile, a table of per-(row, warp) counts and its
+// scan), and then writes the tile out in output order: consecutive threads write consecutive
+// destinations, one contiguous run per child.
+__global__ __launch_bounds__(kTileThreads, 3) void k_part_scatter(
     Topology t, LevelArgs lv, const double *sx, const double *sy, const double *sz,
     const uint32_t *sid, double *dx, double *dy, double *dz, uint32_t *did, const SegSel *sel,
     const uint32_t *tile_off, unsigned long long *nbmin, unsigned long long *nbmax,
     uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char scat_raw[];
+    ScatTile &S = *reinterpret_cast<ScatTile *>(scat_raw);
     TileRef r;
-    if (!tile_of(t, lv, r)) return;
-    // [child][dim] running bounds of this thread, as ordered keys
-    unsigned long long cmn[2][3] = {{~0ull, ~0ull, ~0ull}, {~0ull, ~0ull, ~0ull}};
-    unsigned long long cmx[2][3] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
+    if (!tile_at(t, lv, blockIdx.x, r)) return;  // block-uniform
+    constexpr int kRows = kTile / kTileThreads;
+    constexpr int kWarps = kTileThreads / 32;
+    __shared__ uint32_t cntL[kRows][kWarps], cntR[kRows][kWarps];
+    __shared__ uint32_t s_nl;
+    __shared__ unsigned long long red[kWarps][12];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t n = r.hi - r.lo;  // bodies of this tile
+#pragma unroll
+    for (int i = 0; i < kRows; ++i) {
+        const uint32_t q = (uint32_t)i * kTileThreads + threadIdx.x;
+        if (q < n) {
+            const uint32_t k = r.start + r.lo + q;
+            cp_async8(&S.x[q], sx + k);
+            cp_async8(&S.y[q], sy + k);
+            cp_async8(&S.z[q], sz + k);
+            cp_async4(&S.id[q], sid + k);
+        }
+    }
     const SegSel s = sel[r.seg];
     const uint32_t mid = split_rank(lv, r.cnt);
     // without tile offsets every segment is one tile: nothing goes left before it
     const uint32_t lbase = tile_off ? tile_off[(size_t)r.seg * lv.tiles + r.tile] : 0u;
     const uint32_t rbase = r.lo - lbase;
-    // The tile as kRows rows of one element per thread: all loads first, then one ballot
-    // per row, one table of per-(row, warp) counts and its row-major exclusive scan, so the
-    // stable order costs three block barriers per tile.
-    constexpr int kRows = kTile / kTileThreads;
-    constexpr int kWarps = kTileThreads / 32;
-    __shared__ uint32_t cntL[kRows][kWarps], cntR[kRows][kWarps];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t lt = (1u << lane) - 1u;
-    double vx[kRows], vy[kRows], vz[kRows];
-    uint32_t vid[kRows], bl[kRows], br[kRows];
-    bool isL[kRows], in[kRows];
+    cp_async_wait_all();
+    __syncthreads();
+
+    // [child][dim] running bounds of this thread, as ordered keys
+    unsigned long long cmn[2][3] = {{~0ull, ~0ull, ~0ull}, {~0ull, ~0ull, ~0ull}};
+    unsigned long long cmx[2][3] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
+    uint32_t bl[kRows], br[kRows];
 #pragma unroll
     for (int i = 0; i < kRows; ++i) {
-        const uint32_t k = r.lo + (uint32_t)i * kTileThreads + threadIdx.x;
-        in[i] = k < r.hi;
-        vx[i] = vy[i] = vz[i] = 0.0;
-        vid[i] = 0u;
-        if (in[i]) {
-            vx[i] = sx[r.start + k];
-            vy[i] = sy[r.start + k];
-            vz[i] = sz[r.start + k];
-            vid[i] = sid[r.start + k];
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < kRows; ++i) {
-        const unsigned long long kx = ord_key(vx[i]), ky = ord_key(vy[i]), kz = ord_key(vz[i]);
-        const unsigned long long key = s.sd == 0 ? kx : (s.sd == 1 ? ky : kz);
-        isL[i] = in[i] && goes_left(key, vid[i], s.kmed, s.idmed);
-        bl[i] = __ballot_sync(kFull, isL[i]);
-        br[i] = __ballot_sync(kFull, in[i] && !isL[i]);
-        if (nbmin && in[i]) {
-            if (isL[i]) {
-                cmn[0][0] = min(cmn[0][0], kx); cmx[0][0] = max(cmx[0][0], kx);
-                cmn[0][1] = min(cmn[0][1], ky); cmx[0][1] = max(cmx[0][1], ky);
-                cmn[0][2] = min(cmn[0][2], kz); cmx[0][2] = max(cmx[0][2], kz);
-            } else {
-                cmn[1][0] = min(cmn[1][0], kx); cmx[1][0] = max(cmx[1][0], kx);
-                cmn[1][1] = min(cmn[1][1], ky); cmx[1][1] = max(cmx[1][1], ky);
-                cmn[1][2] = min(cmn[1][2], kz); cmx[1][2] = max(cmx[1][2], kz);
+        const uint32_t q = (uint32_t)i * kTileThreads + threadIdx.x;
+        const bool in = q < n;
+        bool isL = false;
+        if (in) {
+            const unsigned long long kx = ord_key(S.x[q]), ky = ord_key(S.y[q]),
+                                     kz = ord_key(S.z[q]);
+            const unsigned long long key = s.sd == 0 ? kx : (s.sd == 1 ? ky : kz);
+            isL = goes_left(key, S.id[q], s.kmed, s.idmed);
+            if (nbmin) {
+                if (isL) {
+                    cmn[0][0] = min(cmn[0][0], kx); cmx[0][0] = max(cmx[0][0], kx);
+                    cmn[0][1] = min(cmn[0][1], ky); cmx[0][1] = max(cmx[0][1], ky);
+                    cmn[0][2] = min(cmn[0][2], kz); cmx[0][2] = max(cmx[0][2], kz);
+                } else {
+                    cmn[1][0] = min(cmn[1][0], kx); cmx[1][0] = max(cmx[1][0], kx);
+                    cmn[1][1] = min(cmn[1][1], ky); cmx[1][1] = max(cmx[1][1], ky);
+                    cmn[1][2] = min(cmn[1][2], kz); cmx[1][2] = max(cmx[1][2], kz);
+                }
             }
         }
+        bl[i] = __ballot_sync(kFull, in && isL);
+        br[i] = __ballot_sync(kFull, in && !isL);
     }
     if (lane == 0) {
 #pragma unroll
@@ -886,34 +918,50 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
             if (lane >= o) { sa += ua; sb += ub; }
         }
         const uint32_t ea = sa - a0 - a1, eb = sb - b0 - b1;
-        // a one-tile segment checks here what k_tile_scan checks otherwise: exactly the
-        // wanted rank went left
-        if (!tile_off && lane == 31 && sa != mid) atomicOr(err, kErrSelect);
+        // a one-tile segment checks here what the select kernels check otherwise: exactly
+        // the wanted rank went left
+        if (lane == 31) {
+            s_nl = sa;
+            if (!tile_off && sa != mid) atomicOr(err, kErrSelect);
+        }
         __syncwarp();
         if (c0 < kCells) { cntL[c0 / kWarps][c0 % kWarps] = ea; cntR[c0 / kWarps][c0 % kWarps] = eb; }
         if (c1 < kCells) { cntL[c1 / kWarps][c1 % kWarps] = ea + a0; cntR[c1 / kWarps][c1 % kWarps] = eb + b0; }
     }
     __syncthreads();
+    const uint32_t nl = s_nl;
 #pragma unroll
     for (int i = 0; i < kRows; ++i) {
-        if (!in[i]) continue;
-        const uint32_t dst = isL[i] ? r.start + lbase + cntL[i][warp] + __popc(bl[i] & lt)
-                                    : r.start + mid + rbase + cntR[i][warp] + __popc(br[i] & lt);
-        // a failed select (flagged by k_tile_scan) must not write outside the segment
-        if (dst < r.start + r.cnt) {
-            dx[dst] = vx[i];
-            dy[dst] = vy[i];
-            dz[dst] = vz[i];
-            did[dst] = vid[i];
-            if (lv.med_pos && vid[i] == s.idmed) {
-                const unsigned long long key =
-                    ord_key(s.sd == 0 ? vx[i] : (s.sd == 1 ? vy[i] : vz[i]));
+        const uint32_t q = (uint32_t)i * kTileThreads + threadIdx.x;
+        if ((bl[i] | br[i]) >> lane & 1u) {
+            const bool isL = bl[i] >> lane & 1u;
+            const uint32_t slot = isL ? cntL[i][warp] + __popc(bl[i] & lt)
+                                      : nl + cntR[i][warp] + __popc(br[i] & lt);
+            S.order[slot] = (uint16_t)q;
+        }
+    }
+    __syncthreads();
+    // write-out in output order: slots [0, nl) are the tile's left bodies, the rest its right
+    const uint32_t lstart = r.start + lbase, rstart = r.start + mid + rbase - nl;
+    const uint32_t end = r.start + r.cnt;
+    for (uint32_t j = threadIdx.x; j < n; j += kTileThreads) {
+        const uint32_t q = S.order[j];
+        const uint32_t dst = (j < nl ? lstart : rstart) + j;
+        // a failed select (flagged by the select kernels) must not write outside the segment
+        if (dst < end) {
+            const double vx = S.x[q], vy = S.y[q], vz = S.z[q];
+            const uint32_t vid = S.id[q];
+            dx[dst] = vx;
+            dy[dst] = vy;
+            dz[dst] = vz;
+            did[dst] = vid;
+            if (lv.med_pos && vid == s.idmed) {
+                const unsigned long long key = ord_key(s.sd == 0 ? vx : (s.sd == 1 ? vy : vz));
                 if (key == s.kmed) *lv.med_pos = dst;
             }
         }
     }
     if (nbmin) {
-        __shared__ unsigned long long red[kTileThreads / 32][12];
 #pragma unroll
         for (int c = 0; c < 2; ++c)
 #pragma unroll
@@ -933,7 +981,7 @@ __global__ __launch_bounds__(kTileThreads) void k_part_scatter(
             const int c = threadIdx.x / 6, q = threadIdx.x % 6, d = q % 3;
             const bool is_max = q >= 3;
             unsigned long long v = is_max ? 0ull : ~0ull;
-            for (int wq = 0; wq < kTileThreads / 32; ++wq)
+            for (int wq = 0; wq < kWarps; ++wq)
                 v = is_max ? max(v, red[wq][threadIdx.x]) : min(v, red[wq][threadIdx.x]);
             const size_t child = 2 * (size_t)r.seg + c;
             if (is_max)
@@ -999,10 +1047,12 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
                                     s.sel, no, tile_off, s.err);
         launched += 1;
     }
-    k_part_scatter<<<grid, kTileThreads, 0, st>>>(t, lv, w.x[cur], w.y[cur], w.z[cur],
-                                                  w.id[cur], w.x[nxt], w.y[nxt], w.z[nxt],
-                                                  w.id[nxt], s.sel, tile_off, nbmin, nbmax,
-                                                  s.err);
+    // set on every launch: the attribute belongs to the current device's context
+    cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(ScatTile));
+    k_part_scatter<<<grid, kTileThreads, sizeof(ScatTile), st>>>(
+        t, lv, w.x[cur], w.y[cur], w.z[cur], w.id[cur], w.x[nxt], w.y[nxt], w.z[nxt], w.id[nxt],
+        s.sel, tile_off, nbmin, nbmax, s.err);
     return launched + 1;
 }
 
@@ -1040,8 +1090,22 @@ struct LocalSmem {
     uint32_t lvl_off[kLocalLevels + 1];
     uint32_t nlvl;
     uint32_t wcnt[kLocalWarps];
+    // teams of warps on one node: per-warp bounds and left counts, per-team candidate count
+    unsigned long long bb[kLocalWarps][6];
+    uint32_t wl[kLocalWarps];
+    uint32_t tcnt[kLocalWarps];
 };
 constexpr int kLocalSmallCap = 640;
+
+// Barrier of a team of W warps (warps team*W .. team*W+W-1): named barrier 1+team over its
+// 32*W threads, or the warp's own sync for a one-warp team.
+__device__ __forceinline__ void team_sync(uint32_t team, uint32_t W) {
+    if (W == 1) {
+        __syncwarp();
+    } else {
+        asm volatile("barrier.sync %0, %1;" ::"r"(1u + team), "r"(32u * W) : "memory");
+    }
+}
 
 // Candidate filter of the radix select: the top `kb` bits of the key and the top `ib` bits of
 // the id are fixed to kp / ip.
@@ -1447,17 +1511,27 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
     for (uint32_t L = 0;; ++L) {
         const uint32_t lo = S.lvl_off[L], hi = S.lvl_off[L + 1];
         if (hi == lo) break;
-        for (uint32_t i = lo + warp; i < hi; i += kLocalWarps) {
+        // Levels with fewer nodes than warps give each node a team of W warps (W = 8, 4, 2
+        // at 1, 2, 3-4 nodes), which splits the node's passes and meets at a named barrier;
+        // deeper levels run one warp per node.
+        const uint32_t G = hi - lo;
+        uint32_t W = 1;
+        while (2u * W * G <= (uint32_t)kLocalWarps) W *= 2u;
+        const uint32_t team = (uint32_t)warp / W, tw = (uint32_t)warp % W;
+        const uint32_t lead = team * W;  // the team's first warp: its buffers are the team's
+        const uint32_t tstep = 32u * W, ttid = tw * 32u + (uint32_t)lane;
+        for (uint32_t i = lo + team; i < hi; i += (uint32_t)kLocalWarps / W) {
             const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
             if (cn <= 32u) {
                 // the whole subtree of a node of <= 32 bodies in one warp's registers; its
                 // descendants (parent also <= 32) were done with it
-                if (S.tab_pcn[i] > 32u) small_subtree(S, t, no, st, cn, nid, leaf, lane, err);
+                if (tw == 0 && S.tab_pcn[i] > 32u)
+                    small_subtree(S, t, no, st, cn, nid, leaf, lane, err);
                 continue;
             }
             // ---- 1. bounding box and split
             unsigned long long kmn[3] = {~0ull, ~0ull, ~0ull}, kmx[3] = {0ull, 0ull, 0ull};
-            for (uint32_t k = lane; k < cn; k += 32) {
+            for (uint32_t k = ttid; k < cn; k += tstep) {
                 const uint32_t l = S.perm[st + k];
                 const unsigned long long k0 = ord_key(S.x[l]), k1 = ord_key(S.y[l]),
                                          k2 = ord_key(S.z[l]);
@@ -1465,18 +1539,39 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                 kmn[1] = min(kmn[1], k1); kmx[1] = max(kmx[1], k1);
                 kmn[2] = min(kmn[2], k2); kmx[2] = max(kmx[2], k2);
             }
-            double mn[3], mx[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 kmn[d] = warp_min(kmn[d]);
                 kmx[d] = warp_max(kmx[d]);
+            }
+            if (W > 1) {
+                if (lane == 0) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        S.bb[warp][d] = kmn[d];
+                        S.bb[warp][3 + d] = kmx[d];
+                    }
+                }
+                if (ttid == 0) S.tcnt[team] = 0u;  // candidate count of the gather below
+                team_sync(team, W);
+                for (uint32_t q = 0; q < W; ++q) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        kmn[d] = min(kmn[d], S.bb[lead + q][d]);
+                        kmx[d] = max(kmx[d], S.bb[lead + q][3 + d]);
+                    }
+                }
+            }
+            double mn[3], mx[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
                 mn[d] = ord_val(kmn[d]);
                 mx[d] = ord_val(kmx[d]);
             }
             uint32_t sd;
             double size;
             choose_split(mn, mx, sd, size);
-            if (lane == 0) {
+            if (ttid == 0) {
                 no.split_dim[nid] = (uint8_t)sd;
                 no.size[nid] = size;
             }
@@ -1491,23 +1586,26 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                 rs.ib = 0;
                 rs.ip = 0;
             }
-            uint32_t *h = S.hist[warp];
+            // a team alternates between its first two warps' histograms, so that clearing the
+            // next pass's never races with the reads of this pass's
+            uint32_t pass = 0;
             while (ccount > 32) {
                 if (rs.kb == 64 && rs.ib == 32) {  // cannot happen with distinct ids
-                    if (lane == 0) atomicOr(err, kErrSelect);
+                    if (ttid == 0) atomicOr(err, kErrSelect);
                     break;
                 }
+                uint32_t *h = S.hist[W > 1 ? lead + (pass & 1u) : (uint32_t)warp];
+                ++pass;
                 const int w = rs.width();
-#pragma unroll
-                for (int q = 0; q < 8; ++q) h[lane * 8 + q] = 0u;
-                __syncwarp();
-                for (uint32_t k = lane; k < cn; k += 32) {
+                for (uint32_t q = ttid; q < 256u; q += tstep) h[q] = 0u;
+                team_sync(team, W);
+                for (uint32_t k = ttid; k < cn; k += tstep) {
                     const uint32_t l = S.perm[st + k];
                     const unsigned long long key = ord_key(coord(S, sd, l));
                     const uint32_t id = S.id[l];
                     if (rs.match(key, id)) atomicAdd(&h[rs.digit(key, id, w)], 1u);
                 }
-                __syncwarp();
+                team_sync(team, W);
                 uint32_t mine = 0;
 #pragma unroll
                 for (int q = 0; q < 8; ++q) mine += h[lane * 8 + q];
@@ -1540,11 +1638,12 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                 rs.fix(dsel, w);
                 r -= below;
                 ccount = cnt;
-                __syncwarp();
+                if (W == 1) __syncwarp();
             }
-            // gather the <= 32 candidates, then rank them by comparison
+            // gather the <= 32 candidates (a team counts them in shared memory; their order
+            // does not matter, they are ranked by comparison)
             uint32_t ng = 0;
-            for (uint32_t base = 0; base < cn; base += 32) {
+            for (uint32_t base = tw * 32u; base < cn; base += tstep) {
                 const uint32_t k = base + lane;
                 bool hit = false;
                 unsigned long long key = 0;
@@ -1556,20 +1655,28 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                     hit = rs.match(key, id);
                 }
                 const uint32_t m = __ballot_sync(kFull, hit);
-                if (hit) {
-                    const uint32_t off = ng + __popc(m & lt);
-                    if (off < 32) {
-                        S.ckey[warp][off] = key;
-                        S.cid[warp][off] = id;
-                        S.clid[warp][off] = (uint16_t)l;
+                if (m) {
+                    uint32_t b0 = ng;
+                    if (W > 1) {
+                        if (lane == 0) b0 = atomicAdd(&S.tcnt[team], (uint32_t)__popc(m));
+                        b0 = __shfl_sync(kFull, b0, 0);
                     }
+                    if (hit) {
+                        const uint32_t off = b0 + __popc(m & lt);
+                        if (off < 32) {
+                            S.ckey[lead][off] = key;
+                            S.cid[lead][off] = id;
+                            S.clid[lead][off] = (uint16_t)l;
+                        }
+                    }
+                    ng += __popc(m);
                 }
-                ng += __popc(m);
             }
-            __syncwarp();
+            team_sync(team, W);
+            if (W > 1) ng = S.tcnt[team];
             const bool have = (uint32_t)lane < min(ng, 32u);
-            const unsigned long long mk = have ? S.ckey[warp][lane] : ~0ull;
-            const uint32_t mi = have ? S.cid[warp][lane] : kFull;
+            const unsigned long long mk = have ? S.ckey[lead][lane] : ~0ull;
+            const uint32_t mi = have ? S.cid[lead][lane] : kFull;
             uint32_t rank = 0;
             for (int q = 0; q < 32; ++q) {
                 const unsigned long long ok = __shfl_sync(kFull, mk, q);
@@ -1578,16 +1685,39 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
             }
             const uint32_t wm = __ballot_sync(kFull, have && rank == r);
             const int ml = wm ? __ffs(wm) - 1 : 0;
-            if (!wm && lane == 0) atomicOr(err, kErrSelect);
+            if (!wm && ttid == 0) atomicOr(err, kErrSelect);
             const unsigned long long kmed = __shfl_sync(kFull, mk, ml);
             const uint32_t idmed = __shfl_sync(kFull, mi, ml);
-            if (lane == 0) no.split_val[nid] = coord(S, sd, S.clid[warp][ml]);
-            // ---- 3. stable partition around the median
+            if (ttid == 0) no.split_val[nid] = coord(S, sd, S.clid[lead][ml]);
+            // ---- 3. stable partition around the median: warp tw of the team takes the
+            // tw-th contiguous chunk of the node, after its left count is known
             const uint32_t mid = cn / 2;
-            uint32_t offL = 0, offR = 0;
-            for (uint32_t base = 0; base < cn; base += 32) {
+            const uint32_t chunk = W > 1 ? ((cn + W - 1) / W + 31u) & ~31u : cn;
+            const uint32_t c_lo = min(cn, tw * chunk), c_hi = min(cn, c_lo + chunk);
+            uint32_t offL = 0, totalL = 0;
+            if (W > 1) {
+                uint32_t cl = 0;
+                for (uint32_t base = c_lo; base < c_hi; base += 32) {
+                    const uint32_t k = base + lane;
+                    bool isL = false;
+                    if (k < c_hi) {
+                        const uint32_t l = S.perm[st + k];
+                        isL = goes_left(ord_key(coord(S, sd, l)), S.id[l], kmed, idmed);
+                    }
+                    cl += __popc(__ballot_sync(kFull, isL));
+                }
+                if (lane == 0) S.wl[warp] = cl;
+                team_sync(team, W);
+                for (uint32_t q = 0; q < W; ++q) {
+                    const uint32_t v = S.wl[lead + q];
+                    if (q < tw) offL += v;
+                    totalL += v;
+                }
+            }
+            uint32_t offR = c_lo - offL;
+            for (uint32_t base = c_lo; base < c_hi; base += 32) {
                 const uint32_t k = base + lane;
-                bool in = k < cn, isL = false;
+                bool in = k < c_hi, isL = false;
                 uint32_t l = 0;
                 if (in) {
                     l = S.perm[st + k];
@@ -1602,19 +1732,19 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                 offL += __popc(bl);
                 offR += __popc(br);
             }
+            if (W == 1) totalL = offL;
             // an inexact split (a failed select) leaves perm2 partly unwritten: keep perm, a
             // valid permutation, and report the error
-            __syncwarp();
-            if (offL == mid) {
-                for (uint32_t k = lane; k < cn; k += 32) S.perm[st + k] = S.perm2[st + k];
-            } else if (lane == 0) {
+            team_sync(team, W);
+            if (totalL == mid) {
+                for (uint32_t k = ttid; k < cn; k += tstep) S.perm[st + k] = S.perm2[st + k];
+            } else if (ttid == 0) {
                 atomicOr(err, kErrSelect);
             }
-            __syncwarp();
+            if (W == 1) __syncwarp();
         }
         // ---- children that are still internal, appended as the next level
         __syncthreads();
-        const uint32_t G = hi - lo;
         uint32_t fill = hi;
         for (uint32_t base = 0; base < 2 * G; base += blockDim.x) {
             const uint32_t u = base + threadIdx.x;
