@@ -146,6 +146,20 @@ __device__ __forceinline__ T warp_max(T v) {
     for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
     return v;
 }
+// 64-bit keys: minimum (maximum) of the high words, then of the low words among the lanes
+// that hold it -- two warp reductions instead of a five-step shuffle tree of 64-bit values.
+__device__ __forceinline__ unsigned long long warp_min(unsigned long long v) {
+    const uint32_t hi = (uint32_t)(v >> 32), lo = (uint32_t)v;
+    const uint32_t mh = __reduce_min_sync(kFull, hi);
+    const uint32_t ml = __reduce_min_sync(kFull, hi == mh ? lo : 0xffffffffu);
+    return ((unsigned long long)mh << 32) | ml;
+}
+__device__ __forceinline__ unsigned long long warp_max(unsigned long long v) {
+    const uint32_t hi = (uint32_t)(v >> 32), lo = (uint32_t)v;
+    const uint32_t mh = __reduce_max_sync(kFull, hi);
+    const uint32_t ml = __reduce_max_sync(kFull, hi == mh ? lo : 0u);
+    return ((unsigned long long)mh << 32) | ml;
+}
 // The build's first work arrays (positions and body ids in original order); with `bmin` set,
 // also the bounding box of the whole set (segment 0 of level 0) on ordered keys.
 __global__ __launch_bounds__(256) void k_init_work(Bodies b, double *wx, double *wy, double *wz,
@@ -1077,9 +1091,13 @@ constexpr int kLocalLevels = 16;
 // blocks share an SM instead of three.
 template <int kCap>
 struct LocalSmem {
-    double x[kCap], y[kCap], z[kCap], m[kCap];
+    double xyz[3][kCap];  // positions, one row per dimension
+    double m[kCap];
     uint32_t id[kCap];
-    uint32_t hist[kLocalWarps][256];
+    union {  // radix histograms (top-down), then internal nodes' moment sums (bottom-up)
+        uint32_t hist[kLocalWarps][256];
+        double mom[kLocalWarps * 128];
+    };
     unsigned long long ckey[kLocalWarps][32];
     uint32_t cid[kLocalWarps][32];
     // internal sub-segments of every level, appended level after level
@@ -1316,7 +1334,7 @@ __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
 
 template <class Smem>
 __device__ __forceinline__ double coord(const Smem &S, uint32_t sd, uint32_t l) {
-    return sd == 0 ? S.x[l] : (sd == 1 ? S.y[l] : S.z[l]);
+    return S.xyz[sd][l];
 }
 
 // Mixed leaf record: origin o = position of the leaf's first body, as hi + lo floats.  The
@@ -1326,7 +1344,7 @@ template <class Smem>
 __device__ __forceinline__ NodeF leaf_nodef(Smem &S, uint32_t st, uint32_t cn,
                                             uint32_t s0, const LocalOut &o) {
     const uint32_t l0 = S.perm[st];
-    const double ox = S.x[l0], oy = S.y[l0], oz = S.z[l0];
+    const double ox = S.xyz[0][l0], oy = S.xyz[1][l0], oz = S.xyz[2][l0];
     for (uint32_t k = st; k < st + cn; ++k) S.perm2[k] = (uint16_t)st;
     NodeF r;
     const float hx = (float)ox, hy = (float)oy, hz = (float)oz;
@@ -1351,15 +1369,15 @@ __device__ __forceinline__ void leaf_sums(const Smem &S, uint32_t st, uint32_t c
         const double mm = S.m[l];
         if (o.recd) {
             f[0] += mm;
-            f[1] = fma(mm, S.x[l], f[1]);
-            f[2] = fma(mm, S.y[l], f[2]);
-            f[3] = fma(mm, S.z[l], f[3]);
+            f[1] = fma(mm, S.xyz[0][l], f[1]);
+            f[2] = fma(mm, S.xyz[1][l], f[2]);
+            f[3] = fma(mm, S.xyz[2][l], f[3]);
         }
         if (o.recf && !is_heavy(S.id[l], o.heavy, o.n_heavy)) {
             g[0] += mm;
-            g[1] = fma(mm, S.x[l], g[1]);
-            g[2] = fma(mm, S.y[l], g[2]);
-            g[3] = fma(mm, S.z[l], g[3]);
+            g[1] = fma(mm, S.xyz[0][l], g[1]);
+            g[2] = fma(mm, S.xyz[1][l], g[2]);
+            g[3] = fma(mm, S.xyz[2][l], g[3]);
         }
     }
 }
@@ -1393,7 +1411,7 @@ __device__ __forceinline__ void small_subtree(Smem &S, const Topology &t, const 
                                            uint32_t leaf, int lane, uint32_t *err) {
     const bool valid = (uint32_t)lane < cn;
     const uint32_t l = valid ? S.perm[st + lane] : 0u;
-    const double c[3] = {S.x[l], S.y[l], S.z[l]};
+    const double c[3] = {S.xyz[0][l], S.xyz[1][l], S.xyz[2][l]};
     const unsigned long long k[3] = {ord_key(c[0]), ord_key(c[1]), ord_key(c[2])};
     const uint32_t id = S.id[l];
     uint32_t rank[3] = {0u, 0u, 0u};
@@ -1487,9 +1505,9 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
     const uint32_t lt = (1u << lane) - 1u;
 
     for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
-        S.x[k] = wx[s0 + k];
-        S.y[k] = wy[s0 + k];
-        S.z[k] = wz[s0 + k];
+        S.xyz[0][k] = wx[s0 + k];
+        S.xyz[1][k] = wy[s0 + k];
+        S.xyz[2][k] = wz[s0 + k];
         const uint32_t id = wid[s0 + k];
         S.id[k] = id;
         S.m[k] = o.mass[id];
@@ -1533,8 +1551,8 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
             unsigned long long kmn[3] = {~0ull, ~0ull, ~0ull}, kmx[3] = {0ull, 0ull, 0ull};
             for (uint32_t k = ttid; k < cn; k += tstep) {
                 const uint32_t l = S.perm[st + k];
-                const unsigned long long k0 = ord_key(S.x[l]), k1 = ord_key(S.y[l]),
-                                         k2 = ord_key(S.z[l]);
+                const unsigned long long k0 = ord_key(S.xyz[0][l]), k1 = ord_key(S.xyz[1][l]),
+                                         k2 = ord_key(S.xyz[2][l]);
                 kmn[0] = min(kmn[0], k0); kmx[0] = max(kmx[0], k0);
                 kmn[1] = min(kmn[1], k1); kmx[1] = max(kmx[1], k1);
                 kmn[2] = min(kmn[2], k2); kmx[2] = max(kmx[2], k2);
@@ -1814,6 +1832,11 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
             }
         }
     }
+    // Internal nodes' sums are also kept in shared memory, by node id within the segment's
+    // subtree while they fit (every node of a 640-body subtree at leaf size 7), so that the
+    // level above reads them without a round trip through L2.
+    const uint32_t nsets = (want_d ? 1u : 0u) + (want_f ? 1u : 0u);
+    const uint32_t mslots = nsets ? (uint32_t)(kLocalWarps * 128 / 4) / nsets : 0u;
     for (int L = (int)S.nlvl - 1; L >= 0; --L) {
         for (uint32_t i = S.lvl_off[L] + threadIdx.x; i < S.lvl_off[L + 1]; i += blockDim.x) {
             const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
@@ -1834,6 +1857,13 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                         store_moments(o.mof, cid, g);
                         o.recf[cid] = leaf_nodef(S, cst, ccn, s0, o);
                     }
+                } else if (cid - root < mslots) {
+                    const double *m = S.mom + 4 * (cid - root) * nsets;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (want_d) f[q] = m[q];
+                        if (want_f) g[q] = m[(want_d ? 4 : 0) + q];
+                    }
                 } else {
                     if (want_d) load_moments(o.mo, cid, f);
                     if (want_f) load_moments(o.mof, cid, g);
@@ -1842,6 +1872,14 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                 for (int q = 0; q < 4; ++q) {
                     if (want_d) fs[q] = __dadd_rn(fs[q], f[q]);
                     if (want_f) gs[q] = __dadd_rn(gs[q], g[q]);
+                }
+            }
+            if (nid - root < mslots) {
+                double *m = S.mom + 4 * (nid - root) * nsets;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (want_d) m[q] = fs[q];
+                    if (want_f) m[(want_d ? 4 : 0) + q] = gs[q];
                 }
             }
             const double size = no.size[nid];
@@ -1865,7 +1903,7 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
     for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
         const uint32_t l = S.perm[k];
         const uint32_t id = S.id[l];
-        const double x = S.x[l], y = S.y[l], z = S.z[l], mm = S.m[l];
+        const double x = S.xyz[0][l], y = S.xyz[1][l], z = S.xyz[2][l], mm = S.m[l];
         if (o.tpos) o.tpos[s0 + k] = make_double4_32a(x, y, z, mm);
         o.tid[s0 + k] = id;
         {
@@ -1880,8 +1918,8 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                                         (float)(z - (double)hz), fml);
             if (o.recf) {
                 const uint32_t l0 = S.perm[S.perm2[k]];
-                o.trel[s0 + k] = make_float4((float)(x - S.x[l0]), (float)(y - S.y[l0]),
-                                             (float)(z - S.z[l0]), fm);
+                o.trel[s0 + k] = make_float4((float)(x - S.xyz[0][l0]), (float)(y - S.xyz[1][l0]),
+                                             (float)(z - S.xyz[2][l0]), fm);
             }
         }
     }
