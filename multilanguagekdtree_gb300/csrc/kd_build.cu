@@ -1084,6 +1084,7 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
 
 constexpr int kLocalWarps = kLocalThreads / 32;
 constexpr int kLocalLevels = 16;
+constexpr int kLocalSizeSlots = 256;
 
 // Shared memory of one block, for segments of at most kCap bodies.  The kernel is built for
 // two capacities: kLocalMax, and kLocalSmallCap for trees whose local segments are all at
@@ -1108,6 +1109,8 @@ struct LocalSmem {
     uint32_t lvl_off[kLocalLevels + 1];
     uint32_t nlvl;
     uint32_t wcnt[kLocalWarps];
+    // node sizes by node id within the segment's subtree (for the bottom-up records)
+    double nsize[kLocalSizeSlots];
     // teams of warps on one node: per-warp bounds and left counts, per-team candidate count
     unsigned long long bb[kLocalWarps][6];
     uint32_t wl[kLocalWarps];
@@ -1408,7 +1411,8 @@ __device__ __forceinline__ void load_moments(const Moments &mo, uint32_t id, dou
 template <class Smem>
 __device__ __forceinline__ void small_subtree(Smem &S, const Topology &t, const NodeOut &no,
                                            uint32_t st, uint32_t cn, uint32_t nid,
-                                           uint32_t leaf, int lane, uint32_t *err) {
+                                           uint32_t root, uint32_t leaf, int lane,
+                                           uint32_t *err) {
     const bool valid = (uint32_t)lane < cn;
     const uint32_t l = valid ? S.perm[st + lane] : 0u;
     const double c[3] = {S.xyz[0][l], S.xyz[1][l], S.xyz[2][l]};
@@ -1450,10 +1454,11 @@ __device__ __forceinline__ void small_subtree(Smem &S, const Topology &t, const 
         const uint32_t B = sd == 0 ? sel[0] : (sd == 1 ? sel[1] : sel[2]);
         const uint32_t rs = sd == 0 ? rank[0] : (sd == 1 ? rank[1] : rank[2]);
         const uint32_t half = nc / 2;
-        // rank value of the median: the (half+1)-th smallest rank among the members
-        const uint32_t rmed = __fns(B, 0u, (int)half + 1);
-        const int ml = __ffs(__ballot_sync(kFull, mem && rs == rmed)) - 1;
-        if (ml < 0 || rmed > 31u) {
+        // members ranked below this lane's body; the median is the member with exactly
+        // `half` below it.  Distinct ranks (one bit of B per member) are checked here.
+        const uint32_t below = mem ? (uint32_t)__popc(B & ((1u << rs) - 1u)) : 0u;
+        const int ml = __ffs(__ballot_sync(kFull, mem && below == half)) - 1;
+        if (ml < 0 || (uint32_t)__popc(B) != nc) {
             if (lane == 0) atomicOr(err, kErrSelect);
             break;
         }
@@ -1463,9 +1468,10 @@ __device__ __forceinline__ void small_subtree(Smem &S, const Topology &t, const 
             no.split_dim[ni] = (uint8_t)sd;
             no.size[ni] = size;
             no.split_val[ni] = sv;
+            if (ni - root < (uint32_t)kLocalSizeSlots) S.nsize[ni - root] = size;
         }
         // members in rank order of the split dimension: the left half lies below the median
-        if (mem) pos = ns + (uint32_t)__popc(B & ((1u << rs) - 1u));
+        if (mem) pos = ns + below;
         const uint32_t rc = nc - half;
         if (rc > leaf) {  // at most one pending entry per depth: sp stays below 32
             if (lane == sp) {
@@ -1544,7 +1550,7 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                 // the whole subtree of a node of <= 32 bodies in one warp's registers; its
                 // descendants (parent also <= 32) were done with it
                 if (tw == 0 && S.tab_pcn[i] > 32u)
-                    small_subtree(S, t, no, st, cn, nid, leaf, lane, err);
+                    small_subtree(S, t, no, st, cn, nid, root, leaf, lane, err);
                 continue;
             }
             // ---- 1. bounding box and split
@@ -1592,6 +1598,7 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
             if (ttid == 0) {
                 no.split_dim[nid] = (uint8_t)sd;
                 no.size[nid] = size;
+                if (nid - root < (uint32_t)kLocalSizeSlots) S.nsize[nid - root] = size;
             }
             // ---- 2. exact select of rank cn/2
             uint32_t r = cn / 2, ccount = cn;
@@ -1882,7 +1889,8 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
                     if (want_f) m[(want_d ? 4 : 0) + q] = gs[q];
                 }
             }
-            const double size = no.size[nid];
+            const double size =
+                nid - root < (uint32_t)kLocalSizeSlots ? S.nsize[nid - root] : no.size[nid];
             const uint32_t right = nid + 1 + t.ttab[lc];
             if (want_d) {
                 store_moments(o.mo, nid, fs);
