@@ -461,17 +461,27 @@ __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
         __syncthreads();
         const double *w = pick(wx, wy, wz, s.sd) + r.start;
         constexpr int kRows = kTile / kTileThreads;
+        // the next tile's keys are requested before this tile's are binned, so that the
+        // loads of one overlap the shared-memory atomics of the other
+        double v[kRows];
+#pragma unroll
+        for (int i = 0; i < kRows; ++i) {
+            const uint32_t k = r.lo + (uint32_t)i * kTileThreads + threadIdx.x;
+            v[i] = k < hi ? w[k] : 0.0;
+        }
         for (uint32_t base = r.lo; base < hi; base += kTile) {
-            double v[kRows];
+            double nv[kRows];
 #pragma unroll
             for (int i = 0; i < kRows; ++i) {
-                const uint32_t k = base + (uint32_t)i * kTileThreads + threadIdx.x;
-                v[i] = k < hi ? w[k] : 0.0;
+                const uint32_t k = base + kTile + (uint32_t)i * kTileThreads + threadIdx.x;
+                nv[i] = k < hi ? w[k] : 0.0;
             }
 #pragma unroll
             for (int i = 0; i < kRows; ++i)
                 if (base + (uint32_t)i * kTileThreads + threadIdx.x < hi)
                     atomicAdd(&h[lin_bin(v[i], s.lo, s.scale)], 1u);
+#pragma unroll
+            for (int i = 0; i < kRows; ++i) v[i] = nv[i];
         }
         __syncthreads();
         for (int b = threadIdx.x; b < kHistBins; b += blockDim.x)
@@ -742,9 +752,10 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
         const bool bykey = kmn != kmx;
         int bits = bykey ? 64 - __clzll((long long)(kmn ^ kmx)) : 32 - __clz((int)(imn ^ imx));
         const uint32_t shift = bits > nbits ? (uint32_t)(bits - nbits) : 0u;
-        auto digit = [&](unsigned long long key, uint32_t id, uint32_t pos) -> uint32_t {
-            if (lin) return lin_bin(w[pos], st.lo, st.scale) >> (kHistBits - nbits);
-            return bykey ? ((uint32_t)(key >> shift) & (nb - 1)) : ((id >> shift) & (nb - 1));
+        // the candidate's bin; its id is loaded only when the pass bins by id
+        auto digit = [&](unsigned long long key, uint32_t pos) -> uint32_t {
+            if (lin) return lin_bin(ord_val(key), st.lo, st.scale) >> (kHistBits - nbits);
+            return bykey ? ((uint32_t)(key >> shift) & (nb - 1)) : ((ids[pos] >> shift) & (nb - 1));
         };
         for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) h[b] = 0;
         if (threadIdx.x == 0) ncomp = 0;
@@ -753,20 +764,20 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
             unsigned long long key;
             uint32_t pos;
             get(j, key, pos);
-            atomicAdd(&h[digit(key, ids[pos], pos)], 1u);
+            atomicAdd(&h[digit(key, pos)], 1u);
         }
         __syncthreads();
         find_bin(h, r, out3, nb);
         const uint32_t dig = out3[0], below = out3[1], inbin = out3[2];
         const int dst = src == 1 ? 2 : 1;
         for (uint32_t base = 0; base < c; base += blockDim.x) {
-            uint32_t j = base + threadIdx.x;
-            bool in = j < c;
+            const uint32_t j = base + threadIdx.x;
+            const bool in = j < c;
             unsigned long long key = 0;
             uint32_t pos = 0;
             if (in) get(j, key, pos);
-            bool hit = in && digit(key, ids[pos], pos) == dig;
-            uint32_t m = __ballot_sync(kFull, hit);
+            const bool hit = in && digit(key, pos) == dig;
+            const uint32_t m = __ballot_sync(kFull, hit);
             if (m) {
                 uint32_t leader = __ffs(m) - 1, slot = 0;
                 if (lane == (int)leader) slot = atomicAdd(&ncomp, (uint32_t)__popc(m));
