@@ -632,8 +632,15 @@ __device__ __forceinline__ void tile_offsets(const Topology &t, const LevelArgs 
     } else {
         if (threadIdx.x < kSmallSegTiles) scnt[threadIdx.x] = 0u;
         __syncthreads();
-        for (uint32_t j = threadIdx.x; j < cnt; j += blockDim.x)
-            if (goes_left(ord_key(w[j]), ids[j], kmed, idmed)) atomicAdd(&scnt[j / kTile], 1u);
+        // one ballot per warp row (a row of 32 never straddles a tile) and one atomic
+        for (uint32_t base = 0; base < cnt; base += blockDim.x) {
+            const uint32_t j = base + threadIdx.x;
+            const bool L = j < cnt && goes_left(ord_key(w[j]), ids[j], kmed, idmed);
+            const uint32_t m = __ballot_sync(kFull, L);
+            const uint32_t tile = (base + 32u * warp) / kTile;
+            if (lane == 0 && m && tile < (uint32_t)kSmallSegTiles)
+                atomicAdd(&scnt[tile], (uint32_t)__popc(m));
+        }
         __syncthreads();
         if (threadIdx.x < ntiles && threadIdx.x < kSmallSegTiles) tc[threadIdx.x] = scnt[threadIdx.x];
         if (threadIdx.x == 0 && ntiles > kSmallSegTiles) atomicOr(s.err, kErrSelect);
@@ -1158,6 +1165,15 @@ struct RadixState {
     __device__ __forceinline__ int width() const {
         return kb < 64 ? min(8, 64 - kb) : min(8, 32 - ib);
     }
+    // (key, id) orders below every candidate: its fixed bits compare lower
+    __device__ __forceinline__ bool below(unsigned long long key, uint32_t id) const {
+        if (kb > 0) {
+            const unsigned long long t = kb == 64 ? key : (key >> (64 - kb));
+            if (t != kp) return t < kp;
+            if (kb < 64) return false;
+        }
+        return ib > 0 && (id >> (32 - ib)) < ip;
+    }
     __device__ __forceinline__ void fix(uint32_t d, int w) {
         if (kb < 64) {
             kp = (kp << w) | d;
@@ -1268,7 +1284,8 @@ __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
         __syncwarp();
     }
     // gather the <= 32 candidates, then rank them by comparison
-    uint32_t ng = 0;
+    // with it, per tile the bodies that order below every candidate: they go left
+    uint32_t ng = 0, lo0 = 0, lo1 = 0;
     for (uint32_t base = 0; base < cn; base += 32) {
         const uint32_t k = base + lane;
         bool hit = false;
@@ -1278,6 +1295,10 @@ __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
             key = ord_key(w[k]);
             id = ids[k];
             hit = rs.match(key, id);
+            if (!hit && rs.below(key, id)) {
+                lo0 += k < (uint32_t)kTile ? 1u : 0u;
+                lo1 += k >= (uint32_t)kTile ? 1u : 0u;
+            }
         }
         const uint32_t m = __ballot_sync(kFull, hit);
         if (hit) {
@@ -1323,16 +1344,15 @@ __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
         no.split_val[nid] = w[pos];
     }
     if (!tile_off) return;  // one tile: the scatter counts and checks by itself
-    // the bodies going left in each of the segment's (at most two) tiles
+    // the bodies going left in each of the segment's (at most two) tiles: those below every
+    // candidate, counted in the gather, and the candidates that order below the median
     const int ml = __ffs(wm) - 1;
     const unsigned long long kmed = __shfl_sync(kFull, mk, ml);
     const uint32_t idmed = __shfl_sync(kFull, mi, ml);
-    uint32_t c0 = 0, c1 = 0;
-    for (uint32_t k = lane; k < cn; k += 32) {
-        const bool L = goes_left(ord_key(w[k]), ids[k], kmed, idmed);
-        c0 += (L && k < (uint32_t)kTile) ? 1u : 0u;
-        c1 += (L && k >= (uint32_t)kTile) ? 1u : 0u;
-    }
+    const bool cl = have && goes_left(mk, mi, kmed, idmed);
+    const uint32_t cpk = have ? cpos[warp][lane] : 0u;
+    uint32_t c0 = lo0 + (cl && cpk < (uint32_t)kTile ? 1u : 0u);
+    uint32_t c1 = lo1 + (cl && cpk >= (uint32_t)kTile ? 1u : 0u);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         c0 += __shfl_xor_sync(kFull, c0, o);
