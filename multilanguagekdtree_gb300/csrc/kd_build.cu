@@ -18,8 +18,8 @@
 // (bounding box -> split -> exact median select -> stable partition into the other
 // ping-pong buffer, which also reduces the children's bounding boxes); below that, one
 // thread block takes a whole segment into shared memory and finishes its subtree there
-// (one warp per node: radix select on a warp-private histogram, ballot partition; nodes of
-// at most 32 bodies in one warp's registers).
+// (one warp or a team of warps per node: radix select, ballot partition; nodes of at most
+// 32 bodies in one warp's registers).
 #include "kd_internal.cuh"
 
 namespace kd {
@@ -1091,14 +1091,18 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
 // ------------------------------------------------------------------ local subtree finish
 //
 // One thread block owns a segment of at most kLocalMax bodies and builds its whole subtree
-// in shared memory.  Per level, every internal sub-segment is handled by one warp, with no
-// block barrier inside the level:
+// in shared memory.  Per level, every internal sub-segment of more than 32 bodies is
+// handled by one warp -- by a team of 2, 4 or 8 warps meeting at a named barrier when the
+// level has fewer sub-segments than the block has warps -- with no block barrier inside the
+// level:
 //   1. bounding box -> split_dim, size (choose_split);
-//   2. exact rank-len/2 select on (key, body id): 8-bit radix passes over a warp-private
+//   2. exact rank-len/2 select on (key, body id): 8-bit radix passes over the team's
 //      histogram, narrowing the candidate set until at most 32 remain, then a 32-lane
 //      rank by comparison;
 //   3. stable partition of the sub-segment's index list around the median.
-// A block barrier separates levels (the next level's sub-segment table).
+// A sub-segment of at most 32 bodies finishes its whole subtree in one warp's registers.
+// A block barrier separates levels (the next level's sub-segment table); then the node sums
+// and records are formed bottom-up, level by level.
 
 constexpr int kLocalWarps = kLocalThreads / 32;
 constexpr int kLocalLevels = 16;
