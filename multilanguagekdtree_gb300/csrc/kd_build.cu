@@ -1107,6 +1107,9 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
 constexpr int kLocalWarps = kLocalThreads / 32;
 constexpr int kLocalLevels = 16;
 constexpr int kLocalSizeSlots = 256;
+#ifndef KD_LOCAL_SORTED
+#define KD_LOCAL_SORTED 1
+#endif
 
 // Shared memory of one block, for segments of at most kCap bodies.  The kernel is built for
 // two capacities: kLocalMax, and kLocalSmallCap for trees whose local segments are all at
@@ -1530,6 +1533,122 @@ __device__ __forceinline__ void small_subtree(Smem &S, const Topology &t, const 
     __syncwarp();
 }
 
+// The bottom-up pass and the tree-ordered outputs of a finished segment: its bodies in tree
+// order in perm, its internal nodes in the level table (shared by both subtree finishes).
+template <class Smem>
+__device__ __forceinline__ void local_finish(Smem &S, const Topology &t, const NodeOut &no,
+                                             const LocalOut &o, uint32_t root, uint32_t s0,
+                                             uint32_t c0, uint32_t leaf) {
+    // ================================================================ bottom-up moments
+    const bool want_d = o.recd != nullptr, want_f = o.recf != nullptr;
+    if (c0 <= leaf) {
+        if (threadIdx.x == 0) {
+            double f[4], g[4];
+            leaf_sums(S, 0, c0, o, f, g);
+            if (want_d) {
+                store_moments(o.mo, root, f);
+                o.recd[root] = make_noded(f[0], f[1], f[2], f[3], 0.0, s0, c0);
+            }
+            if (want_f) {
+                store_moments(o.mof, root, g);
+                o.recf[root] = leaf_nodef(S, 0, c0, s0, o);
+            }
+        }
+    }
+    // Internal nodes' sums are also kept in shared memory, by node id within the segment's
+    // subtree while they fit (every node of a 640-body subtree at leaf size 7), so that the
+    // level above reads them without a round trip through L2.
+    const uint32_t nsets = (want_d ? 1u : 0u) + (want_f ? 1u : 0u);
+    const uint32_t mslots = nsets ? (uint32_t)(kLocalWarps * 128 / 4) / nsets : 0u;
+    for (int L = (int)S.nlvl - 1; L >= 0; --L) {
+        for (uint32_t i = S.lvl_off[L] + threadIdx.x; i < S.lvl_off[L + 1]; i += blockDim.x) {
+            const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
+            const uint32_t lc = cn / 2;
+            double fs[4] = {0.0, 0.0, 0.0, 0.0}, gs[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int side = 0; side < 2; ++side) {
+                const uint32_t cst = side ? st + lc : st;
+                const uint32_t ccn = side ? cn - lc : lc;
+                const uint32_t cid = side ? nid + 1 + t.ttab[lc] : nid + 1;
+                double f[4], g[4];
+                if (ccn <= leaf) {
+                    leaf_sums(S, cst, ccn, o, f, g);
+                    if (want_d) {
+                        store_moments(o.mo, cid, f);
+                        o.recd[cid] = make_noded(f[0], f[1], f[2], f[3], 0.0, s0 + cst, ccn);
+                    }
+                    if (want_f) {
+                        store_moments(o.mof, cid, g);
+                        o.recf[cid] = leaf_nodef(S, cst, ccn, s0, o);
+                    }
+                } else if (cid - root < mslots) {
+                    const double *m = S.mom + 4 * (cid - root) * nsets;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (want_d) f[q] = m[q];
+                        if (want_f) g[q] = m[(want_d ? 4 : 0) + q];
+                    }
+                } else {
+                    if (want_d) load_moments(o.mo, cid, f);
+                    if (want_f) load_moments(o.mof, cid, g);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (want_d) fs[q] = __dadd_rn(fs[q], f[q]);
+                    if (want_f) gs[q] = __dadd_rn(gs[q], g[q]);
+                }
+            }
+            if (nid - root < mslots) {
+                double *m = S.mom + 4 * (nid - root) * nsets;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (want_d) m[q] = fs[q];
+                    if (want_f) m[(want_d ? 4 : 0) + q] = gs[q];
+                }
+            }
+            const double size =
+                nid - root < (uint32_t)kLocalSizeSlots ? S.nsize[nid - root] : no.size[nid];
+            const uint32_t right = nid + 1 + t.ttab[lc];
+            if (want_d) {
+                store_moments(o.mo, nid, fs);
+                const NodeD q = make_noded(fs[0], fs[1], fs[2], fs[3], size, right, 0u);
+                o.recd[nid] = q;
+                o.recp[nid] = make_nodep(q);
+            }
+            if (want_f) {
+                store_moments(o.mof, nid, gs);
+                o.recf[nid] = make_nodef(gs[0], gs[1], gs[2], gs[3], size, right, 0u);
+            }
+        }
+        __syncthreads();
+    }
+
+    // ================================================================ tree-ordered bodies
+    __syncthreads();  // leaf starts in perm2 (a root leaf has no level barrier above)
+    for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
+        const uint32_t l = S.perm[k];
+        const uint32_t id = S.id[l];
+        const double x = S.xyz[0][l], y = S.xyz[1][l], z = S.xyz[2][l], mm = S.m[l];
+        if (o.tpos) o.tpos[s0 + k] = make_double4_32a(x, y, z, mm);
+        o.tid[s0 + k] = id;
+        {
+            const float hx = (float)x, hy = (float)y, hz = (float)z;
+            const bool hv = is_heavy(id, o.heavy, o.n_heavy);
+            const float fm = hv ? 0.0f : (float)mm;
+            // light mass split hi (thi.w) + lo (tlo.w): the heavy bodies' direct sums read
+            // every light mass back to ~2^-48 relative
+            const float fml = hv ? 0.0f : (float)(mm - (double)fm);
+            o.thi[s0 + k] = make_float4(hx, hy, hz, fm);
+            o.tlo[s0 + k] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
+                                        (float)(z - (double)hz), fml);
+            if (o.recf) {
+                const uint32_t l0 = S.perm[S.perm2[k]];
+                o.trel[s0 + k] = make_float4((float)(x - S.xyz[0][l0]), (float)(y - S.xyz[1][l0]),
+                                             (float)(z - S.xyz[2][l0]), fm);
+            }
+        }
+    }
+}
+
 template <int kCap>
 __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void k_local(
     Topology t, const uint32_t *roots,
@@ -1858,114 +1977,430 @@ __global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void
         __syncthreads();
     }
 
-    // ================================================================ bottom-up moments
-    const bool want_d = o.recd != nullptr, want_f = o.recf != nullptr;
-    if (c0 <= leaf) {
-        if (threadIdx.x == 0) {
-            double f[4], g[4];
-            leaf_sums(S, 0, c0, o, f, g);
-            if (want_d) {
-                store_moments(o.mo, root, f);
-                o.recd[root] = make_noded(f[0], f[1], f[2], f[3], 0.0, s0, c0);
-            }
-            if (want_f) {
-                store_moments(o.mof, root, g);
-                o.recf[root] = leaf_nodef(S, 0, c0, s0, o);
-            }
+    local_finish(S, t, no, o, root, s0, c0, leaf);
+}
+
+// ------------------------------------------------------------------ presorted subtree finish
+//
+// The same subtree, built from three sorted lists instead of a select per node.  The
+// segment's bodies are sorted once along each dimension by (ordered key, local index) --
+// the local index orders bodies as their ids do, since every partition above was stable --
+// with a stable block radix sort of 16-bit indices over the key bits below the segment's
+// common prefix.  Each node then owns the same range [st, st + cn) of all three lists, each
+// sorted along its dimension: its bounding box is the lists' first and last entries, its
+// median the entry st + cn/2 of the split dimension's list, whose first half is the left
+// child.  A level flags its nodes' left bodies and partitions the other two lists stably
+// within every node at once (one block scan per level), so a level costs the same few passes
+// over the segment whatever the size and number of its nodes.  At the end each leaf's bodies
+// are put in index order (the select-based finish, used above kLocalSmallCap bodies, leaves
+// the bodies of its <= 32-body subtrees in rank order of their last split dimension: the
+// same leaves, the same splits); the bottom-up pass and the outputs are the shared ones.
+template <int kCap>
+struct SortSmem {
+    double xyz[3][kCap];  // positions, one row per dimension
+    double m[kCap];
+    uint32_t id[kCap];
+    uint16_t lst[2][3][kCap];  // the three sorted lists; levels alternate between the copies
+    uint16_t perm[kCap], perm2[kCap];
+    uint16_t aux[kCap];  // sort: rank within the warp's run of the digit; levels: node of a position
+    uint8_t dig[kCap];   // sort: digit of a position
+    uint8_t flag[kCap];  // levels: body goes to the left child
+    union {  // radix counters (sort), then internal nodes' moment sums (bottom-up)
+        uint32_t hist[kLocalWarps][256];
+        double mom[kLocalWarps * 128];
+    };
+    uint16_t estart[3][kCap / 2];  // levels: scan value at each node's first position
+    uint16_t cslot[kCap];          // levels: next-level slot of child 2j + side of node j
+    uint32_t tab_id[kCap];
+    uint16_t tab_st[kCap], tab_cn[kCap];
+    uint8_t tab_sd[kCap];
+    uint32_t lvl_off[kLocalLevels + 1];
+    uint32_t nlvl;
+    uint32_t wcnt[kLocalWarps];
+    uint32_t wscan[kLocalWarps][4];
+    unsigned long long red[kLocalWarps][6];
+    double nsize[kLocalSizeSlots];
+};
+static_assert(kLocalThreads == 256, "one thread per radix digit");
+constexpr uint16_t kNoNode = 0xffffu;
+
+// Exclusive block scan of three counts per thread (v[d] in, prefix out); `tot` gets the
+// totals.  Two block barriers.
+template <class Smem>
+__device__ __forceinline__ void block_scan3(Smem &S, uint32_t (&v)[3], int lane, int warp) {
+    uint32_t inc[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        inc[d] = v[d];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(kFull, inc[d], o);
+            if (lane >= o) inc[d] += u;
         }
+        if (lane == 31) S.wscan[warp][d] = inc[d];
     }
-    // Internal nodes' sums are also kept in shared memory, by node id within the segment's
-    // subtree while they fit (every node of a 640-body subtree at leaf size 7), so that the
-    // level above reads them without a round trip through L2.
-    const uint32_t nsets = (want_d ? 1u : 0u) + (want_f ? 1u : 0u);
-    const uint32_t mslots = nsets ? (uint32_t)(kLocalWarps * 128 / 4) / nsets : 0u;
-    for (int L = (int)S.nlvl - 1; L >= 0; --L) {
-        for (uint32_t i = S.lvl_off[L] + threadIdx.x; i < S.lvl_off[L + 1]; i += blockDim.x) {
-            const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
-            const uint32_t lc = cn / 2;
-            double fs[4] = {0.0, 0.0, 0.0, 0.0}, gs[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int side = 0; side < 2; ++side) {
-                const uint32_t cst = side ? st + lc : st;
-                const uint32_t ccn = side ? cn - lc : lc;
-                const uint32_t cid = side ? nid + 1 + t.ttab[lc] : nid + 1;
-                double f[4], g[4];
-                if (ccn <= leaf) {
-                    leaf_sums(S, cst, ccn, o, f, g);
-                    if (want_d) {
-                        store_moments(o.mo, cid, f);
-                        o.recd[cid] = make_noded(f[0], f[1], f[2], f[3], 0.0, s0 + cst, ccn);
-                    }
-                    if (want_f) {
-                        store_moments(o.mof, cid, g);
-                        o.recf[cid] = leaf_nodef(S, cst, ccn, s0, o);
-                    }
-                } else if (cid - root < mslots) {
-                    const double *m = S.mom + 4 * (cid - root) * nsets;
+    __syncthreads();
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        if (want_d) f[q] = m[q];
-                        if (want_f) g[q] = m[(want_d ? 4 : 0) + q];
-                    }
-                } else {
-                    if (want_d) load_moments(o.mo, cid, f);
-                    if (want_f) load_moments(o.mof, cid, g);
-                }
+    for (int d = 0; d < 3; ++d) {
+        uint32_t pre = 0;
+        for (int w = 0; w < warp; ++w) pre += S.wscan[w][d];
+        v[d] = pre + inc[d] - v[d];
+    }
+    __syncthreads();
+}
+
+// Stable sort of the segment's local indices along dimension d by (ordered key, index) into
+// S.lst[0][d].  LSD radix passes of 8 bits over the top 32 of the key bits below the
+// segment's common prefix (all of them when there are at most 32, and the sort is exact);
+// warp w ranks the positions of its chunk in order (the peers of a digit by eight ballots),
+// a digit-major scan over the warps' counts gives every run its offset, and the positions
+// are scattered, ties keeping the index order.  Runs of keys equal in those 32 bits -- values
+// within 2^-32 of the segment's range of each other -- are then ordered by the whole key,
+// each by one thread.
+template <class Smem>
+__device__ void sort_dim(Smem &S, int d, uint32_t c0, unsigned long long kmin,
+                         unsigned long long kmax, int lane, int warp) {
+    const int dbits = kmin == kmax ? 0 : 64 - __clzll((long long)(kmin ^ kmax));
+    const int lsb = dbits > 32 ? dbits - 32 : 0;  // the sorted window is bits [lsb, dbits)
+    const int passes = (dbits - lsb + 7) / 8;
+    // ping-pong so that the last pass writes S.lst[0][d]; the first reads the identity
+    uint16_t *src = (passes & 1) ? S.lst[1][d] : S.lst[0][d];
+    uint16_t *dst = (passes & 1) ? S.lst[0][d] : S.lst[1][d];
+    for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) src[k] = (uint16_t)k;
+    __syncthreads();
+    const uint32_t chunk = ((c0 + kLocalWarps - 1) / kLocalWarps + 31u) & ~31u;
+    const uint32_t w0 = min(c0, (uint32_t)warp * chunk), w1 = min(c0, w0 + chunk);
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int q = 0; q < passes; ++q) {
+        const int shift = lsb + 8 * q;
+        uint32_t *h = S.hist[warp];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (want_d) fs[q] = __dadd_rn(fs[q], f[q]);
-                    if (want_f) gs[q] = __dadd_rn(gs[q], g[q]);
-                }
-            }
-            if (nid - root < mslots) {
-                double *m = S.mom + 4 * (nid - root) * nsets;
+        for (int j = 0; j < 8; ++j) h[lane * 8 + j] = 0u;
+        __syncwarp();
+        for (uint32_t base = w0; base < w1; base += 32) {
+            const uint32_t p = base + lane;
+            const bool valid = p < w1;
+            const uint32_t body = valid ? src[p] : 0u;
+            const uint32_t dg =
+                valid ? (uint32_t)(ord_key(S.xyz[d][body]) >> shift) & 0xffu : 0u;
+            uint32_t peers = __ballot_sync(kFull, valid);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (want_d) m[q] = fs[q];
-                    if (want_f) m[(want_d ? 4 : 0) + q] = gs[q];
-                }
+            for (int b = 0; b < 8; ++b) {
+                const uint32_t bb = __ballot_sync(kFull, (dg >> b) & 1u);
+                peers &= ((dg >> b) & 1u) ? bb : ~bb;
             }
-            const double size =
-                nid - root < (uint32_t)kLocalSizeSlots ? S.nsize[nid - root] : no.size[nid];
-            const uint32_t right = nid + 1 + t.ttab[lc];
-            if (want_d) {
-                store_moments(o.mo, nid, fs);
-                const NodeD q = make_noded(fs[0], fs[1], fs[2], fs[3], size, right, 0u);
-                o.recd[nid] = q;
-                o.recp[nid] = make_nodep(q);
+            uint32_t cnt = 0;
+            if (valid) {
+                cnt = h[dg];
+                S.aux[p] = (uint16_t)(cnt + __popc(peers & lt));
+                S.dig[p] = (uint8_t)dg;
             }
-            if (want_f) {
-                store_moments(o.mof, nid, gs);
-                o.recf[nid] = make_nodef(gs[0], gs[1], gs[2], gs[3], size, right, 0u);
+            __syncwarp();
+            // the highest lane of each run adds the run's size
+            if (valid && (peers >> lane) == 1u) h[dg] = cnt + __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        {   // thread t: offsets of digit t, warp by warp, after every smaller digit
+            const uint32_t t = threadIdx.x;
+            uint32_t tot = 0;
+#pragma unroll
+            for (int w = 0; w < kLocalWarps; ++w) tot += S.hist[w][t];
+            uint32_t inc = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(kFull, inc, o);
+                if (lane >= o) inc += u;
+            }
+            if (lane == 31) S.wscan[warp][3] = inc;
+            __syncthreads();
+            uint32_t run = inc - tot;
+            for (int w = 0; w < warp; ++w) run += S.wscan[w][3];
+#pragma unroll
+            for (int w = 0; w < kLocalWarps; ++w) {
+                const uint32_t c = S.hist[w][t];
+                S.hist[w][t] = run;
+                run += c;
             }
         }
         __syncthreads();
+        for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x)
+            dst[S.hist[p / chunk][S.dig[p]] + S.aux[p]] = src[p];
+        __syncthreads();
+        uint16_t *tmp = src;
+        src = dst;
+        dst = tmp;
     }
-
-    // ================================================================ tree-ordered bodies
-    __syncthreads();  // leaf starts in perm2 (a root leaf has no level barrier above)
-    for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
-        const uint32_t l = S.perm[k];
-        const uint32_t id = S.id[l];
-        const double x = S.xyz[0][l], y = S.xyz[1][l], z = S.xyz[2][l], mm = S.m[l];
-        if (o.tpos) o.tpos[s0 + k] = make_double4_32a(x, y, z, mm);
-        o.tid[s0 + k] = id;
-        {
-            const float hx = (float)x, hy = (float)y, hz = (float)z;
-            const bool hv = is_heavy(id, o.heavy, o.n_heavy);
-            const float fm = hv ? 0.0f : (float)mm;
-            // light mass split hi (thi.w) + lo (tlo.w): the heavy bodies' direct sums read
-            // every light mass back to ~2^-48 relative
-            const float fml = hv ? 0.0f : (float)(mm - (double)fm);
-            o.thi[s0 + k] = make_float4(hx, hy, hz, fm);
-            o.tlo[s0 + k] = make_float4((float)(x - (double)hx), (float)(y - (double)hy),
-                                        (float)(z - (double)hz), fml);
-            if (o.recf) {
-                const uint32_t l0 = S.perm[S.perm2[k]];
-                o.trel[s0 + k] = make_float4((float)(x - S.xyz[0][l0]), (float)(y - S.xyz[1][l0]),
-                                             (float)(z - S.xyz[2][l0]), fm);
+    if (lsb == 0) return;  // every distinguishing bit was sorted on
+    // runs of keys equal in the window, in whole-key order (index order inside a run so far)
+    uint16_t *l = S.lst[0][d];
+    for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x) {
+        const unsigned long long hp = ord_key(S.xyz[d][l[p]]) >> lsb;
+        if (p > 0 && (ord_key(S.xyz[d][l[p - 1]]) >> lsb) == hp) continue;
+        uint32_t e = p + 1;  // the run [p, e)
+        while (e < c0 && (ord_key(S.xyz[d][l[e]]) >> lsb) == hp) ++e;
+        for (uint32_t a2 = p + 1; a2 < e; ++a2) {  // insertion sort by (key, index)
+            const uint16_t v = l[a2];
+            const unsigned long long kv = ord_key(S.xyz[d][v]);
+            uint32_t b2 = a2;
+            while (b2 > p) {
+                const uint16_t u = l[b2 - 1];
+                const unsigned long long ku = ord_key(S.xyz[d][u]);
+                if (ku < kv || (ku == kv && u < v)) break;
+                l[b2] = u;
+                --b2;
             }
+            l[b2] = v;
         }
     }
+    __syncthreads();
+}
+
+template <int kCap>
+__global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
+    Topology t, const uint32_t *roots, NodeOut no, const double *wx, const double *wy,
+    const double *wz, const uint32_t *wid, LocalOut o, uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SortSmem<kCap> &S = *reinterpret_cast<SortSmem<kCap> *>(smem_raw);
+    const uint32_t root = roots[blockIdx.x];
+    const uint32_t s0 = t.start[root], c0 = t.count[root];
+    const uint32_t leaf = t.leaf;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    unsigned long long kmn[3] = {~0ull, ~0ull, ~0ull}, kmx[3] = {0ull, 0ull, 0ull};
+    for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
+        const double x = wx[s0 + k], y = wy[s0 + k], z = wz[s0 + k];
+        S.xyz[0][k] = x;
+        S.xyz[1][k] = y;
+        S.xyz[2][k] = z;
+        const uint32_t id = wid[s0 + k];
+        S.id[k] = id;
+        S.m[k] = o.mass[id];
+        const unsigned long long k0 = ord_key(x), k1 = ord_key(y), k2 = ord_key(z);
+        kmn[0] = min(kmn[0], k0); kmx[0] = max(kmx[0], k0);
+        kmn[1] = min(kmn[1], k1); kmx[1] = max(kmx[1], k1);
+        kmn[2] = min(kmn[2], k2); kmx[2] = max(kmx[2], k2);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        kmn[d] = warp_min(kmn[d]);
+        kmx[d] = warp_max(kmx[d]);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            S.red[warp][d] = kmn[d];
+            S.red[warp][3 + d] = kmx[d];
+        }
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t g0 = c0 > leaf ? 1u : 0u;
+        S.tab_st[0] = 0;
+        S.tab_cn[0] = (uint16_t)c0;
+        S.tab_id[0] = root;
+        S.lvl_off[0] = 0;
+        S.lvl_off[1] = g0;
+        S.nlvl = g0;
+    }
+    __syncthreads();
+
+    if (c0 > leaf) {  // block-uniform
+        // ================================================================ sorted lists
+        for (int d = 0; d < 3; ++d) {
+            unsigned long long a = ~0ull, b = 0ull;
+            for (int w = 0; w < kLocalWarps; ++w) {
+                a = min(a, S.red[w][d]);
+                b = max(b, S.red[w][3 + d]);
+            }
+            sort_dim(S, d, c0, a, b, lane, warp);
+        }
+        // ================================================================ levels
+        int cur = 0;
+        uint32_t plo = 0;  // first table slot of the previous level
+        for (uint32_t L = 0;; ++L) {
+            const uint32_t lo = S.lvl_off[L], hi = S.lvl_off[L + 1];
+            if (hi == lo) break;
+            uint16_t(*Lc)[kCap] = S.lst[cur];
+            uint16_t(*Ln)[kCap] = S.lst[cur ^ 1];
+            // ---- split of every node: bounds from the lists' ends, median at st + cn/2
+            for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+                const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
+                double mn[3], mx[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    mn[d] = S.xyz[d][Lc[d][st]];
+                    mx[d] = S.xyz[d][Lc[d][st + cn - 1]];
+                }
+                uint32_t sd;
+                double size;
+                choose_split(mn, mx, sd, size);
+                const double sv = S.xyz[sd][Lc[sd][st + cn / 2]];
+                no.split_dim[nid] = (uint8_t)sd;
+                no.size[nid] = size;
+                no.split_val[nid] = sv;
+                if (nid - root < (uint32_t)kLocalSizeSlots) S.nsize[nid - root] = size;
+                S.tab_sd[i] = (uint8_t)sd;
+            }
+            __syncthreads();
+            // ---- each position's node (from its parent's node and side); the left bodies
+            // flagged from the split lists
+            for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x) {
+                uint32_t j = 0;
+                if (L > 0) {
+                    const uint32_t jp = S.aux[p];  // node of p one level up
+                    if (jp != kNoNode) {
+                        const uint32_t ip = plo + jp;
+                        const uint32_t side = p >= (uint32_t)S.tab_st[ip] + S.tab_cn[ip] / 2u;
+                        j = S.cslot[2 * jp + side];
+                    } else {
+                        j = kNoNode;
+                    }
+                }
+                S.aux[p] = (uint16_t)j;
+                if (j != kNoNode) {
+                    const uint32_t i = lo + j;
+                    const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], sd = S.tab_sd[i];
+                    S.flag[Lc[sd][p]] = (p - st) < cn / 2 ? 1u : 0u;
+                }
+            }
+            __syncthreads();
+            // ---- stable partition of the lists inside every node: a block scan of the left
+            // flags along each list (zero where a list needs no partition) gives each left
+            // body its rank among the node's left bodies
+            const uint32_t per = (c0 + blockDim.x - 1) / blockDim.x;
+            const uint32_t p0 = min(c0, threadIdx.x * per), p1 = min(c0, p0 + per);
+            // the flags of position p along the three lists, bit d (zero where the list
+            // needs no partition), kept in dig[p]
+            uint32_t e[3] = {0u, 0u, 0u};
+            for (uint32_t p = p0; p < p1; ++p) {
+                const uint32_t j = S.aux[p];
+                uint32_t fb = 0u;
+                if (j != kNoNode) {
+                    const uint32_t sd = S.tab_sd[lo + j];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d)
+                        if ((uint32_t)d != sd) fb |= (uint32_t)S.flag[Lc[d][p]] << d;
+                }
+                S.dig[p] = (uint8_t)fb;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) e[d] += (fb >> d) & 1u;
+            }
+            block_scan3(S, e, lane, warp);
+            {   // the scan value at every node's first position
+                uint32_t r[3] = {e[0], e[1], e[2]};
+                for (uint32_t p = p0; p < p1; ++p) {
+                    const uint32_t j = S.aux[p];
+                    if (j != kNoNode && p == S.tab_st[lo + j]) {
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) S.estart[d][j] = (uint16_t)r[d];
+                    }
+                    const uint32_t fb = S.dig[p];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) r[d] += (fb >> d) & 1u;
+                }
+            }
+            __syncthreads();
+            for (uint32_t p = p0; p < p1; ++p) {
+                const uint32_t j = S.aux[p];
+                const uint32_t fb = S.dig[p];
+                uint32_t st = 0, half = 0, sd = 3;
+                if (j != kNoNode) {
+                    st = S.tab_st[lo + j];
+                    half = S.tab_cn[lo + j] / 2u;
+                    sd = S.tab_sd[lo + j];
+                }
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const uint16_t v = Lc[d][p];
+                    uint32_t q = p;
+                    if (j != kNoNode && (uint32_t)d != sd) {
+                        const uint32_t f = (fb >> d) & 1u;
+                        const uint32_t rl = e[d] - S.estart[d][j];  // left bodies before p
+                        q = f ? st + rl : st + half + (p - st - rl);
+                        e[d] += f;
+                    }
+                    Ln[d][q] = v;
+                }
+            }
+            __syncthreads();
+            cur ^= 1;
+            // ---- children that are still internal, appended as the next level
+            const uint32_t G = hi - lo;
+            uint32_t fill = hi;
+            for (uint32_t base = 0; base < 2 * G; base += blockDim.x) {
+                const uint32_t u = base + threadIdx.x;
+                bool keep = false;
+                uint32_t cst = 0, ccn = 0, cid = 0;
+                if (u < 2 * G) {
+                    const uint32_t i = lo + (u >> 1);
+                    const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], id = S.tab_id[i];
+                    const uint32_t lc = cn / 2;
+                    if (u & 1) {
+                        cst = st + lc;
+                        ccn = cn - lc;
+                        cid = id + 1 + t.ttab[lc];
+                    } else {
+                        cst = st;
+                        ccn = lc;
+                        cid = id + 1;
+                    }
+                    keep = ccn > leaf;
+                }
+                const uint32_t m = __ballot_sync(kFull, keep);
+                if (lane == 0) S.wcnt[warp] = __popc(m);
+                __syncthreads();
+                uint32_t off = fill, tot = 0;
+                for (int q = 0; q < kLocalWarps; ++q) {
+                    if (q < warp) off += S.wcnt[q];
+                    tot += S.wcnt[q];
+                }
+                if (u < 2 * G) {
+                    const uint32_t slot = off + __popc(m & ((1u << lane) - 1u));
+                    S.cslot[u] = keep && slot < (uint32_t)kCap ? (uint16_t)(slot - hi) : kNoNode;
+                    if (keep && slot < (uint32_t)kCap) {
+                        S.tab_st[slot] = (uint16_t)cst;
+                        S.tab_cn[slot] = (uint16_t)ccn;
+                        S.tab_id[slot] = cid;
+                    }
+                }
+                fill += tot;
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) {
+                if (L + 2 > (uint32_t)kLocalLevels || fill > (uint32_t)kCap) {
+                    atomicOr(err, kErrSelect);
+                    fill = hi;  // stop: cannot happen for segments of <= kCap bodies
+                }
+                S.lvl_off[L + 2] = fill;
+                if (fill > hi) S.nlvl = L + 2;
+            }
+            __syncthreads();
+            plo = lo;
+        }
+        // ================================================================ leaf order
+        // every leaf's bodies (the same in all three lists) in index order
+        uint16_t(*Lf)[kCap] = S.lst[cur];
+        const uint32_t nint = S.lvl_off[S.nlvl];
+        for (uint32_t u = threadIdx.x; u < 2 * nint; u += blockDim.x) {
+            const uint32_t i = u >> 1;
+            const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], lc = cn / 2;
+            const uint32_t cst = (u & 1) ? st + lc : st, ccn = (u & 1) ? cn - lc : lc;
+            if (ccn > leaf) continue;
+            for (uint32_t a = 0; a < ccn; ++a) {  // insertion sort of <= leaf entries
+                const uint16_t v = Lf[0][cst + a];
+                uint32_t b = a;
+                while (b > 0 && S.perm[cst + b - 1] > v) {
+                    S.perm[cst + b] = S.perm[cst + b - 1];
+                    --b;
+                }
+                S.perm[cst + b] = v;
+            }
+        }
+    } else {
+        for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) S.perm[k] = (uint16_t)k;
+    }
+    __syncthreads();
+    local_finish(S, t, no, o, root, s0, c0, leaf);
 }
 
 template <int kCap>
@@ -1983,6 +2418,17 @@ static void launch_local_cap(const Topology &t, const uint32_t *roots, uint32_t 
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
                   uint32_t max_count, const NodeOut &no, const Work &w, int cur,
                   const LocalOut &out, uint32_t *err, cudaStream_t st) {
+#if KD_LOCAL_SORTED
+    if (max_count <= (uint32_t)kLocalSmallCap) {
+        // segments of at most kLocalSmallCap bodies: the presorted finish, 4 blocks per SM
+        const size_t smem = sizeof(SortSmem<kLocalSmallCap>);
+        cudaFuncSetAttribute(k_local_sorted<kLocalSmallCap>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_local_sorted<kLocalSmallCap><<<n_roots, kLocalThreads, smem, st>>>(
+            t, roots, no, w.x[cur], w.y[cur], w.z[cur], w.id[cur], out, err);
+        return;
+    }
+#endif
     if (max_count <= (uint32_t)kLocalSmallCap)
         launch_local_cap<kLocalSmallCap>(t, roots, n_roots, no, w, cur, out, err, st);
     else
