@@ -2002,15 +2002,23 @@ struct SortSmem {
     uint32_t id[kCap];
     uint16_t lst[2][3][kCap];  // the three sorted lists; levels alternate between the copies
     uint16_t perm[kCap], perm2[kCap];
-    uint16_t aux[kCap];  // sort: rank within the warp's run of the digit; levels: node of a position
-    uint8_t dig[kCap];   // sort: digit of a position
-    uint8_t flag[kCap];  // levels: body goes to the left child
+    union {
+        struct {                     // sort, per dimension: a position's rank within its
+            uint16_t rank[3][kCap];  // warp's run of its digit, and the digit
+            uint8_t dig[3][kCap];
+        } so;
+        struct {                           // levels
+            uint16_t node[kCap];           // node of a position (slot within the level)
+            uint8_t fb[kCap];              // a position's partition flags, bit d for list d
+            uint8_t flag[kCap];            // body goes to the left child
+            uint16_t estart[3][kCap / 2];  // scan value at each node's first position
+            uint16_t cslot[kCap];          // next-level slot of child 2j + side of node j
+        } lv;
+    };
     union {  // radix counters (sort), then internal nodes' moment sums (bottom-up)
         uint32_t hist[kLocalWarps][256];
         double mom[kLocalWarps * 128];
     };
-    uint16_t estart[3][kCap / 2];  // levels: scan value at each node's first position
-    uint16_t cslot[kCap];          // levels: next-level slot of child 2j + side of node j
     uint32_t tab_id[kCap];
     uint16_t tab_st[kCap], tab_cn[kCap];
     uint8_t tab_sd[kCap];
@@ -2049,108 +2057,132 @@ __device__ __forceinline__ void block_scan3(Smem &S, uint32_t (&v)[3], int lane,
     __syncthreads();
 }
 
-// Stable sort of the segment's local indices along dimension d by (ordered key, index) into
-// S.lst[0][d].  LSD radix passes of 8 bits over the top 32 of the key bits below the
-// segment's common prefix (all of them when there are at most 32, and the sort is exact);
-// warp w ranks the positions of its chunk in order (the peers of a digit by eight ballots),
-// a digit-major scan over the warps' counts gives every run its offset, and the positions
-// are scattered, ties keeping the index order.  Runs of keys equal in those 32 bits -- values
-// within 2^-32 of the segment's range of each other -- are then ordered by the whole key,
-// each by one thread.
+// Stable sorts of the segment's local indices along the three dimensions by (ordered key,
+// index) into S.lst[0][d], side by side: warps 0-2 sort x, 3-5 y, 6-7 z, so that the three
+// sorts share every block barrier.  LSD radix passes of 8 bits over the top 32 of the key
+// bits below the segment's common prefix in that dimension (all of them when there are at
+// most 32, and the sort is exact); each warp ranks the positions of its chunk in order (the
+// peers of a digit by eight ballots), a digit-major scan over the group's counts gives every
+// run its offset, and the positions are scattered, ties keeping the index order.  Runs of keys
+// equal in the sorted window -- values within 2^-32 of the segment's range of each other --
+// are then ordered by the whole key, each by one thread.
 template <class Smem>
-__device__ void sort_dim(Smem &S, int d, uint32_t c0, unsigned long long kmin,
-                         unsigned long long kmax, int lane, int warp) {
-    const int dbits = kmin == kmax ? 0 : 64 - __clzll((long long)(kmin ^ kmax));
-    const int lsb = dbits > 32 ? dbits - 32 : 0;  // the sorted window is bits [lsb, dbits)
-    const int passes = (dbits - lsb + 7) / 8;
-    // ping-pong so that the last pass writes S.lst[0][d]; the first reads the identity
-    uint16_t *src = (passes & 1) ? S.lst[1][d] : S.lst[0][d];
-    uint16_t *dst = (passes & 1) ? S.lst[0][d] : S.lst[1][d];
-    for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) src[k] = (uint16_t)k;
-    __syncthreads();
-    const uint32_t chunk = ((c0 + kLocalWarps - 1) / kLocalWarps + 31u) & ~31u;
-    const uint32_t w0 = min(c0, (uint32_t)warp * chunk), w1 = min(c0, w0 + chunk);
-    const uint32_t lt = (1u << lane) - 1u;
-    for (int q = 0; q < passes; ++q) {
-        const int shift = lsb + 8 * q;
-        uint32_t *h = S.hist[warp];
+__device__ void sort_lists(Smem &S, uint32_t c0, const unsigned long long (&kmin)[3],
+                           const unsigned long long (&kmax)[3], int lane, int warp) {
+    constexpr int kFirst[4] = {0, 3, 6, kLocalWarps};  // warps of dimension d: [kFirst[d], kFirst[d+1])
+    int lsb[3], passes[3], np = 0;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) h[lane * 8 + j] = 0u;
-        __syncwarp();
-        for (uint32_t base = w0; base < w1; base += 32) {
-            const uint32_t p = base + lane;
-            const bool valid = p < w1;
-            const uint32_t body = valid ? src[p] : 0u;
-            const uint32_t dg =
-                valid ? (uint32_t)(ord_key(S.xyz[d][body]) >> shift) & 0xffu : 0u;
-            uint32_t peers = __ballot_sync(kFull, valid);
-#pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                const uint32_t bb = __ballot_sync(kFull, (dg >> b) & 1u);
-                peers &= ((dg >> b) & 1u) ? bb : ~bb;
-            }
-            uint32_t cnt = 0;
-            if (valid) {
-                cnt = h[dg];
-                S.aux[p] = (uint16_t)(cnt + __popc(peers & lt));
-                S.dig[p] = (uint8_t)dg;
-            }
-            __syncwarp();
-            // the highest lane of each run adds the run's size
-            if (valid && (peers >> lane) == 1u) h[dg] = cnt + __popc(peers);
-            __syncwarp();
-        }
-        __syncthreads();
-        {   // thread t: offsets of digit t, warp by warp, after every smaller digit
-            const uint32_t t = threadIdx.x;
-            uint32_t tot = 0;
-#pragma unroll
-            for (int w = 0; w < kLocalWarps; ++w) tot += S.hist[w][t];
-            uint32_t inc = tot;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t u = __shfl_up_sync(kFull, inc, o);
-                if (lane >= o) inc += u;
-            }
-            if (lane == 31) S.wscan[warp][3] = inc;
-            __syncthreads();
-            uint32_t run = inc - tot;
-            for (int w = 0; w < warp; ++w) run += S.wscan[w][3];
-#pragma unroll
-            for (int w = 0; w < kLocalWarps; ++w) {
-                const uint32_t c = S.hist[w][t];
-                S.hist[w][t] = run;
-                run += c;
-            }
-        }
-        __syncthreads();
-        for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x)
-            dst[S.hist[p / chunk][S.dig[p]] + S.aux[p]] = src[p];
-        __syncthreads();
-        uint16_t *tmp = src;
-        src = dst;
-        dst = tmp;
+    for (int d = 0; d < 3; ++d) {
+        const int dbits = kmin[d] == kmax[d] ? 0 : 64 - __clzll((long long)(kmin[d] ^ kmax[d]));
+        lsb[d] = dbits > 32 ? dbits - 32 : 0;  // the sorted window is bits [lsb, dbits)
+        passes[d] = (dbits - lsb[d] + 7) / 8;
+        np = max(np, passes[d]);
+        // ping-pong so that the last pass writes S.lst[0][d]; the first reads the identity
+        uint16_t *src0 = S.lst[passes[d] & 1][d];
+        for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) src0[k] = (uint16_t)k;
     }
-    if (lsb == 0) return;  // every distinguishing bit was sorted on
-    // runs of keys equal in the window, in whole-key order (index order inside a run so far)
-    uint16_t *l = S.lst[0][d];
-    for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x) {
-        const unsigned long long hp = ord_key(S.xyz[d][l[p]]) >> lsb;
-        if (p > 0 && (ord_key(S.xyz[d][l[p - 1]]) >> lsb) == hp) continue;
-        uint32_t e = p + 1;  // the run [p, e)
-        while (e < c0 && (ord_key(S.xyz[d][l[e]]) >> lsb) == hp) ++e;
-        for (uint32_t a2 = p + 1; a2 < e; ++a2) {  // insertion sort by (key, index)
-            const uint16_t v = l[a2];
-            const unsigned long long kv = ord_key(S.xyz[d][v]);
-            uint32_t b2 = a2;
-            while (b2 > p) {
-                const uint16_t u = l[b2 - 1];
-                const unsigned long long ku = ord_key(S.xyz[d][u]);
-                if (ku < kv || (ku == kv && u < v)) break;
-                l[b2] = u;
-                --b2;
+    __syncthreads();
+    // this warp's dimension and its values (selected, not indexed at run time)
+    const int md = warp < kFirst[1] ? 0 : (warp < kFirst[2] ? 1 : 2);
+    const int mfirst = md == 0 ? kFirst[0] : (md == 1 ? kFirst[1] : kFirst[2]);
+    const int mnw = (md == 0 ? kFirst[1] : (md == 1 ? kFirst[2] : kFirst[3])) - mfirst;
+    const int mlsb = md == 0 ? lsb[0] : (md == 1 ? lsb[1] : lsb[2]);
+    const int mpasses = md == 0 ? passes[0] : (md == 1 ? passes[1] : passes[2]);
+    const uint32_t chunk = ((c0 + mnw - 1) / mnw + 31u) & ~31u;
+    const uint32_t w0 = min(c0, (uint32_t)(warp - mfirst) * chunk), w1 = min(c0, w0 + chunk);
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int q = 0; q < np; ++q) {
+        if (q < mpasses) {  // warp-uniform
+            const int shift = mlsb + 8 * q;
+            const uint16_t *src = S.lst[(mpasses - q) & 1][md];
+            uint32_t *h = S.hist[warp];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) h[lane * 8 + j] = 0u;
+            __syncwarp();
+            for (uint32_t base = w0; base < w1; base += 32) {
+                const uint32_t p = base + lane;
+                const bool valid = p < w1;
+                const uint32_t body = valid ? src[p] : 0u;
+                const uint32_t dg =
+                    valid ? (uint32_t)(ord_key(S.xyz[md][body]) >> shift) & 0xffu : 0u;
+                uint32_t peers = __ballot_sync(kFull, valid);
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    const uint32_t bb = __ballot_sync(kFull, (dg >> b) & 1u);
+                    peers &= ((dg >> b) & 1u) ? bb : ~bb;
+                }
+                uint32_t cnt = 0;
+                if (valid) {
+                    cnt = h[dg];
+                    S.so.rank[md][p] = (uint16_t)(cnt + __popc(peers & lt));
+                    S.so.dig[md][p] = (uint8_t)dg;
+                }
+                __syncwarp();
+                // the highest lane of each run adds the run's size
+                if (valid && (peers >> lane) == 1u) h[dg] = cnt + __popc(peers);
+                __syncwarp();
             }
-            l[b2] = v;
+        }
+        __syncthreads();
+        {   // thread t: offsets of digit t in each dimension, warp by warp, after every
+            // smaller digit
+            const uint32_t t = threadIdx.x;
+            uint32_t v[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                v[d] = 0u;
+                if (q < passes[d])
+                    for (int w = kFirst[d]; w < kFirst[d + 1]; ++w) v[d] += S.hist[w][t];
+            }
+            block_scan3(S, v, lane, warp);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (q >= passes[d]) continue;
+                uint32_t run = v[d];
+                for (int w = kFirst[d]; w < kFirst[d + 1]; ++w) {
+                    const uint32_t c = S.hist[w][t];
+                    S.hist[w][t] = run;
+                    run += c;
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (q >= passes[d]) continue;
+            const uint16_t *src = S.lst[(passes[d] - q) & 1][d];
+            uint16_t *dst = S.lst[(passes[d] - q - 1) & 1][d];
+            const uint32_t cd = ((c0 + (kFirst[d + 1] - kFirst[d]) - 1) /
+                                     (uint32_t)(kFirst[d + 1] - kFirst[d]) + 31u) & ~31u;
+            for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x)
+                dst[S.hist[kFirst[d] + p / cd][S.so.dig[d][p]] + S.so.rank[d][p]] = src[p];
+        }
+        __syncthreads();
+    }
+    // runs of keys equal in the window, in whole-key order (index order inside a run so far)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (lsb[d] == 0) continue;  // every distinguishing bit was sorted on
+        uint16_t *l = S.lst[0][d];
+        const int sh = lsb[d];
+        for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x) {
+            const unsigned long long hp = ord_key(S.xyz[d][l[p]]) >> sh;
+            if (p > 0 && (ord_key(S.xyz[d][l[p - 1]]) >> sh) == hp) continue;
+            uint32_t e = p + 1;  // the run [p, e)
+            while (e < c0 && (ord_key(S.xyz[d][l[e]]) >> sh) == hp) ++e;
+            for (uint32_t a2 = p + 1; a2 < e; ++a2) {  // insertion sort by (key, index)
+                const uint16_t v = l[a2];
+                const unsigned long long kv = ord_key(S.xyz[d][v]);
+                uint32_t b2 = a2;
+                while (b2 > p) {
+                    const uint16_t u = l[b2 - 1];
+                    const unsigned long long ku = ord_key(S.xyz[d][u]);
+                    if (ku < kv || (ku == kv && u < v)) break;
+                    l[b2] = u;
+                    --b2;
+                }
+                l[b2] = v;
+            }
         }
     }
     __syncthreads();
@@ -2206,14 +2238,17 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
 
     if (c0 > leaf) {  // block-uniform
         // ================================================================ sorted lists
+        unsigned long long a[3], b[3];
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
-            unsigned long long a = ~0ull, b = 0ull;
+            a[d] = ~0ull;
+            b[d] = 0ull;
             for (int w = 0; w < kLocalWarps; ++w) {
-                a = min(a, S.red[w][d]);
-                b = max(b, S.red[w][3 + d]);
+                a[d] = min(a[d], S.red[w][d]);
+                b[d] = max(b[d], S.red[w][3 + d]);
             }
-            sort_dim(S, d, c0, a, b, lane, warp);
         }
+        sort_lists(S, c0, a, b, lane, warp);
         // ================================================================ levels
         int cur = 0;
         uint32_t plo = 0;  // first table slot of the previous level
@@ -2247,20 +2282,22 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
             for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x) {
                 uint32_t j = 0;
                 if (L > 0) {
-                    const uint32_t jp = S.aux[p];  // node of p one level up
+                    const uint32_t jp = S.lv.node[p];  // node of p one level up
                     if (jp != kNoNode) {
                         const uint32_t ip = plo + jp;
                         const uint32_t side = p >= (uint32_t)S.tab_st[ip] + S.tab_cn[ip] / 2u;
-                        j = S.cslot[2 * jp + side];
+                        j = S.lv.cslot[2 * jp + side];
                     } else {
                         j = kNoNode;
                     }
                 }
-                S.aux[p] = (uint16_t)j;
+                S.lv.node[p] = (uint16_t)j;
                 if (j != kNoNode) {
                     const uint32_t i = lo + j;
                     const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], sd = S.tab_sd[i];
-                    S.flag[Lc[sd][p]] = (p - st) < cn / 2 ? 1u : 0u;
+                    // a node whose children are both leaves keeps its lists unpartitioned:
+                    // its leaves are read from its split dimension's list
+                    if (cn > 2u * leaf) S.lv.flag[Lc[sd][p]] = (p - st) < cn / 2 ? 1u : 0u;
                 }
             }
             __syncthreads();
@@ -2273,15 +2310,15 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
             // needs no partition), kept in dig[p]
             uint32_t e[3] = {0u, 0u, 0u};
             for (uint32_t p = p0; p < p1; ++p) {
-                const uint32_t j = S.aux[p];
+                const uint32_t j = S.lv.node[p];
                 uint32_t fb = 0u;
-                if (j != kNoNode) {
+                if (j != kNoNode && S.tab_cn[lo + j] > 2u * leaf) {
                     const uint32_t sd = S.tab_sd[lo + j];
 #pragma unroll
                     for (int d = 0; d < 3; ++d)
-                        if ((uint32_t)d != sd) fb |= (uint32_t)S.flag[Lc[d][p]] << d;
+                        if ((uint32_t)d != sd) fb |= (uint32_t)S.lv.flag[Lc[d][p]] << d;
                 }
-                S.dig[p] = (uint8_t)fb;
+                S.lv.fb[p] = (uint8_t)fb;
 #pragma unroll
                 for (int d = 0; d < 3; ++d) e[d] += (fb >> d) & 1u;
             }
@@ -2289,22 +2326,23 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
             {   // the scan value at every node's first position
                 uint32_t r[3] = {e[0], e[1], e[2]};
                 for (uint32_t p = p0; p < p1; ++p) {
-                    const uint32_t j = S.aux[p];
+                    const uint32_t j = S.lv.node[p];
                     if (j != kNoNode && p == S.tab_st[lo + j]) {
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) S.estart[d][j] = (uint16_t)r[d];
+                        for (int d = 0; d < 3; ++d) S.lv.estart[d][j] = (uint16_t)r[d];
                     }
-                    const uint32_t fb = S.dig[p];
+                    const uint32_t fb = S.lv.fb[p];
 #pragma unroll
                     for (int d = 0; d < 3; ++d) r[d] += (fb >> d) & 1u;
                 }
             }
             __syncthreads();
             for (uint32_t p = p0; p < p1; ++p) {
-                const uint32_t j = S.aux[p];
-                const uint32_t fb = S.dig[p];
+                const uint32_t j = S.lv.node[p];
+                const uint32_t fb = S.lv.fb[p];
                 uint32_t st = 0, half = 0, sd = 3;
-                if (j != kNoNode) {
+                const bool part = j != kNoNode && S.tab_cn[lo + j] > 2u * leaf;
+                if (part) {
                     st = S.tab_st[lo + j];
                     half = S.tab_cn[lo + j] / 2u;
                     sd = S.tab_sd[lo + j];
@@ -2313,9 +2351,9 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
                 for (int d = 0; d < 3; ++d) {
                     const uint16_t v = Lc[d][p];
                     uint32_t q = p;
-                    if (j != kNoNode && (uint32_t)d != sd) {
+                    if (part && (uint32_t)d != sd) {
                         const uint32_t f = (fb >> d) & 1u;
-                        const uint32_t rl = e[d] - S.estart[d][j];  // left bodies before p
+                        const uint32_t rl = e[d] - S.lv.estart[d][j];  // left bodies before p
                         q = f ? st + rl : st + half + (p - st - rl);
                         e[d] += f;
                     }
@@ -2356,7 +2394,7 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
                 }
                 if (u < 2 * G) {
                     const uint32_t slot = off + __popc(m & ((1u << lane) - 1u));
-                    S.cslot[u] = keep && slot < (uint32_t)kCap ? (uint16_t)(slot - hi) : kNoNode;
+                    S.lv.cslot[u] = keep && slot < (uint32_t)kCap ? (uint16_t)(slot - hi) : kNoNode;
                     if (keep && slot < (uint32_t)kCap) {
                         S.tab_st[slot] = (uint16_t)cst;
                         S.tab_cn[slot] = (uint16_t)ccn;
@@ -2386,8 +2424,10 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
             const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], lc = cn / 2;
             const uint32_t cst = (u & 1) ? st + lc : st, ccn = (u & 1) ? cn - lc : lc;
             if (ccn > leaf) continue;
+            // a parent with two leaves left its other lists unpartitioned
+            const uint16_t *lf = cn > 2u * leaf ? Lf[0] : Lf[S.tab_sd[i]];
             for (uint32_t a = 0; a < ccn; ++a) {  // insertion sort of <= leaf entries
-                const uint16_t v = Lf[0][cst + a];
+                const uint16_t v = lf[cst + a];
                 uint32_t b = a;
                 while (b > 0 && S.perm[cst + b - 1] > v) {
                     S.perm[cst + b] = S.perm[cst + b - 1];
