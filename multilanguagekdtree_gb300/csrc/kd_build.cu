@@ -1540,7 +1540,37 @@ __device__ __forceinline__ void local_finish(Smem &S, const Topology &t, const N
                                              const LocalOut &o, uint32_t root, uint32_t s0,
                                              uint32_t c0, uint32_t leaf) {
     // ================================================================ bottom-up moments
+    // Three phases: every leaf at once (sums, records), the internal nodes' sums level by
+    // level from the deepest (left + right), then every internal node's record at once.
     const bool want_d = o.recd != nullptr, want_f = o.recf != nullptr;
+    // Node sums are also kept in shared memory, by node id within the segment's subtree
+    // while they fit (every node of a 640-body subtree at leaf size 7), so that the phases
+    // read them without a round trip through L2.
+    const uint32_t nsets = (want_d ? 1u : 0u) + (want_f ? 1u : 0u);
+    const uint32_t mslots = nsets ? (uint32_t)(kLocalWarps * 128 / 4) / nsets : 0u;
+    auto keep_sums = [&](uint32_t id, const double f[4], const double g[4]) {
+        if (id - root >= mslots) return;
+        double *m = S.mom + 4 * (id - root) * nsets;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (want_d) m[q] = f[q];
+            if (want_f) m[(want_d ? 4 : 0) + q] = g[q];
+        }
+    };
+    auto read_sums = [&](uint32_t id, double f[4], double g[4]) {
+        if (id - root < mslots) {
+            const double *m = S.mom + 4 * (id - root) * nsets;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (want_d) f[q] = m[q];
+                if (want_f) g[q] = m[(want_d ? 4 : 0) + q];
+            }
+        } else {
+            if (want_d) load_moments(o.mo, id, f);
+            if (want_f) load_moments(o.mof, id, g);
+        }
+    };
+    const uint32_t nint = S.lvl_off[S.nlvl];  // internal nodes (table slots [0, nint))
     if (c0 <= leaf) {
         if (threadIdx.x == 0) {
             double f[4], g[4];
@@ -1555,71 +1585,63 @@ __device__ __forceinline__ void local_finish(Smem &S, const Topology &t, const N
             }
         }
     }
-    // Internal nodes' sums are also kept in shared memory, by node id within the segment's
-    // subtree while they fit (every node of a 640-body subtree at leaf size 7), so that the
-    // level above reads them without a round trip through L2.
-    const uint32_t nsets = (want_d ? 1u : 0u) + (want_f ? 1u : 0u);
-    const uint32_t mslots = nsets ? (uint32_t)(kLocalWarps * 128 / 4) / nsets : 0u;
+    // ---- leaves: the children of internal nodes with at most `leaf` bodies
+    for (uint32_t u = threadIdx.x; u < 2 * nint; u += blockDim.x) {
+        const uint32_t i = u >> 1;
+        const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
+        const uint32_t lc = cn / 2;
+        const uint32_t cst = (u & 1) ? st + lc : st, ccn = (u & 1) ? cn - lc : lc;
+        if (ccn > leaf) continue;
+        const uint32_t cid = (u & 1) ? nid + 1 + t.ttab[lc] : nid + 1;
+        double f[4], g[4];
+        leaf_sums(S, cst, ccn, o, f, g);
+        if (want_d) {
+            store_moments(o.mo, cid, f);
+            o.recd[cid] = make_noded(f[0], f[1], f[2], f[3], 0.0, s0 + cst, ccn);
+        }
+        if (want_f) {
+            store_moments(o.mof, cid, g);
+            o.recf[cid] = leaf_nodef(S, cst, ccn, s0, o);
+        }
+        keep_sums(cid, f, g);
+    }
+    __syncthreads();
+    // ---- internal nodes' sums, deepest level first
     for (int L = (int)S.nlvl - 1; L >= 0; --L) {
         for (uint32_t i = S.lvl_off[L] + threadIdx.x; i < S.lvl_off[L + 1]; i += blockDim.x) {
-            const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
+            const uint32_t cn = S.tab_cn[i], nid = S.tab_id[i];
             const uint32_t lc = cn / 2;
             double fs[4] = {0.0, 0.0, 0.0, 0.0}, gs[4] = {0.0, 0.0, 0.0, 0.0};
             for (int side = 0; side < 2; ++side) {
-                const uint32_t cst = side ? st + lc : st;
-                const uint32_t ccn = side ? cn - lc : lc;
                 const uint32_t cid = side ? nid + 1 + t.ttab[lc] : nid + 1;
                 double f[4], g[4];
-                if (ccn <= leaf) {
-                    leaf_sums(S, cst, ccn, o, f, g);
-                    if (want_d) {
-                        store_moments(o.mo, cid, f);
-                        o.recd[cid] = make_noded(f[0], f[1], f[2], f[3], 0.0, s0 + cst, ccn);
-                    }
-                    if (want_f) {
-                        store_moments(o.mof, cid, g);
-                        o.recf[cid] = leaf_nodef(S, cst, ccn, s0, o);
-                    }
-                } else if (cid - root < mslots) {
-                    const double *m = S.mom + 4 * (cid - root) * nsets;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        if (want_d) f[q] = m[q];
-                        if (want_f) g[q] = m[(want_d ? 4 : 0) + q];
-                    }
-                } else {
-                    if (want_d) load_moments(o.mo, cid, f);
-                    if (want_f) load_moments(o.mof, cid, g);
-                }
+                read_sums(cid, f, g);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     if (want_d) fs[q] = __dadd_rn(fs[q], f[q]);
                     if (want_f) gs[q] = __dadd_rn(gs[q], g[q]);
                 }
             }
-            if (nid - root < mslots) {
-                double *m = S.mom + 4 * (nid - root) * nsets;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (want_d) m[q] = fs[q];
-                    if (want_f) m[(want_d ? 4 : 0) + q] = gs[q];
-                }
-            }
-            const double size =
-                nid - root < (uint32_t)kLocalSizeSlots ? S.nsize[nid - root] : no.size[nid];
-            const uint32_t right = nid + 1 + t.ttab[lc];
-            if (want_d) {
-                store_moments(o.mo, nid, fs);
-                const NodeD q = make_noded(fs[0], fs[1], fs[2], fs[3], size, right, 0u);
-                o.recd[nid] = q;
-                o.recp[nid] = make_nodep(q);
-            }
-            if (want_f) {
-                store_moments(o.mof, nid, gs);
-                o.recf[nid] = make_nodef(gs[0], gs[1], gs[2], gs[3], size, right, 0u);
-            }
+            if (want_d) store_moments(o.mo, nid, fs);
+            if (want_f) store_moments(o.mof, nid, gs);
+            keep_sums(nid, fs, gs);
         }
         __syncthreads();
+    }
+    // ---- internal nodes' records
+    for (uint32_t i = threadIdx.x; i < nint; i += blockDim.x) {
+        const uint32_t cn = S.tab_cn[i], nid = S.tab_id[i];
+        double fs[4], gs[4];
+        read_sums(nid, fs, gs);
+        const double size =
+            nid - root < (uint32_t)kLocalSizeSlots ? S.nsize[nid - root] : no.size[nid];
+        const uint32_t right = nid + 1 + t.ttab[cn / 2];
+        if (want_d) {
+            const NodeD q = make_noded(fs[0], fs[1], fs[2], fs[3], size, right, 0u);
+            o.recd[nid] = q;
+            o.recp[nid] = make_nodep(q);
+        }
+        if (want_f) o.recf[nid] = make_nodef(gs[0], gs[1], gs[2], gs[3], size, right, 0u);
     }
 
     // ================================================================ tree-ordered bodies
