@@ -18,8 +18,8 @@
 // (bounding box -> split -> exact median select -> stable partition into the other
 // ping-pong buffer, which also reduces the children's bounding boxes); below that, one
 // thread block takes a whole segment into shared memory and finishes its subtree there
-// (one warp or a team of warps per node: radix select, ballot partition; nodes of at most
-// 32 bodies in one warp's registers).
+// (per-dimension sorted lists: bounds and medians read off the lists, one segmented stable
+// partition of the lists per level).
 #include "kd_internal.cuh"
 
 namespace kd {
@@ -1089,70 +1089,10 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
 }
 
 // ------------------------------------------------------------------ local subtree finish
-//
-// One thread block owns a segment of at most kLocalMax bodies and builds its whole subtree
-// in shared memory.  Per level, every internal sub-segment of more than 32 bodies is
-// handled by one warp -- by a team of 2, 4 or 8 warps meeting at a named barrier when the
-// level has fewer sub-segments than the block has warps -- with no block barrier inside the
-// level:
-//   1. bounding box -> split_dim, size (choose_split);
-//   2. exact rank-len/2 select on (key, body id): 8-bit radix passes over the team's
-//      histogram, narrowing the candidate set until at most 32 remain, then a 32-lane
-//      rank by comparison;
-//   3. stable partition of the sub-segment's index list around the median.
-// A sub-segment of at most 32 bodies finishes its whole subtree in one warp's registers.
-// A block barrier separates levels (the next level's sub-segment table); then the node sums
-// and records are formed bottom-up, level by level.
 
 constexpr int kLocalWarps = kLocalThreads / 32;
 constexpr int kLocalLevels = 16;
 constexpr int kLocalSizeSlots = 256;
-#ifndef KD_LOCAL_SORTED
-#define KD_LOCAL_SORTED 1
-#endif
-
-// Shared memory of one block, for segments of at most kCap bodies.  The kernel is built for
-// two capacities: kLocalMax, and kLocalSmallCap for trees whose local segments are all at
-// most that big (at 1e7 and 2e7 bodies they hold ~610): ~44 KB instead of ~62 KB, so four
-// blocks share an SM instead of three.
-template <int kCap>
-struct LocalSmem {
-    double xyz[3][kCap];  // positions, one row per dimension
-    double m[kCap];
-    uint32_t id[kCap];
-    union {  // radix histograms (top-down), then internal nodes' moment sums (bottom-up)
-        uint32_t hist[kLocalWarps][256];
-        double mom[kLocalWarps * 128];
-    };
-    unsigned long long ckey[kLocalWarps][32];
-    uint32_t cid[kLocalWarps][32];
-    // internal sub-segments of every level, appended level after level
-    uint32_t tab_id[kCap];
-    uint16_t tab_st[kCap], tab_cn[kCap], tab_pcn[kCap];
-    uint16_t perm[kCap], perm2[kCap];
-    uint16_t clid[kLocalWarps][32];
-    uint32_t lvl_off[kLocalLevels + 1];
-    uint32_t nlvl;
-    uint32_t wcnt[kLocalWarps];
-    // node sizes by node id within the segment's subtree (for the bottom-up records)
-    double nsize[kLocalSizeSlots];
-    // teams of warps on one node: per-warp bounds and left counts, per-team candidate count
-    unsigned long long bb[kLocalWarps][6];
-    uint32_t wl[kLocalWarps];
-    uint32_t tcnt[kLocalWarps];
-};
-constexpr int kLocalSmallCap = 640;
-
-// Barrier of a team of W warps (warps team*W .. team*W+W-1): named barrier 1+team over its
-// 32*W threads, or the warp's own sync for a one-warp team.
-__device__ __forceinline__ void team_sync(uint32_t team, uint32_t W) {
-    if (W == 1) {
-        __syncwarp();
-    } else {
-        asm volatile("barrier.sync %0, %1;" ::"r"(1u + team), "r"(32u * W) : "memory");
-    }
-}
-
 // Candidate filter of the radix select: the top `kb` bits of the key and the top `ib` bits of
 // the id are fixed to kp / ip.
 struct RadixState {
@@ -1373,11 +1313,6 @@ __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
     }
 }
 
-template <class Smem>
-__device__ __forceinline__ double coord(const Smem &S, uint32_t sd, uint32_t l) {
-    return S.xyz[sd][l];
-}
-
 // Mixed leaf record: origin o = position of the leaf's first body, as hi + lo floats.  The
 // leaf's first position is noted in perm2 for every body of the leaf, whose offset from o
 // goes to trel with the tree-ordered bodies.
@@ -1437,104 +1372,8 @@ __device__ __forceinline__ void load_moments(const Moments &mo, uint32_t id, dou
     v[3] = mo.S[3 * (size_t)id + 2];
 }
 
-// Whole subtree of a node of cn <= 32 bodies (tree positions [st, st+cn) of the block) in
-// one warp: lane k holds one body; its rank among the cn bodies in each dimension, by
-// (ordered key, id) as the exact select orders them, is counted once.  Then every internal
-// node of the subtree takes O(1) warp instructions: bounding box from the lanes of minimum
-// and maximum rank, split by choose_split, median = the member of rank-order position c/2
-// (the (c/2+1)-th set bit of the members' rank mask), and the new tree positions are the
-// members' positions in rank order of the split dimension (the left half below the median,
-// as the exact select and partition of the larger nodes give).  Writes split_dim, size,
-// split_val of the internal nodes and the subtree's final order into perm.
-template <class Smem>
-__device__ __forceinline__ void small_subtree(Smem &S, const Topology &t, const NodeOut &no,
-                                           uint32_t st, uint32_t cn, uint32_t nid,
-                                           uint32_t root, uint32_t leaf, int lane,
-                                           uint32_t *err) {
-    const bool valid = (uint32_t)lane < cn;
-    const uint32_t l = valid ? S.perm[st + lane] : 0u;
-    const double c[3] = {S.xyz[0][l], S.xyz[1][l], S.xyz[2][l]};
-    const unsigned long long k[3] = {ord_key(c[0]), ord_key(c[1]), ord_key(c[2])};
-    const uint32_t id = S.id[l];
-    uint32_t rank[3] = {0u, 0u, 0u};
-    for (uint32_t j = 0; j < cn; ++j) {
-        const uint32_t idj = __shfl_sync(kFull, id, j);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const unsigned long long kj = __shfl_sync(kFull, k[d], j);
-            rank[d] += (kj < k[d] || (kj == k[d] && idj < id)) ? 1u : 0u;
-        }
-    }
-    uint32_t pos = (uint32_t)lane;  // position in the subtree
-    // stack of internal nodes still to split, entry q in lane q: (first position, count, id)
-    uint32_t ss = 0u, sc = cn, si = nid;
-    int sp = cn > leaf ? 1 : 0;
-    while (sp > 0) {
-        --sp;
-        const uint32_t ns = __shfl_sync(kFull, ss, sp), nc = __shfl_sync(kFull, sc, sp),
-                       ni = __shfl_sync(kFull, si, sp);
-        const bool mem = valid && pos >= ns && pos < ns + nc;
-        double mn[3], mx[3];
-        uint32_t sel[3] = {0u, 0u, 0u};
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const uint32_t rlo = __reduce_min_sync(kFull, mem ? rank[d] : 0xffffffffu);
-            const uint32_t rhi = __reduce_max_sync(kFull, mem ? rank[d] : 0u);
-            const int llo = __ffs(__ballot_sync(kFull, mem && rank[d] == rlo)) - 1;
-            const int lhi = __ffs(__ballot_sync(kFull, mem && rank[d] == rhi)) - 1;
-            mn[d] = ord_val(__shfl_sync(kFull, k[d], llo));
-            mx[d] = ord_val(__shfl_sync(kFull, k[d], lhi));
-            sel[d] = __reduce_or_sync(kFull, mem ? (1u << rank[d]) : 0u);
-        }
-        uint32_t sd;
-        double size;
-        choose_split(mn, mx, sd, size);
-        const uint32_t B = sd == 0 ? sel[0] : (sd == 1 ? sel[1] : sel[2]);
-        const uint32_t rs = sd == 0 ? rank[0] : (sd == 1 ? rank[1] : rank[2]);
-        const uint32_t half = nc / 2;
-        // members ranked below this lane's body; the median is the member with exactly
-        // `half` below it.  Distinct ranks (one bit of B per member) are checked here.
-        const uint32_t below = mem ? (uint32_t)__popc(B & ((1u << rs) - 1u)) : 0u;
-        const int ml = __ffs(__ballot_sync(kFull, mem && below == half)) - 1;
-        if (ml < 0 || (uint32_t)__popc(B) != nc) {
-            if (lane == 0) atomicOr(err, kErrSelect);
-            break;
-        }
-        const double cs = sd == 0 ? c[0] : (sd == 1 ? c[1] : c[2]);
-        const double sv = __shfl_sync(kFull, cs, ml);
-        if (lane == 0) {
-            no.split_dim[ni] = (uint8_t)sd;
-            no.size[ni] = size;
-            no.split_val[ni] = sv;
-            if (ni - root < (uint32_t)kLocalSizeSlots) S.nsize[ni - root] = size;
-        }
-        // members in rank order of the split dimension: the left half lies below the median
-        if (mem) pos = ns + below;
-        const uint32_t rc = nc - half;
-        if (rc > leaf) {  // at most one pending entry per depth: sp stays below 32
-            if (lane == sp) {
-                ss = ns + half;
-                sc = rc;
-                si = ni + 1u + t.ttab[half];
-            }
-            ++sp;
-        }
-        if (half > leaf) {
-            if (lane == sp) {
-                ss = ns;
-                sc = half;
-                si = ni + 1u;
-            }
-            ++sp;
-        }
-    }
-    __syncwarp();
-    if (valid) S.perm[st + pos] = (uint16_t)l;
-    __syncwarp();
-}
-
 // The bottom-up pass and the tree-ordered outputs of a finished segment: its bodies in tree
-// order in perm, its internal nodes in the level table (shared by both subtree finishes).
+// order in perm, its internal nodes in the level table.
 template <class Smem>
 __device__ __forceinline__ void local_finish(Smem &S, const Topology &t, const NodeOut &no,
                                              const LocalOut &o, uint32_t root, uint32_t s0,
@@ -1671,354 +1510,21 @@ __device__ __forceinline__ void local_finish(Smem &S, const Topology &t, const N
     }
 }
 
+// One thread block owns a segment of at most kLocalMax bodies and builds its whole subtree
+// in shared memory from three sorted lists.  The segment's bodies are sorted once along each
+// dimension by (ordered key, local index) -- the local index orders bodies as their ids do,
+// since every partition above was stable -- with a stable block radix sort of 16-bit
+// indices over the key bits below the segment's common prefix.  Each node then owns the same
+// range [st, st + cn) of all three lists, each sorted along its dimension: its bounding box
+// is the lists' first and last entries, its median the entry st + cn/2 of the split
+// dimension's list, whose first half is the left child (the exact rank-len/2 median on
+// (coordinate, body id)).  A level flags its nodes' left bodies and partitions the other two
+// lists stably within every node at once (one block scan per level), so a level costs the
+// same few passes over the segment whatever the size and number of its nodes.  At the end
+// each leaf's bodies are put in index order, and the node sums and records are formed
+// bottom-up.
 template <int kCap>
-__global__ __launch_bounds__(kLocalThreads, kCap <= kLocalSmallCap ? 4 : 3) void k_local(
-    Topology t, const uint32_t *roots,
-                                                         NodeOut no, const double *wx,
-                                                         const double *wy, const double *wz,
-                                                         const uint32_t *wid, LocalOut o,
-                                                         uint32_t *err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    LocalSmem<kCap> &S = *reinterpret_cast<LocalSmem<kCap> *>(smem_raw);
-    const uint32_t root = roots[blockIdx.x];
-    const uint32_t s0 = t.start[root], c0 = t.count[root];
-    const uint32_t leaf = t.leaf;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t lt = (1u << lane) - 1u;
-
-    for (uint32_t k = threadIdx.x; k < c0; k += blockDim.x) {
-        S.xyz[0][k] = wx[s0 + k];
-        S.xyz[1][k] = wy[s0 + k];
-        S.xyz[2][k] = wz[s0 + k];
-        const uint32_t id = wid[s0 + k];
-        S.id[k] = id;
-        S.m[k] = o.mass[id];
-        S.perm[k] = (uint16_t)k;
-    }
-    if (threadIdx.x == 0) {
-        const uint32_t g0 = c0 > leaf ? 1u : 0u;
-        S.tab_st[0] = 0;
-        S.tab_cn[0] = (uint16_t)c0;
-        S.tab_pcn[0] = 0xffffu;
-        S.tab_id[0] = root;
-        S.lvl_off[0] = 0;
-        S.lvl_off[1] = g0;
-        S.nlvl = g0;
-    }
-    __syncthreads();
-
-    // ================================================================ top-down split
-    for (uint32_t L = 0;; ++L) {
-        const uint32_t lo = S.lvl_off[L], hi = S.lvl_off[L + 1];
-        if (hi == lo) break;
-        // Levels with fewer nodes than warps give each node a team of W warps (W = 8, 4, 2
-        // at 1, 2, 3-4 nodes), which splits the node's passes and meets at a named barrier;
-        // deeper levels run one warp per node.
-        const uint32_t G = hi - lo;
-        uint32_t W = 1;
-        while (2u * W * G <= (uint32_t)kLocalWarps) W *= 2u;
-        const uint32_t team = (uint32_t)warp / W, tw = (uint32_t)warp % W;
-        const uint32_t lead = team * W;  // the team's first warp: its buffers are the team's
-        const uint32_t tstep = 32u * W, ttid = tw * 32u + (uint32_t)lane;
-        for (uint32_t i = lo + team; i < hi; i += (uint32_t)kLocalWarps / W) {
-            const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], nid = S.tab_id[i];
-            if (cn <= 32u) {
-                // the whole subtree of a node of <= 32 bodies in one warp's registers; its
-                // descendants (parent also <= 32) were done with it
-                if (tw == 0 && S.tab_pcn[i] > 32u)
-                    small_subtree(S, t, no, st, cn, nid, root, leaf, lane, err);
-                continue;
-            }
-            // ---- 1. bounding box and split
-            unsigned long long kmn[3] = {~0ull, ~0ull, ~0ull}, kmx[3] = {0ull, 0ull, 0ull};
-            for (uint32_t k = ttid; k < cn; k += tstep) {
-                const uint32_t l = S.perm[st + k];
-                const unsigned long long k0 = ord_key(S.xyz[0][l]), k1 = ord_key(S.xyz[1][l]),
-                                         k2 = ord_key(S.xyz[2][l]);
-                kmn[0] = min(kmn[0], k0); kmx[0] = max(kmx[0], k0);
-                kmn[1] = min(kmn[1], k1); kmx[1] = max(kmx[1], k1);
-                kmn[2] = min(kmn[2], k2); kmx[2] = max(kmx[2], k2);
-            }
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                kmn[d] = warp_min(kmn[d]);
-                kmx[d] = warp_max(kmx[d]);
-            }
-            if (W > 1) {
-                if (lane == 0) {
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        S.bb[warp][d] = kmn[d];
-                        S.bb[warp][3 + d] = kmx[d];
-                    }
-                }
-                if (ttid == 0) S.tcnt[team] = 0u;  // candidate count of the gather below
-                team_sync(team, W);
-                for (uint32_t q = 0; q < W; ++q) {
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        kmn[d] = min(kmn[d], S.bb[lead + q][d]);
-                        kmx[d] = max(kmx[d], S.bb[lead + q][3 + d]);
-                    }
-                }
-            }
-            double mn[3], mx[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                mn[d] = ord_val(kmn[d]);
-                mx[d] = ord_val(kmx[d]);
-            }
-            uint32_t sd;
-            double size;
-            choose_split(mn, mx, sd, size);
-            if (ttid == 0) {
-                no.split_dim[nid] = (uint8_t)sd;
-                no.size[nid] = size;
-                if (nid - root < (uint32_t)kLocalSizeSlots) S.nsize[nid - root] = size;
-            }
-            // ---- 2. exact select of rank cn/2
-            uint32_t r = cn / 2, ccount = cn;
-            RadixState rs;
-            {
-                const unsigned long long kmin = sd == 0 ? kmn[0] : (sd == 1 ? kmn[1] : kmn[2]);
-                const unsigned long long kmax = sd == 0 ? kmx[0] : (sd == 1 ? kmx[1] : kmx[2]);
-                rs.kb = __clzll((long long)(kmin ^ kmax));
-                rs.kp = rs.kb == 0 ? 0ull : (rs.kb == 64 ? kmin : (kmin >> (64 - rs.kb)));
-                rs.ib = 0;
-                rs.ip = 0;
-            }
-            // a team alternates between its first two warps' histograms, so that clearing the
-            // next pass's never races with the reads of this pass's
-            uint32_t pass = 0;
-            while (ccount > 32) {
-                if (rs.kb == 64 && rs.ib == 32) {  // cannot happen with distinct ids
-                    if (ttid == 0) atomicOr(err, kErrSelect);
-                    break;
-                }
-                uint32_t *h = S.hist[W > 1 ? lead + (pass & 1u) : (uint32_t)warp];
-                ++pass;
-                const int w = rs.width();
-                for (uint32_t q = ttid; q < 256u; q += tstep) h[q] = 0u;
-                team_sync(team, W);
-                for (uint32_t k = ttid; k < cn; k += tstep) {
-                    const uint32_t l = S.perm[st + k];
-                    const unsigned long long key = ord_key(coord(S, sd, l));
-                    const uint32_t id = S.id[l];
-                    if (rs.match(key, id)) atomicAdd(&h[rs.digit(key, id, w)], 1u);
-                }
-                team_sync(team, W);
-                uint32_t mine = 0;
-#pragma unroll
-                for (int q = 0; q < 8; ++q) mine += h[lane * 8 + q];
-                uint32_t inc = mine;
-#pragma unroll
-                for (int off = 1; off < 32; off <<= 1) {
-                    const uint32_t v = __shfl_up_sync(kFull, inc, off);
-                    if (lane >= off) inc += v;
-                }
-                const uint32_t before = inc - mine;
-                uint32_t dsel = 0, below = 0, cnt = 0;
-                const bool owner = r >= before && r < inc;
-                if (owner) {
-                    uint32_t cum = before;
-                    for (int q = 0; q < 8; ++q) {
-                        const uint32_t c = h[lane * 8 + q];
-                        if (r < cum + c) {
-                            dsel = (uint32_t)(lane * 8 + q);
-                            below = cum;
-                            cnt = c;
-                            break;
-                        }
-                        cum += c;
-                    }
-                }
-                const int src = __ffs(__ballot_sync(kFull, owner)) - 1;
-                dsel = __shfl_sync(kFull, dsel, src);
-                below = __shfl_sync(kFull, below, src);
-                cnt = __shfl_sync(kFull, cnt, src);
-                rs.fix(dsel, w);
-                r -= below;
-                ccount = cnt;
-                if (W == 1) __syncwarp();
-            }
-            // gather the <= 32 candidates (a team counts them in shared memory; their order
-            // does not matter, they are ranked by comparison)
-            uint32_t ng = 0;
-            for (uint32_t base = tw * 32u; base < cn; base += tstep) {
-                const uint32_t k = base + lane;
-                bool hit = false;
-                unsigned long long key = 0;
-                uint32_t id = 0, l = 0;
-                if (k < cn) {
-                    l = S.perm[st + k];
-                    key = ord_key(coord(S, sd, l));
-                    id = S.id[l];
-                    hit = rs.match(key, id);
-                }
-                const uint32_t m = __ballot_sync(kFull, hit);
-                if (m) {
-                    uint32_t b0 = ng;
-                    if (W > 1) {
-                        if (lane == 0) b0 = atomicAdd(&S.tcnt[team], (uint32_t)__popc(m));
-                        b0 = __shfl_sync(kFull, b0, 0);
-                    }
-                    if (hit) {
-                        const uint32_t off = b0 + __popc(m & lt);
-                        if (off < 32) {
-                            S.ckey[lead][off] = key;
-                            S.cid[lead][off] = id;
-                            S.clid[lead][off] = (uint16_t)l;
-                        }
-                    }
-                    ng += __popc(m);
-                }
-            }
-            team_sync(team, W);
-            if (W > 1) ng = S.tcnt[team];
-            const bool have = (uint32_t)lane < min(ng, 32u);
-            const unsigned long long mk = have ? S.ckey[lead][lane] : ~0ull;
-            const uint32_t mi = have ? S.cid[lead][lane] : kFull;
-            uint32_t rank = 0;
-            for (int q = 0; q < 32; ++q) {
-                const unsigned long long ok = __shfl_sync(kFull, mk, q);
-                const uint32_t oi = __shfl_sync(kFull, mi, q);
-                rank += (ok < mk || (ok == mk && oi < mi)) ? 1u : 0u;
-            }
-            const uint32_t wm = __ballot_sync(kFull, have && rank == r);
-            const int ml = wm ? __ffs(wm) - 1 : 0;
-            if (!wm && ttid == 0) atomicOr(err, kErrSelect);
-            const unsigned long long kmed = __shfl_sync(kFull, mk, ml);
-            const uint32_t idmed = __shfl_sync(kFull, mi, ml);
-            if (ttid == 0) no.split_val[nid] = coord(S, sd, S.clid[lead][ml]);
-            // ---- 3. stable partition around the median: warp tw of the team takes the
-            // tw-th contiguous chunk of the node, after its left count is known
-            const uint32_t mid = cn / 2;
-            const uint32_t chunk = W > 1 ? ((cn + W - 1) / W + 31u) & ~31u : cn;
-            const uint32_t c_lo = min(cn, tw * chunk), c_hi = min(cn, c_lo + chunk);
-            uint32_t offL = 0, totalL = 0;
-            if (W > 1) {
-                uint32_t cl = 0;
-                for (uint32_t base = c_lo; base < c_hi; base += 32) {
-                    const uint32_t k = base + lane;
-                    bool isL = false;
-                    if (k < c_hi) {
-                        const uint32_t l = S.perm[st + k];
-                        isL = goes_left(ord_key(coord(S, sd, l)), S.id[l], kmed, idmed);
-                    }
-                    cl += __popc(__ballot_sync(kFull, isL));
-                }
-                if (lane == 0) S.wl[warp] = cl;
-                team_sync(team, W);
-                for (uint32_t q = 0; q < W; ++q) {
-                    const uint32_t v = S.wl[lead + q];
-                    if (q < tw) offL += v;
-                    totalL += v;
-                }
-            }
-            uint32_t offR = c_lo - offL;
-            for (uint32_t base = c_lo; base < c_hi; base += 32) {
-                const uint32_t k = base + lane;
-                bool in = k < c_hi, isL = false;
-                uint32_t l = 0;
-                if (in) {
-                    l = S.perm[st + k];
-                    isL = goes_left(ord_key(coord(S, sd, l)), S.id[l], kmed, idmed);
-                }
-                const uint32_t bl = __ballot_sync(kFull, in && isL);
-                const uint32_t br = __ballot_sync(kFull, in && !isL);
-                if (in) {
-                    const uint32_t dst = isL ? offL + __popc(bl & lt) : mid + offR + __popc(br & lt);
-                    if (dst < cn) S.perm2[st + dst] = (uint16_t)l;
-                }
-                offL += __popc(bl);
-                offR += __popc(br);
-            }
-            if (W == 1) totalL = offL;
-            // an inexact split (a failed select) leaves perm2 partly unwritten: keep perm, a
-            // valid permutation, and report the error
-            team_sync(team, W);
-            if (totalL == mid) {
-                for (uint32_t k = ttid; k < cn; k += tstep) S.perm[st + k] = S.perm2[st + k];
-            } else if (ttid == 0) {
-                atomicOr(err, kErrSelect);
-            }
-            if (W == 1) __syncwarp();
-        }
-        // ---- children that are still internal, appended as the next level
-        __syncthreads();
-        uint32_t fill = hi;
-        for (uint32_t base = 0; base < 2 * G; base += blockDim.x) {
-            const uint32_t u = base + threadIdx.x;
-            bool keep = false;
-            uint32_t cst = 0, ccn = 0, cid = 0, pcn = 0;
-            if (u < 2 * G) {
-                const uint32_t i = lo + (u >> 1);
-                const uint32_t st = S.tab_st[i], cn = S.tab_cn[i], id = S.tab_id[i];
-                pcn = cn;
-                const uint32_t lc = cn / 2;
-                if (u & 1) {
-                    cst = st + lc;
-                    ccn = cn - lc;
-                    cid = id + 1 + t.ttab[lc];
-                } else {
-                    cst = st;
-                    ccn = lc;
-                    cid = id + 1;
-                }
-                keep = ccn > leaf;
-            }
-            const uint32_t m = __ballot_sync(kFull, keep);
-            if (lane == 0) S.wcnt[warp] = __popc(m);
-            __syncthreads();
-            uint32_t off = fill;
-            uint32_t tot = 0;
-            for (int q = 0; q < kLocalWarps; ++q) {
-                if (q < warp) off += S.wcnt[q];
-                tot += S.wcnt[q];
-            }
-            if (keep) {
-                const uint32_t slot = off + __popc(m & lt);
-                if (slot < (uint32_t)kCap) {
-                    S.tab_st[slot] = (uint16_t)cst;
-                    S.tab_cn[slot] = (uint16_t)ccn;
-                    S.tab_pcn[slot] = (uint16_t)pcn;
-                    S.tab_id[slot] = cid;
-                }
-            }
-            fill += tot;
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) {
-            if (L + 2 > (uint32_t)kLocalLevels || fill > (uint32_t)kCap) {
-                atomicOr(err, kErrSelect);
-                fill = hi;  // stop: cannot happen for segments of <= kCap bodies
-            }
-            S.lvl_off[L + 2] = fill;
-            if (fill > hi) S.nlvl = L + 2;
-        }
-        __syncthreads();
-    }
-
-    local_finish(S, t, no, o, root, s0, c0, leaf);
-}
-
-// ------------------------------------------------------------------ presorted subtree finish
-//
-// The same subtree, built from three sorted lists instead of a select per node.  The
-// segment's bodies are sorted once along each dimension by (ordered key, local index) --
-// the local index orders bodies as their ids do, since every partition above was stable --
-// with a stable block radix sort of 16-bit indices over the key bits below the segment's
-// common prefix.  Each node then owns the same range [st, st + cn) of all three lists, each
-// sorted along its dimension: its bounding box is the lists' first and last entries, its
-// median the entry st + cn/2 of the split dimension's list, whose first half is the left
-// child.  A level flags its nodes' left bodies and partitions the other two lists stably
-// within every node at once (one block scan per level), so a level costs the same few passes
-// over the segment whatever the size and number of its nodes.  At the end each leaf's bodies
-// are put in index order (the select-based finish, used above kLocalSmallCap bodies, leaves
-// the bodies of its <= 32-body subtrees in rank order of their last split dimension: the
-// same leaves, the same splits); the bottom-up pass and the outputs are the shared ones.
-template <int kCap>
-struct SortSmem {
+struct LocalSmem {
     double xyz[3][kCap];  // positions, one row per dimension
     double m[kCap];
     uint32_t id[kCap];
@@ -2211,11 +1717,11 @@ __device__ void sort_lists(Smem &S, uint32_t c0, const unsigned long long (&kmin
 }
 
 template <int kCap>
-__global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
+__global__ __launch_bounds__(kLocalThreads, 4) void k_local(
     Topology t, const uint32_t *roots, NodeOut no, const double *wx, const double *wy,
     const double *wz, const uint32_t *wid, LocalOut o, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SortSmem<kCap> &S = *reinterpret_cast<SortSmem<kCap> *>(smem_raw);
+    LocalSmem<kCap> &S = *reinterpret_cast<LocalSmem<kCap> *>(smem_raw);
     const uint32_t root = roots[blockIdx.x];
     const uint32_t s0 = t.start[root], c0 = t.count[root];
     const uint32_t leaf = t.leaf;
@@ -2465,36 +1971,17 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local_sorted(
     local_finish(S, t, no, o, root, s0, c0, leaf);
 }
 
-template <int kCap>
-static void launch_local_cap(const Topology &t, const uint32_t *roots, uint32_t n_roots,
-                             const NodeOut &no, const Work &w, int cur, const LocalOut &out,
-                             uint32_t *err, cudaStream_t st) {
-    // set on every launch: the attribute belongs to the current device's context, and a
-    // process may hold contexts on several devices
-    const size_t smem = sizeof(LocalSmem<kCap>);
-    cudaFuncSetAttribute(k_local<kCap>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_local<kCap><<<n_roots, kLocalThreads, smem, st>>>(t, roots, no, w.x[cur], w.y[cur],
-                                                        w.z[cur], w.id[cur], out, err);
-}
-
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
                   uint32_t max_count, const NodeOut &no, const Work &w, int cur,
                   const LocalOut &out, uint32_t *err, cudaStream_t st) {
-#if KD_LOCAL_SORTED
-    if (max_count <= (uint32_t)kLocalSmallCap) {
-        // segments of at most kLocalSmallCap bodies: the presorted finish, 4 blocks per SM
-        const size_t smem = sizeof(SortSmem<kLocalSmallCap>);
-        cudaFuncSetAttribute(k_local_sorted<kLocalSmallCap>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_local_sorted<kLocalSmallCap><<<n_roots, kLocalThreads, smem, st>>>(
-            t, roots, no, w.x[cur], w.y[cur], w.z[cur], w.id[cur], out, err);
-        return;
-    }
-#endif
-    if (max_count <= (uint32_t)kLocalSmallCap)
-        launch_local_cap<kLocalSmallCap>(t, roots, n_roots, no, w, cur, out, err, st);
-    else
-        launch_local_cap<kLocalMax>(t, roots, n_roots, no, w, cur, out, err, st);
+    (void)max_count;  // every local segment holds at most kLocalMax bodies
+    // set on every launch: the attribute belongs to the current device's context, and a
+    // process may hold contexts on several devices
+    const size_t smem = sizeof(LocalSmem<kLocalMax>);
+    cudaFuncSetAttribute(k_local<kLocalMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    k_local<kLocalMax><<<n_roots, kLocalThreads, smem, st>>>(t, roots, no, w.x[cur], w.y[cur],
+                                                             w.z[cur], w.id[cur], out, err);
 }
 
 // ------------------------------------------------------------------ moments above the local roots

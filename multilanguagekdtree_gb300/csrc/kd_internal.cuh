@@ -18,9 +18,9 @@ __device__ __forceinline__ dbl4 ldg_dbl4(const dbl4 *p) {
 
 // ---------------------------------------------------------------- tuning constants
 // Segments of at most kLocalMax bodies finish their whole subtree in one thread block of
-// kLocalThreads threads, in shared memory (tunable at compile time).
+// kLocalThreads threads, in shared memory: ~56 KB at 640 bodies, four blocks per SM.
 #ifndef KD_LOCAL_MAX
-#define KD_LOCAL_MAX 1024
+#define KD_LOCAL_MAX 640
 #endif
 #ifndef KD_LOCAL_THREADS
 #define KD_LOCAL_THREADS 256
