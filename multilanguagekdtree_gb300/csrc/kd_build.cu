@@ -1587,13 +1587,13 @@ __device__ __forceinline__ void block_scan3(Smem &S, uint32_t (&v)[3], int lane,
 
 // Stable sorts of the segment's local indices along the three dimensions by (ordered key,
 // index) into S.lst[0][d], side by side: warps 0-2 sort x, 3-5 y, 6-7 z, so that the three
-// sorts share every block barrier.  LSD radix passes of 8 bits over the top 32 of the key
+// sorts share every block barrier.  LSD radix passes of 8 bits over the top 24 of the key
 // bits below the segment's common prefix in that dimension (all of them when there are at
-// most 32, and the sort is exact); each warp ranks the positions of its chunk in order (the
+// most 24, and the sort is exact); each warp ranks the positions of its chunk in order (the
 // peers of a digit by eight ballots), a digit-major scan over the group's counts gives every
 // run its offset, and the positions are scattered, ties keeping the index order.  Runs of keys
-// equal in the sorted window -- values within 2^-32 of the segment's range of each other --
-// are then ordered by the whole key, each by one thread.
+// equal in the sorted window -- values within about 2^-24 of the segment's range of each
+// other -- are then ordered by the whole key, every entry ranking itself within its run.
 template <class Smem>
 __device__ void sort_lists(Smem &S, uint32_t c0, const unsigned long long (&kmin)[3],
                            const unsigned long long (&kmax)[3], int lane, int warp) {
@@ -1602,7 +1602,7 @@ __device__ void sort_lists(Smem &S, uint32_t c0, const unsigned long long (&kmin
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int dbits = kmin[d] == kmax[d] ? 0 : 64 - __clzll((long long)(kmin[d] ^ kmax[d]));
-        lsb[d] = dbits > 32 ? dbits - 32 : 0;  // the sorted window is bits [lsb, dbits)
+        lsb[d] = dbits > 24 ? dbits - 24 : 0;  // the sorted window is bits [lsb, dbits)
         passes[d] = (dbits - lsb[d] + 7) / 8;
         np = max(np, passes[d]);
         // ping-pong so that the last pass writes S.lst[0][d]; the first reads the identity
@@ -1687,31 +1687,34 @@ __device__ void sort_lists(Smem &S, uint32_t c0, const unsigned long long (&kmin
         }
         __syncthreads();
     }
-    // runs of keys equal in the window, in whole-key order (index order inside a run so far)
+    // runs of keys equal in the window, in whole-key order: every position of a run ranks its
+    // body among the run's by (key, index) and is written to that rank, in parallel
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         if (lsb[d] == 0) continue;  // every distinguishing bit was sorted on
-        uint16_t *l = S.lst[0][d];
+        const uint16_t *l = S.lst[0][d];
+        uint16_t *tmp = S.lst[1][d];
         const int sh = lsb[d];
         for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x) {
-            const unsigned long long hp = ord_key(S.xyz[d][l[p]]) >> sh;
-            if (p > 0 && (ord_key(S.xyz[d][l[p - 1]]) >> sh) == hp) continue;
-            uint32_t e = p + 1;  // the run [p, e)
-            while (e < c0 && (ord_key(S.xyz[d][l[e]]) >> sh) == hp) ++e;
-            for (uint32_t a2 = p + 1; a2 < e; ++a2) {  // insertion sort by (key, index)
-                const uint16_t v = l[a2];
-                const unsigned long long kv = ord_key(S.xyz[d][v]);
-                uint32_t b2 = a2;
-                while (b2 > p) {
-                    const uint16_t u = l[b2 - 1];
-                    const unsigned long long ku = ord_key(S.xyz[d][u]);
-                    if (ku < kv || (ku == kv && u < v)) break;
-                    l[b2] = u;
-                    --b2;
-                }
-                l[b2] = v;
+            const uint16_t v = l[p];
+            const unsigned long long kv = ord_key(S.xyz[d][v]), wv = kv >> sh;
+            uint32_t a2 = p, e = p + 1;  // the run [a2, e)
+            while (a2 > 0 && (ord_key(S.xyz[d][l[a2 - 1]]) >> sh) == wv) --a2;
+            while (e < c0 && (ord_key(S.xyz[d][l[e]]) >> sh) == wv) ++e;
+            uint32_t r = 0;
+            for (uint32_t k = a2; k < e; ++k) {
+                const uint16_t u = l[k];
+                const unsigned long long ku = ord_key(S.xyz[d][u]);
+                r += (ku < kv || (ku == kv && u < v)) ? 1u : 0u;
             }
+            tmp[a2 + r] = v;
         }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (lsb[d] == 0) continue;
+        for (uint32_t p = threadIdx.x; p < c0; p += blockDim.x) S.lst[0][d][p] = S.lst[1][d][p];
     }
     __syncthreads();
 }
