@@ -51,7 +51,6 @@ struct Plan {
     std::vector<std::vector<uint32_t>> glevels;  // internal nodes of the multi-block levels
     std::vector<uint32_t> gmax;           // largest segment per multi-block level
     std::vector<uint32_t> local_roots;
-    uint32_t local_max = 0;               // bodies of the largest local root
     std::vector<uint32_t> ttab;
     uint64_t par4_slots = 0, par4_last = 0;
     bool par4_ok = true;
@@ -106,7 +105,6 @@ bool make_plan(uint32_t n, uint32_t leaf, Plan &p, std::string &err) {
         if (!local_found && mx <= (uint32_t)kLocalMax) {
             local_found = true;
             for (const E &e : cur) p.local_roots.push_back(e.id);
-            p.local_max = mx;
         }
         std::vector<uint32_t> internal;
         nxt.clear();
@@ -476,7 +474,7 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     o.heavy = c->d_heavy;
     o.n_heavy = c->n_heavy;
     const uint32_t nr = (uint32_t)p.local_roots.size();
-    launch_local(c->topo, c->d_local_roots, nr, p.local_max, c->nout, c->work, cur, o,
+    launch_local(c->topo, c->d_local_roots, nr, c->nout, c->work, cur, o,
                  c->dev_err, c->st);
     launch_moments_top(c->topo, c->d_local_roots, nr, c->nout, o, c->st);
     c->final_buf = cur;

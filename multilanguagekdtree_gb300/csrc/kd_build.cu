@@ -1975,9 +1975,8 @@ __global__ __launch_bounds__(kLocalThreads, 4) void k_local(
 }
 
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
-                  uint32_t max_count, const NodeOut &no, const Work &w, int cur,
-                  const LocalOut &out, uint32_t *err, cudaStream_t st) {
-    (void)max_count;  // every local segment holds at most kLocalMax bodies
+                  const NodeOut &no, const Work &w, int cur, const LocalOut &out,
+                  uint32_t *err, cudaStream_t st) {
     // set on every launch: the attribute belongs to the current device's context, and a
     // process may hold contexts on several devices
     const size_t smem = sizeof(LocalSmem<kLocalMax>);

@@ -256,12 +256,11 @@ void launch_place_selected(uint32_t *id, const uint32_t *med_pos, uint32_t goal,
 int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
                  Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready = false,
                  uint32_t seg_max = 0xffffffffu);
-// Subtree finish of every local root: split decisions, tree order, and the moments and
-// walk records of all nodes below the local roots.
-// max_count: the largest local root's body count (the shared-memory layout is chosen by it).
+// Subtree finish of every local root (each of at most kLocalMax bodies): split decisions,
+// tree order, and the moments and walk records of all nodes below the local roots.
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,
-                  uint32_t max_count, const NodeOut &no, const Work &w, int cur,
-                  const LocalOut &out, uint32_t *err, cudaStream_t st);
+                  const NodeOut &no, const Work &w, int cur, const LocalOut &out,
+                  uint32_t *err, cudaStream_t st);
 // Moments and records of the nodes above the local roots (one thread per local root climbs).
 void launch_moments_top(const Topology &t, const uint32_t *roots, uint32_t n_roots,
                         const NodeOut &no, const LocalOut &out, cudaStream_t st);
