@@ -673,8 +673,10 @@ __device__ __forceinline__ void walk_group_warp(
     }
 }
 
+static_assert(kGroupWarps * 32 >= kMaxHeavy, "a block loads the heavy bodies");
+// 16 warps per SM (128 registers)
 template <bool kCount, bool kPot>
-__global__ __launch_bounds__(kGroupWarps * 32, 4) void k_walk_group(
+__global__ __launch_bounds__(kGroupWarps * 32, 16 / kGroupWarps) void k_walk_group(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
     const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
     const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,
@@ -762,7 +764,8 @@ __global__ __launch_bounds__(kFinishThreads) void k_heavy_finish(
 // ysink_s (tree order) = -sum m w + the FP64 heavy-body terms; per list entry the sum over
 // the group's sinks of w goes to U (a body, tree order) or G (a node); the heavy bodies'
 // source sums go to yheavy.
-__global__ __launch_bounds__(kGroupWarps * 32, 3) void k_adj_group(
+// 12 warps per SM
+__global__ __launch_bounds__(kGroupWarps * 32, 12 / kGroupWarps) void k_adj_group(
     const NodeF *__restrict__ rec, const float4 *__restrict__ thi,
     const float4 *__restrict__ tlo, const float4 *__restrict__ trel,
     const uint32_t *__restrict__ tid, const uint32_t *__restrict__ gstart,

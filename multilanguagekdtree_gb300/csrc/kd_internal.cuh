@@ -276,7 +276,8 @@ void launch_walk_fp64(const NodeD *rec, const NodeP *recp, const float4 *thi,
 // gstart[g]..gstart[g+1] in tree order, boxed in two parts split at gsplit[g]; stk_cap =
 // per-warp stack entries (a multiple of 32).
 constexpr int kGroupSinks = 64;
-constexpr int kGroupWarps = 4;
+constexpr int kGroupWarps = 2;  // groups (warps) per block: a finished warp's block frees
+                                // its SM slot sooner than with 4 or 8
 #ifndef KD_GROUP_FLUSH
 #define KD_GROUP_FLUSH 128
 #endif
