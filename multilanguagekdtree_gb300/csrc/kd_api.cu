@@ -445,7 +445,12 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
                      levels ? c->scr.bmax[0] : nullptr, c->st);
     c->launches += 3;  // init + local finish + upward pass
     int cur = 0;
-    for (size_t l = 0; l < p.glevels.size(); ++l) {
+    // the last two levels (one when the root is the only multi-block segment) in one pass
+    const size_t L = p.glevels.size();
+    const size_t npair = L >= 2 && p.gmax[L - 2] <= kPairMax
+                             ? 2
+                             : (L >= 1 && p.gmax[L - 1] <= kPairMax ? 1 : 0);
+    for (size_t l = 0; l + npair < L; ++l) {
         LevelArgs lv;
         lv.ids = c->d_glevels[l];
         lv.G = (uint32_t)p.glevels[l].size();
@@ -457,6 +462,15 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
         const uint32_t G_next = l + 1 < p.glevels.size() ? (uint32_t)p.glevels[l + 1].size() : 0u;
         c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, (int)l, G_next,
                                     c->st, true, p.gmax[l]);
+        cur ^= 1;
+    }
+    if (npair) {
+        const size_t l0 = L - npair;
+        c->launches += launch_pair(c->topo, c->d_glevels[l0],
+                                   npair == 2 ? c->d_glevels[l0 + 1] : nullptr,
+                                   (uint32_t)p.glevels[l0].size(), p.gmax[l0],
+                                   c->scr.bmin[l0 & 1], c->scr.bmax[l0 & 1], c->nout, c->work,
+                                   cur, c->scr.err, c->st);
         cur ^= 1;
     }
     LocalOut o;

@@ -1313,6 +1313,397 @@ __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
     }
 }
 
+// ------------------------------------------------------------------ the last two levels
+
+// The last two multi-block levels (segments of at most kPairMax bodies, whose grandchildren
+// are local roots; the last level alone when the whole set is its only segment) in one block
+// per segment, with one read and one write of the bodies instead of two: the block stages the
+// segment's positions in shared memory, selects the segment's median, reduces the children's
+// bounding boxes, selects both children's medians at once, and writes the bodies out in the
+// order two stable partitions leave them (the left child's left child first).  A select
+// narrows its candidates with 8-bit radix passes over the key bits below the node's common
+// prefix, then over the id, as the warp select does, and ranks the last <= 32 in one warp.
+constexpr int kPairThreads = 256;
+constexpr int kPairWarps = kPairThreads / 32;
+static_assert(kPairMax < 65536u, "16-bit positions and per-class counts");
+static_assert(kPairThreads == 256, "one thread per radix bin");
+
+struct PairShared {
+    uint32_t hist[2][256];
+    uint32_t wsum[kPairWarps];
+    unsigned long long wsum64[kPairWarps];
+    uint32_t res[2][3];  // per selection: bin of the wanted rank, count below it, count in it
+    uint32_t ccnt[2];
+    unsigned long long ckey[2][32];
+    uint32_t cid[2][32], cpos[2][32];
+    unsigned long long kmed[2];
+    uint32_t idmed[2], posmed[2], sd[2];
+    uint32_t nleft;
+    unsigned long long red[kPairWarps][12];
+    unsigned long long box[12];  // the children's bounds: [side][min x, y, z, max x, y, z]
+};
+
+__device__ __forceinline__ RadixState radix_start(unsigned long long kmn, unsigned long long kmx) {
+    RadixState q;
+    q.kb = __clzll((long long)(kmn ^ kmx));
+    q.kp = q.kb == 0 ? 0ull : (q.kb == 64 ? kmn : (kmn >> (64 - q.kb)));
+    q.ib = 0;
+    q.ip = 0;
+    return q;
+}
+
+// Exact select by (key, id) of rank r0 (r1) among the bodies of selection 0 (1), along the
+// coordinate array v0 (v1): with ns = 1 the whole segment of cn bodies; with ns = 2 the
+// bodies j with side[j] == s, n0 and n1 of them.  kmn / kmx: each selection's bounds on that
+// coordinate as ordered keys.  Leaves the median's key, id and position in P.kmed, P.idmed
+// and P.posmed (key ~0 and position kFull, with kErrSelect in err, when a select fails).
+__device__ void pair_select(PairShared &P, const double *v0, const double *v1,
+                            const uint8_t *side, uint32_t cn, const uint32_t *gid, int ns,
+                            unsigned long long kmn0, unsigned long long kmx0,
+                            unsigned long long kmn1, unsigned long long kmx1, uint32_t n0,
+                            uint32_t n1, uint32_t r0, uint32_t r1, uint32_t *err) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    RadixState q0 = radix_start(kmn0, kmx0), q1 = radix_start(kmn1, kmx1);
+    bool a0 = n0 > 32u, a1 = ns > 1 && n1 > 32u;  // still narrowing
+    bool f0 = r0 >= n0, f1 = ns > 1 && r1 >= n1;   // failed
+    a0 = a0 && !f0;
+    a1 = a1 && !f1;
+    for (int round = 0; a0 || a1; ++round) {
+        // at most 8 passes over the key and 4 over the id; distinct ids always narrow
+        if (round >= 16) {
+            f0 = f0 || a0;
+            f1 = f1 || a1;
+            break;
+        }
+        if (a0 && q0.kb == 64 && q0.ib == 32) { a0 = false; f0 = true; }
+        if (a1 && q1.kb == 64 && q1.ib == 32) { a1 = false; f1 = true; }
+        if (!(a0 || a1)) break;
+        const int w0 = q0.width(), w1 = q1.width();
+        P.hist[0][threadIdx.x] = 0u;
+        P.hist[1][threadIdx.x] = 0u;
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < cn; j += kPairThreads) {
+            const bool s = ns > 1 && side[j] != 0;
+            if (!(s ? a1 : a0)) continue;
+            RadixState q = q0;
+            int w = w0;
+            if (s) {
+                q = q1;
+                w = w1;
+            }
+            const unsigned long long key = ord_key((s ? v1 : v0)[j]);
+            const uint32_t id = q.kb == 64 ? gid[j] : 0u;  // the id decides only below the key
+            if (q.match(key, id)) atomicAdd(&P.hist[s ? 1 : 0][q.digit(key, id, w)], 1u);
+        }
+        __syncthreads();
+        // both histograms scanned at once: selection 0 in the low 16 bits, 1 in the high
+        const uint32_t h = P.hist[0][threadIdx.x] | (P.hist[1][threadIdx.x] << 16);
+        uint32_t inc = h;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(kFull, inc, o);
+            if (lane >= o) inc += u;
+        }
+        if (lane == 31) P.wsum[warp] = inc;
+        __syncthreads();
+        uint32_t pre = 0, tot = 0;
+#pragma unroll
+        for (int q = 0; q < kPairWarps; ++q) {
+            const uint32_t x = P.wsum[q];
+            pre += q < warp ? x : 0u;
+            tot += x;
+        }
+        const uint32_t before = pre + inc - h;
+        const uint32_t b0 = before & 0xffffu, h0 = h & 0xffffu, b1 = before >> 16, h1 = h >> 16;
+        if (a0 && r0 >= b0 && r0 < b0 + h0) {
+            P.res[0][0] = threadIdx.x;
+            P.res[0][1] = b0;
+            P.res[0][2] = h0;
+        }
+        if (a1 && r1 >= b1 && r1 < b1 + h1) {
+            P.res[1][0] = threadIdx.x;
+            P.res[1][1] = b1;
+            P.res[1][2] = h1;
+        }
+        __syncthreads();
+        // a wanted rank beyond the candidates' count has no bin: a failed select
+        if (a0) {
+            if (r0 >= (tot & 0xffffu)) {
+                a0 = false;
+                f0 = true;
+            } else {
+                q0.fix(P.res[0][0], w0);
+                r0 -= P.res[0][1];
+                a0 = P.res[0][2] > 32u;
+            }
+        }
+        if (a1) {
+            if (r1 >= (tot >> 16)) {
+                a1 = false;
+                f1 = true;
+            } else {
+                q1.fix(P.res[1][0], w1);
+                r1 -= P.res[1][1];
+                a1 = P.res[1][2] > 32u;
+            }
+        }
+    }
+    // the <= 32 candidates of each selection, then their ranks by (key, id) in one warp each
+    if (threadIdx.x < 2) P.ccnt[threadIdx.x] = 0u;
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < cn; j += kPairThreads) {
+        const bool s = ns > 1 && side[j] != 0;
+        if (s ? f1 : f0) continue;
+        const RadixState q = s ? q1 : q0;
+        const unsigned long long key = ord_key((s ? v1 : v0)[j]);
+        const uint32_t id = q.kb == 64 ? gid[j] : 0u;
+        if (q.match(key, id)) {
+            const uint32_t k = atomicAdd(&P.ccnt[s ? 1 : 0], 1u);
+            if (k < 32u) {
+                P.ckey[s ? 1 : 0][k] = key;
+                P.cid[s ? 1 : 0][k] = gid[j];
+                P.cpos[s ? 1 : 0][k] = j;
+            }
+        }
+    }
+    __syncthreads();
+    if (warp < ns) {
+        const bool failed = warp ? f1 : f0;
+        const uint32_t r = warp ? r1 : r0;
+        const uint32_t m = min(P.ccnt[warp], 32u);
+        const bool have = !failed && (uint32_t)lane < m;
+        const unsigned long long mk = have ? P.ckey[warp][lane] : ~0ull;
+        const uint32_t mi = have ? P.cid[warp][lane] : kFull;
+        const uint32_t mp = have ? P.cpos[warp][lane] : kFull;
+        uint32_t rank = 0;
+        for (int q = 0; q < 32; ++q) {
+            const unsigned long long ok = __shfl_sync(kFull, mk, q);
+            const uint32_t oi = __shfl_sync(kFull, mi, q);
+            rank += (ok < mk || (ok == mk && oi < mi)) ? 1u : 0u;
+        }
+        const uint32_t wm = __ballot_sync(kFull, have && rank == r);
+        const int ml = wm ? __ffs(wm) - 1 : 0;
+        const unsigned long long km = __shfl_sync(kFull, mk, ml);
+        const uint32_t im = __shfl_sync(kFull, mi, ml), pm = __shfl_sync(kFull, mp, ml);
+        if (lane == 0) {
+            P.kmed[warp] = wm ? km : ~0ull;
+            P.idmed[warp] = wm ? im : kFull;
+            P.posmed[warp] = wm ? pm : kFull;
+            if (!wm) atomicOr(err, kErrSelect);
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool left_of(unsigned long long key, const uint32_t *gid, uint32_t j,
+                                        unsigned long long kmed, uint32_t idmed) {
+    // the id is read only for a key equal to the median's
+    return key < kmed || (key == kmed && gid[j] < idmed);
+}
+
+__global__ __launch_bounds__(kPairThreads, 3) void k_pair(
+    Topology t, const uint32_t *ids, const uint32_t *ids2, const unsigned long long *bmin,
+    const unsigned long long *bmax, const double *sx, const double *sy, const double *sz,
+    const uint32_t *sid, double *dx, double *dy, double *dz, uint32_t *did, NodeOut no,
+    uint32_t cap, uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char pair_raw[];
+    __shared__ PairShared P;
+    double *X = reinterpret_cast<double *>(pair_raw), *Y = X + cap, *Z = Y + cap;
+    uint16_t *order = reinterpret_cast<uint16_t *>(Z + cap);
+    uint8_t *side = reinterpret_cast<uint8_t *>(order + cap);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t seg = blockIdx.x;
+    const uint32_t nid = ids[seg];
+    const uint32_t start = t.start[nid], cn = t.count[nid];
+    if (cn > cap) {  // block-uniform; the host sizes cap to the level's largest segment
+        if (threadIdx.x == 0) atomicOr(err, kErrSelect);
+        return;
+    }
+    const bool two = ids2 != nullptr;
+    const uint32_t *gid = sid + start;
+    for (uint32_t j = threadIdx.x; j < cn; j += kPairThreads) {
+        cp_async8(&X[j], sx + start + j);
+        cp_async8(&Y[j], sy + start + j);
+        cp_async8(&Z[j], sz + start + j);
+    }
+    if (threadIdx.x == 0) {
+        double mn[3], mx[3];
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = ord_val(bmin[seg * 3 + d]);
+            mx[d] = ord_val(bmax[seg * 3 + d]);
+        }
+        uint32_t sd;
+        double size;
+        choose_split(mn, mx, sd, size);
+        no.split_dim[nid] = (uint8_t)sd;
+        no.size[nid] = size;
+        P.sd[0] = sd;
+        P.nleft = 0u;
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    // ---- the segment's median
+    const uint32_t sdA = P.sd[0];
+    const double *vA = pick(X, Y, Z, sdA);
+    pair_select(P, vA, vA, side, cn, gid, 1, bmin[seg * 3 + sdA], bmax[seg * 3 + sdA], 0ull,
+                0ull, cn, 0u, cn / 2, 0u, err);
+    const unsigned long long kmA = P.kmed[0];
+    const uint32_t imA = P.idmed[0];
+    if (threadIdx.x == 0 && P.posmed[0] < cn) no.split_val[nid] = vA[P.posmed[0]];
+
+    // ---- sides, and the children's bounding boxes (two levels)
+    unsigned long long cmn[2][3] = {{~0ull, ~0ull, ~0ull}, {~0ull, ~0ull, ~0ull}};
+    unsigned long long cmx[2][3] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
+    uint32_t nl = 0;
+    for (uint32_t j = threadIdx.x; j < cn; j += kPairThreads) {
+        const unsigned long long kx = ord_key(X[j]), ky = ord_key(Y[j]), kz = ord_key(Z[j]);
+        const unsigned long long key = sdA == 0 ? kx : (sdA == 1 ? ky : kz);
+        const bool L = left_of(key, gid, j, kmA, imA);
+        side[j] = L ? 0 : 1;
+        nl += L ? 1u : 0u;
+        if (two) {
+            if (L) {
+                cmn[0][0] = min(cmn[0][0], kx); cmx[0][0] = max(cmx[0][0], kx);
+                cmn[0][1] = min(cmn[0][1], ky); cmx[0][1] = max(cmx[0][1], ky);
+                cmn[0][2] = min(cmn[0][2], kz); cmx[0][2] = max(cmx[0][2], kz);
+            } else {
+                cmn[1][0] = min(cmn[1][0], kx); cmx[1][0] = max(cmx[1][0], kx);
+                cmn[1][1] = min(cmn[1][1], ky); cmx[1][1] = max(cmx[1][1], ky);
+                cmn[1][2] = min(cmn[1][2], kz); cmx[1][2] = max(cmx[1][2], kz);
+            }
+        }
+    }
+    nl = __reduce_add_sync(kFull, nl);
+    if (lane == 0) atomicAdd(&P.nleft, nl);
+    if (two) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                cmn[c][d] = warp_min(cmn[c][d]);
+                cmx[c][d] = warp_max(cmx[c][d]);
+            }
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    P.red[warp][6 * c + d] = cmn[c][d];
+                    P.red[warp][6 * c + 3 + d] = cmx[c][d];
+                }
+        }
+    }
+    __syncthreads();
+    const uint32_t nL = P.nleft;
+    if (threadIdx.x == 0 && nL != cn / 2) atomicOr(err, kErrSelect);
+
+    // ---- the children's splits and medians
+    if (two) {
+        if (threadIdx.x < 12) {
+            const bool is_max = threadIdx.x % 6 >= 3;
+            unsigned long long v = is_max ? 0ull : ~0ull;
+            for (int q = 0; q < kPairWarps; ++q)
+                v = is_max ? max(v, P.red[q][threadIdx.x]) : min(v, P.red[q][threadIdx.x]);
+            P.box[threadIdx.x] = v;
+        }
+        __syncthreads();
+        const uint32_t id0 = ids2[2 * seg], id1 = ids2[2 * seg + 1];
+        if (threadIdx.x < 2) {
+            const int c = threadIdx.x;
+            double mn[3], mx[3];
+            for (int d = 0; d < 3; ++d) {
+                mn[d] = ord_val(P.box[6 * c + d]);
+                mx[d] = ord_val(P.box[6 * c + 3 + d]);
+            }
+            uint32_t sd;
+            double size;
+            choose_split(mn, mx, sd, size);
+            const uint32_t cid = c ? id1 : id0;
+            no.split_dim[cid] = (uint8_t)sd;
+            no.size[cid] = size;
+            P.sd[c] = sd;
+        }
+        __syncthreads();
+        const uint32_t sd0 = P.sd[0], sd1 = P.sd[1];
+        const double *v0 = pick(X, Y, Z, sd0), *v1 = pick(X, Y, Z, sd1);
+        pair_select(P, v0, v1, side, cn, gid, 2, P.box[sd0], P.box[3 + sd0], P.box[6 + sd1],
+                    P.box[9 + sd1], nL, cn - nL, t.count[id0] / 2, t.count[id1] / 2, err);
+        if (threadIdx.x < 2) {
+            const uint32_t pm = P.posmed[threadIdx.x];
+            if (pm < cn) no.split_val[threadIdx.x ? id1 : id0] = (threadIdx.x ? v1 : v0)[pm];
+        }
+        const unsigned long long km0 = P.kmed[0], km1 = P.kmed[1];
+        const uint32_t im0 = P.idmed[0], im1 = P.idmed[1];
+        // class = 2 * side in the segment + side in the child: LL, LR, RL, RR
+        for (uint32_t j = threadIdx.x; j < cn; j += kPairThreads) {
+            const uint32_t sa = side[j];
+            const unsigned long long key = ord_key((sa ? v1 : v0)[j]);
+            const bool L = left_of(key, gid, j, sa ? km1 : km0, sa ? im1 : im0);
+            side[j] = (uint8_t)(2u * sa + (L ? 0u : 1u));
+        }
+        __syncthreads();
+    }
+
+    // ---- stable partition by class: each thread takes a run of consecutive bodies; the
+    // per-class counts (16-bit fields of one 64-bit word) are scanned over the block
+    const uint32_t E = (cn + kPairThreads - 1) / kPairThreads;
+    const uint32_t j0 = min(cn, threadIdx.x * E), j1 = min(cn, j0 + E);
+    unsigned long long cnt = 0;
+    for (uint32_t j = j0; j < j1; ++j) cnt += 1ull << (16 * side[j]);
+    unsigned long long inc = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long u = __shfl_up_sync(kFull, inc, o);
+        if (lane >= o) inc += u;
+    }
+    if (lane == 31) P.wsum64[warp] = inc;
+    __syncthreads();
+    unsigned long long pre = 0, tot = 0;
+#pragma unroll
+    for (int q = 0; q < kPairWarps; ++q) {
+        const unsigned long long x = P.wsum64[q];
+        pre += q < warp ? x : 0ull;
+        tot += x;
+    }
+    unsigned long long run = pre + inc - cnt;
+    const uint32_t t0 = (uint32_t)(tot & 0xffffu), t1 = (uint32_t)((tot >> 16) & 0xffffu),
+                   t2 = (uint32_t)((tot >> 32) & 0xffffu);
+    const uint32_t base1 = t0, base2 = t0 + t1, base3 = t0 + t1 + t2;
+    if (threadIdx.x == 0 && two &&
+        (t0 != t.count[ids2[2 * seg]] / 2 || t2 != t.count[ids2[2 * seg + 1]] / 2))
+        atomicOr(err, kErrSelect);
+    for (uint32_t j = j0; j < j1; ++j) {
+        const uint32_t c = side[j];
+        const uint32_t base = c == 0 ? 0u : (c == 1 ? base1 : (c == 2 ? base2 : base3));
+        order[base + (uint32_t)((run >> (16 * c)) & 0xffffu)] = (uint16_t)j;
+        run += 1ull << (16 * c);
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < cn; j += kPairThreads) {
+        const uint32_t q = order[j];
+        const uint32_t dst = start + j;
+        dx[dst] = X[q];
+        dy[dst] = Y[q];
+        dz[dst] = Z[q];
+        did[dst] = gid[q];
+    }
+}
+
+int launch_pair(const Topology &t, const uint32_t *ids, const uint32_t *ids2, uint32_t G,
+                uint32_t cap, const unsigned long long *bmin, const unsigned long long *bmax,
+                const NodeOut &no, Work &w, int cur, uint32_t *err, cudaStream_t st) {
+    const int nxt = cur ^ 1;
+    const size_t smem = ((size_t)cap * (3 * sizeof(double) + sizeof(uint16_t) + 1) + 15) &
+                        ~(size_t)15;
+    // set on every launch: the attribute belongs to the current device's context
+    cudaFuncSetAttribute(k_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pair<<<G, kPairThreads, smem, st>>>(t, ids, ids2, bmin, bmax, w.x[cur], w.y[cur],
+                                          w.z[cur], w.id[cur], w.x[nxt], w.y[nxt], w.z[nxt],
+                                          w.id[nxt], no, cap, err);
+    return 1;
+}
+
 // Mixed leaf record: origin o = position of the leaf's first body, as hi + lo floats.  The
 // leaf's first position is noted in perm2 for every body of the leaf, whose offset from o
 // goes to trel with the tree-ordered bodies.

@@ -26,6 +26,9 @@ __device__ __forceinline__ dbl4 ldg_dbl4(const dbl4 *p) {
 #define KD_LOCAL_THREADS 256
 #endif
 constexpr int kLocalMax = KD_LOCAL_MAX;
+// The last two multi-block levels (segments of at most four local roots' bodies) run as one
+// pass, one block per segment (k_pair).
+constexpr uint32_t kPairMax = 4u * (uint32_t)KD_LOCAL_MAX;
 constexpr int kLocalThreads = KD_LOCAL_THREADS;
 constexpr int kTile = 2048;         // elements per block in the multi-block level passes
 constexpr int kTileThreads = 256;
@@ -256,6 +259,13 @@ void launch_place_selected(uint32_t *id, const uint32_t *med_pos, uint32_t goal,
 int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work &w, int cur,
                  Scratch &s, int lvl, uint32_t G_next, cudaStream_t st, bool box0_ready = false,
                  uint32_t seg_max = 0xffffffffu);
+// The last one or two levels above the local roots in one pass: the segments `ids` (G of
+// them, at most `cap` <= kPairMax bodies each, boxes in bmin/bmax) and, with `ids2` set, their
+// children (ids2[2g], ids2[2g+1]) are split, and the bodies go from work buffer `cur` to the
+// other in the order of the local roots.  Returns the number of kernels launched.
+int launch_pair(const Topology &t, const uint32_t *ids, const uint32_t *ids2, uint32_t G,
+                uint32_t cap, const unsigned long long *bmin, const unsigned long long *bmax,
+                const NodeOut &no, Work &w, int cur, uint32_t *err, cudaStream_t st);
 // Subtree finish of every local root (each of at most kLocalMax bodies): split decisions,
 // tree order, and the moments and walk records of all nodes below the local roots.
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,

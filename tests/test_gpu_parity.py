@@ -100,7 +100,8 @@ def test_simple_sim_vs_golden(kd, golden):
 @pytest.mark.parametrize("n,leaf,layout,gen", [
     (5001, 7, "dfs", "circ"), (20_000, 8, "par4", "ring"), (100_000, 7, "dfs", "ring"),
     (100_000, 8, "par4", "plummer"), (65_537, 7, "par4", "ring"), (1023, 7, "dfs", "plummer"),
-    (1025, 8, "dfs", "ring"), (33_000, 7, "dfs", "plummer"),
+    (1025, 8, "dfs", "ring"), (33_000, 7, "dfs", "plummer"), (2000, 7, "dfs", "plummer"),
+    (2560, 8, "par4", "ring"), (1281, 7, "dfs", "circ"),
 ])
 def test_tree_and_accel_vs_oracle(kd, oracle, n, leaf, layout, gen):
     b = {"circ": lambda: kd.circular_orbits(n - 1, seed=n),
