@@ -1321,8 +1321,8 @@ __global__ __launch_bounds__(kWarpSelWarps * 32) void k_split_select_warp(
 // segment's positions in shared memory, selects the segment's median, reduces the children's
 // bounding boxes, selects both children's medians at once, and writes the bodies out in the
 // order two stable partitions leave them (the left child's left child first).  A select
-// narrows its candidates with 8-bit radix passes over the key bits below the node's common
-// prefix, then over the id, as the warp select does, and ranks the last <= 32 in one warp.
+// narrows its candidates with 8-bit radix passes over the key's offset from the node's
+// smallest key, then over the id, and ranks the last <= 32 in one warp.
 constexpr int kPairThreads = 256;
 constexpr int kPairWarps = kPairThreads / 32;
 static_assert(kPairMax < 65536u, "16-bit positions and per-class counts");
@@ -1363,7 +1363,10 @@ __device__ void pair_select(PairShared &P, const double *v0, const double *v1,
                             unsigned long long kmn1, unsigned long long kmx1, uint32_t n0,
                             uint32_t n1, uint32_t r0, uint32_t r1, uint32_t *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    RadixState q0 = radix_start(kmn0, kmx0), q1 = radix_start(kmn1, kmx1);
+    // the passes bin key - kmn (the offset from the selection's smallest key): the first one
+    // takes the 8 bits below the range's top bit and spreads the bodies over 129-256 bins,
+    // where the key's own bits below its common prefix can leave them in two
+    RadixState q0 = radix_start(0ull, kmx0 - kmn0), q1 = radix_start(0ull, kmx1 - kmn1);
     bool a0 = n0 > 32u, a1 = ns > 1 && n1 > 32u;  // still narrowing
     bool f0 = r0 >= n0, f1 = ns > 1 && r1 >= n1;   // failed
     a0 = a0 && !f0;
@@ -1391,7 +1394,7 @@ __device__ void pair_select(PairShared &P, const double *v0, const double *v1,
                 q = q1;
                 w = w1;
             }
-            const unsigned long long key = ord_key((s ? v1 : v0)[j]);
+            const unsigned long long key = ord_key((s ? v1 : v0)[j]) - (s ? kmn1 : kmn0);
             const uint32_t id = q.kb == 64 ? gid[j] : 0u;  // the id decides only below the key
             if (q.match(key, id)) atomicAdd(&P.hist[s ? 1 : 0][q.digit(key, id, w)], 1u);
         }
@@ -1457,7 +1460,7 @@ __device__ void pair_select(PairShared &P, const double *v0, const double *v1,
         const RadixState q = s ? q1 : q0;
         const unsigned long long key = ord_key((s ? v1 : v0)[j]);
         const uint32_t id = q.kb == 64 ? gid[j] : 0u;
-        if (q.match(key, id)) {
+        if (q.match(key - (s ? kmn1 : kmn0), id)) {
             const uint32_t k = atomicAdd(&P.ccnt[s ? 1 : 0], 1u);
             if (k < 32u) {
                 P.ckey[s ? 1 : 0][k] = key;
