@@ -1529,6 +1529,14 @@ __global__ __launch_bounds__(kPairThreads, 3) void k_pair(
         cp_async8(&Y[j], sy + start + j);
         cp_async8(&Z[j], sz + start + j);
     }
+    // the ids are read by the write-out (and for keys equal to a median's): brought into L2
+    // now, one 128-byte line per thread
+    for (uint32_t j = threadIdx.x * 32u; j < cn; j += kPairThreads * 32u)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(gid + j));
+    if (threadIdx.x == 0 && cn > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(gid + cn - 1));
+    // the children, read after the first select
+    const uint32_t id0 = two ? ids2[2 * seg] : 0u, id1 = two ? ids2[2 * seg + 1] : 0u;
+    const uint32_t half0 = two ? t.count[id0] / 2 : 0u, half1 = two ? t.count[id1] / 2 : 0u;
     if (threadIdx.x == 0) {
         double mn[3], mx[3];
         for (int d = 0; d < 3; ++d) {
@@ -1611,7 +1619,6 @@ __global__ __launch_bounds__(kPairThreads, 3) void k_pair(
             P.box[threadIdx.x] = v;
         }
         __syncthreads();
-        const uint32_t id0 = ids2[2 * seg], id1 = ids2[2 * seg + 1];
         if (threadIdx.x < 2) {
             const int c = threadIdx.x;
             double mn[3], mx[3];
@@ -1631,7 +1638,7 @@ __global__ __launch_bounds__(kPairThreads, 3) void k_pair(
         const uint32_t sd0 = P.sd[0], sd1 = P.sd[1];
         const double *v0 = pick(X, Y, Z, sd0), *v1 = pick(X, Y, Z, sd1);
         pair_select(P, v0, v1, side, cn, gid, 2, P.box[sd0], P.box[3 + sd0], P.box[6 + sd1],
-                    P.box[9 + sd1], nL, cn - nL, t.count[id0] / 2, t.count[id1] / 2, err);
+                    P.box[9 + sd1], nL, cn - nL, half0, half1, err);
         if (threadIdx.x < 2) {
             const uint32_t pm = P.posmed[threadIdx.x];
             if (pm < cn) no.split_val[threadIdx.x ? id1 : id0] = (threadIdx.x ? v1 : v0)[pm];
@@ -1673,9 +1680,7 @@ __global__ __launch_bounds__(kPairThreads, 3) void k_pair(
     const uint32_t t0 = (uint32_t)(tot & 0xffffu), t1 = (uint32_t)((tot >> 16) & 0xffffu),
                    t2 = (uint32_t)((tot >> 32) & 0xffffu);
     const uint32_t base1 = t0, base2 = t0 + t1, base3 = t0 + t1 + t2;
-    if (threadIdx.x == 0 && two &&
-        (t0 != t.count[ids2[2 * seg]] / 2 || t2 != t.count[ids2[2 * seg + 1]] / 2))
-        atomicOr(err, kErrSelect);
+    if (threadIdx.x == 0 && two && (t0 != half0 || t2 != half1)) atomicOr(err, kErrSelect);
     for (uint32_t j = j0; j < j1; ++j) {
         const uint32_t c = side[j];
         const uint32_t base = c == 0 ? 0u : (c == 1 ? base1 : (c == 2 ? base2 : base3));

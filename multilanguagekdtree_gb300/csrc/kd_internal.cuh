@@ -40,7 +40,7 @@ constexpr int kSelCap = 2048;       // capacity of the select's shared-memory so
 #endif
 constexpr int kSelThreads = KD_SEL_THREADS;
 #ifndef KD_MULTI_MIN
-#define KD_MULTI_MIN 8192
+#define KD_MULTI_MIN 4096
 #endif
 constexpr uint32_t kMultiMin = KD_MULTI_MIN;  // segments above this use multi-block histograms
 constexpr int kSelMaxIters = 16;    // radix refinement passes before giving up (error)
