@@ -258,8 +258,9 @@ int kd_direct_accel_noalloc(const double *x, const double *y, const double *z,
 /* Device-side guards, lowered for testing the failure path: the traversal stack of both
  * walks is cut to stack_entries (at most 32 for the FP64 walk, whose stack is one entry per
  * lane; at most 32 * (tree depth + 2) + 64 for the grouped walk and its adjoint) and the
- * radix refinement passes of the block median select (segments above 4,096 bodies) to
- * select_passes (at most 16).  A negative value restores the default.  A walk or select that
+ * radix refinement passes of the block median selects (segments above 4,096 bodies, and the
+ * shared-memory selects of the last two levels above the subtree finish) to select_passes
+ * (at most 16).  A negative value restores the default.  A walk or select that
  * runs out stops, sets a device flag, and the call returns KD_EDEVICE ("traversal stack
  * overflow" / "median select failed to converge"); nothing traps or waits, the step's
  * kick-drift is skipped (the bodies stay at the start of the failed step), and the context

@@ -470,7 +470,7 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
                                    npair == 2 ? c->d_glevels[l0 + 1] : nullptr,
                                    (uint32_t)p.glevels[l0].size(), p.gmax[l0],
                                    c->scr.bmin[l0 & 1], c->scr.bmax[l0 & 1], c->nout, c->work,
-                                   cur, c->scr.err, c->st);
+                                   cur, c->select_passes, c->scr.err, c->st);
         cur ^= 1;
     }
     LocalOut o;

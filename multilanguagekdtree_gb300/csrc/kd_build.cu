@@ -1356,12 +1356,14 @@ __device__ __forceinline__ RadixState radix_start(unsigned long long kmn, unsign
 // coordinate array v0 (v1): with ns = 1 the whole segment of cn bodies; with ns = 2 the
 // bodies j with side[j] == s, n0 and n1 of them.  kmn / kmx: each selection's bounds on that
 // coordinate as ordered keys.  Leaves the median's key, id and position in P.kmed, P.idmed
-// and P.posmed (key ~0 and position kFull, with kErrSelect in err, when a select fails).
+// and P.posmed (key ~0 and position kFull, with kErrSelect in err, when a select fails,
+// also when it would need more than max_rounds radix passes).
 __device__ void pair_select(PairShared &P, const double *v0, const double *v1,
                             const uint8_t *side, uint32_t cn, const uint32_t *gid, int ns,
                             unsigned long long kmn0, unsigned long long kmx0,
                             unsigned long long kmn1, unsigned long long kmx1, uint32_t n0,
-                            uint32_t n1, uint32_t r0, uint32_t r1, uint32_t *err) {
+                            uint32_t n1, uint32_t r0, uint32_t r1, int max_rounds,
+                            uint32_t *err) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // the passes bin key - kmn (the offset from the selection's smallest key): the first one
     // takes the 8 bits below the range's top bit and spreads the bodies over 129-256 bins,
@@ -1372,8 +1374,9 @@ __device__ void pair_select(PairShared &P, const double *v0, const double *v1,
     a0 = a0 && !f0;
     a1 = a1 && !f1;
     for (int round = 0; a0 || a1; ++round) {
-        // at most 8 passes over the key and 4 over the id; distinct ids always narrow
-        if (round >= 16) {
+        // at most 8 passes over the key and 4 over the id (distinct ids always narrow);
+        // fewer when the caller lowers the limit to test this failure path
+        if (round >= max_rounds) {
             f0 = f0 || a0;
             f1 = f1 || a1;
             break;
@@ -1508,7 +1511,7 @@ __global__ __launch_bounds__(kPairThreads, 3) void k_pair(
     Topology t, const uint32_t *ids, const uint32_t *ids2, const unsigned long long *bmin,
     const unsigned long long *bmax, const double *sx, const double *sy, const double *sz,
     const uint32_t *sid, double *dx, double *dy, double *dz, uint32_t *did, NodeOut no,
-    uint32_t cap, uint32_t *err) {
+    uint32_t cap, int max_rounds, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char pair_raw[];
     __shared__ PairShared P;
     double *X = reinterpret_cast<double *>(pair_raw), *Y = X + cap, *Z = Y + cap;
@@ -1558,7 +1561,7 @@ __global__ __launch_bounds__(kPairThreads, 3) void k_pair(
     const uint32_t sdA = P.sd[0];
     const double *vA = pick(X, Y, Z, sdA);
     pair_select(P, vA, vA, side, cn, gid, 1, bmin[seg * 3 + sdA], bmax[seg * 3 + sdA], 0ull,
-                0ull, cn, 0u, cn / 2, 0u, err);
+                0ull, cn, 0u, cn / 2, 0u, max_rounds, err);
     const unsigned long long kmA = P.kmed[0];
     const uint32_t imA = P.idmed[0];
     if (threadIdx.x == 0 && P.posmed[0] < cn) no.split_val[nid] = vA[P.posmed[0]];
@@ -1638,7 +1641,7 @@ __global__ __launch_bounds__(kPairThreads, 3) void k_pair(
         const uint32_t sd0 = P.sd[0], sd1 = P.sd[1];
         const double *v0 = pick(X, Y, Z, sd0), *v1 = pick(X, Y, Z, sd1);
         pair_select(P, v0, v1, side, cn, gid, 2, P.box[sd0], P.box[3 + sd0], P.box[6 + sd1],
-                    P.box[9 + sd1], nL, cn - nL, half0, half1, err);
+                    P.box[9 + sd1], nL, cn - nL, half0, half1, max_rounds, err);
         if (threadIdx.x < 2) {
             const uint32_t pm = P.posmed[threadIdx.x];
             if (pm < cn) no.split_val[threadIdx.x ? id1 : id0] = (threadIdx.x ? v1 : v0)[pm];
@@ -1700,7 +1703,8 @@ __global__ __launch_bounds__(kPairThreads, 3) void k_pair(
 
 int launch_pair(const Topology &t, const uint32_t *ids, const uint32_t *ids2, uint32_t G,
                 uint32_t cap, const unsigned long long *bmin, const unsigned long long *bmax,
-                const NodeOut &no, Work &w, int cur, uint32_t *err, cudaStream_t st) {
+                const NodeOut &no, Work &w, int cur, int max_rounds, uint32_t *err,
+                cudaStream_t st) {
     const int nxt = cur ^ 1;
     const size_t smem = ((size_t)cap * (3 * sizeof(double) + sizeof(uint16_t) + 1) + 15) &
                         ~(size_t)15;
@@ -1708,7 +1712,7 @@ int launch_pair(const Topology &t, const uint32_t *ids, const uint32_t *ids2, ui
     cudaFuncSetAttribute(k_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_pair<<<G, kPairThreads, smem, st>>>(t, ids, ids2, bmin, bmax, w.x[cur], w.y[cur],
                                           w.z[cur], w.id[cur], w.x[nxt], w.y[nxt], w.z[nxt],
-                                          w.id[nxt], no, cap, err);
+                                          w.id[nxt], no, cap, max_rounds, err);
     return 1;
 }
 

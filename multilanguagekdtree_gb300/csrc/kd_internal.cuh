@@ -262,10 +262,12 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
 // The last one or two levels above the local roots in one pass: the segments `ids` (G of
 // them, at most `cap` <= kPairMax bodies each, boxes in bmin/bmax) and, with `ids2` set, their
 // children (ids2[2g], ids2[2g+1]) are split, and the bodies go from work buffer `cur` to the
-// other in the order of the local roots.  Returns the number of kernels launched.
+// other in the order of the local roots.  A select needing more than max_rounds radix
+// passes fails (kErrSelect).  Returns the number of kernels launched.
 int launch_pair(const Topology &t, const uint32_t *ids, const uint32_t *ids2, uint32_t G,
                 uint32_t cap, const unsigned long long *bmin, const unsigned long long *bmax,
-                const NodeOut &no, Work &w, int cur, uint32_t *err, cudaStream_t st);
+                const NodeOut &no, Work &w, int cur, int max_rounds, uint32_t *err,
+                cudaStream_t st);
 // Subtree finish of every local root (each of at most kLocalMax bodies): split decisions,
 // tree order, and the moments and walk records of all nodes below the local roots.
 void launch_local(const Topology &t, const uint32_t *roots, uint32_t n_roots,

@@ -54,9 +54,10 @@ def test_fp64_walk_stack_guard_then_oracle_parity(kd, oracle):
 
 
 def test_select_guard_then_exact_tree(kd, oracle):
-    """n = 20,000: the level of 5,000-body segments runs the block select, which with no
-    refinement pass left reports the failure.  The master state is untouched, so the next
-    build, with the default limits, is the exact tree again."""
+    """n = 20,000: the last two levels above the subtree finish (2,500- and 1,250-body
+    segments) select their medians in shared memory, which takes at least one radix pass;
+    with none left the selects report the failure.  The master state is untouched, so the
+    next build, with the default limits, is the exact tree again."""
     n = 20_000
     b = kd.ring(n, seed=73)
     with kd.KDTreeSim(n, precision="fp64") as s:
