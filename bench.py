@@ -572,12 +572,12 @@ def run_ours(a, ws, rank, local):
 
 # DRAM bytes per body of one launch, from one-pass ncu captures of the 10M-body step (the
 # launch list in profiles/): the grouped walk (4.79 GB), and the build's kernels summed over
-# the step (11.76 GB, every kernel starting with cold caches), both scaled by the number of
+# the step (10.94 GB, every kernel starting with cold caches), both scaled by the number of
 # bodies
 WALK_TRAFFIC_PER_BODY = 479.0
-BUILD_TRAFFIC_PER_BODY = 1176.0
+BUILD_TRAFFIC_PER_BODY = 1094.0
 BUILD_TRAFFIC_NOTE = ("ncu dram read + write of the build's kernels in one 10M-ring step "
-                      "(1,176 B/body, cold caches per kernel), scaled by N")
+                      "(1,094 B/body, cold caches per kernel), scaled by N")
 
 
 def tree_levels(n: int, leaf: int) -> int:
