@@ -455,6 +455,8 @@ __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
     TileRef r;
     const bool has = tile_at(t, lv, seg * lv.tiles + t0, r);  // block-uniform
     uint32_t *gh = hist + (size_t)seg * kHistBins;
+    // a block that holds the whole segment has its final bins in shared memory already
+    const bool alone = per_seg == 1u;
     if (has) {
         const uint32_t hi = min(r.cnt, r.lo + kHistTiles * (uint32_t)kTile);
         for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) h[b] = 0;
@@ -484,18 +486,21 @@ __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
             for (int i = 0; i < kRows; ++i) v[i] = nv[i];
         }
         __syncthreads();
-        for (int b = threadIdx.x; b < kHistBins; b += blockDim.x)
-            if (h[b]) atomicAdd(&gh[b], h[b]);
+        if (!alone)
+            for (int b = threadIdx.x; b < kHistBins; b += blockDim.x)
+                if (h[b]) atomicAdd(&gh[b], h[b]);
     }
-    // the segment's last block sees every block's bins
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(&done[seg], 1u) == per_seg - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) h[b] = __ldcg(&gh[b]);
-    __syncthreads();
+    if (!alone) {
+        // the segment's last block sees every block's bins
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) last = atomicAdd(&done[seg], 1u) == per_seg - 1;
+        __syncthreads();
+        if (!last) return;
+        __threadfence();
+        for (int b = threadIdx.x; b < kHistBins; b += blockDim.x) h[b] = __ldcg(&gh[b]);
+        __syncthreads();
+    }
     find_bin(h, s.r, out3);
     if (threadIdx.x == 0) {
         SegSel o = s;
@@ -505,7 +510,7 @@ __global__ __launch_bounds__(kTileThreads) void k_hist(Topology t, LevelArgs lv,
         sel[seg] = o;
         no.split_dim[id] = (uint8_t)s.sd;
         no.size[id] = size;
-        done[seg] = 0u;
+        if (!alone) done[seg] = 0u;
     }
 }
 
@@ -1059,7 +1064,9 @@ int launch_level(const Topology &t, const LevelArgs &lv, const NodeOut &no, Work
     if (lv.multi) {
         // split + histogram (+ bin search), candidates (+ lower-bin counts), exact median
         // (+ tile offsets)
-        cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * kHistBins * (size_t)G, st);
+        // one histogram block per segment keeps its bins in shared memory: no global bins
+        if (lv.tiles > kHistTiles)
+            cudaMemsetAsync(s.hist, 0, sizeof(uint32_t) * kHistBins * (size_t)G, st);
         cudaMemsetAsync(s.cand_cnt, 0, sizeof(uint32_t) * G, st);
         k_hist<<<G * ((lv.tiles + kHistTiles - 1) / kHistTiles), kTileThreads, 0, st>>>(
             t, lv, w.x[cur], w.y[cur], w.z[cur], bmin, bmax, s.sel, no, s.hist, s.done);
@@ -1352,6 +1359,20 @@ __device__ __forceinline__ RadixState radix_start(unsigned long long kmn, unsign
     return q;
 }
 
+// A radix pass over the key bits (fixed bits kb < 64): the pass's digit of a key is
+// (key >> sh) - base, and the key has the fixed bits exactly when that is below lim.
+struct KeyWindow {
+    unsigned long long base, lim;
+    uint32_t sh;
+};
+__device__ __forceinline__ KeyWindow key_window(const RadixState &q, int w) {
+    KeyWindow k;
+    k.sh = (uint32_t)(64 - q.kb - w);
+    k.base = q.kp << w;
+    k.lim = 1ull << w;
+    return k;
+}
+
 // Exact select by (key, id) of rank r0 (r1) among the bodies of selection 0 (1), along the
 // coordinate array v0 (v1): with ns = 1 the whole segment of cn bodies; with ns = 2 the
 // bodies j with side[j] == s, n0 and n1 of them.  kmn / kmx: each selection's bounds on that
@@ -1385,21 +1406,25 @@ __device__ void pair_select(PairShared &P, const double *v0, const double *v1,
         if (a1 && q1.kb == 64 && q1.ib == 32) { a1 = false; f1 = true; }
         if (!(a0 || a1)) break;
         const int w0 = q0.width(), w1 = q1.width();
+        const KeyWindow k0 = key_window(q0, w0), k1 = key_window(q1, w1);
+        // passes over the id: only for keys equal in all 64 bits
+        const bool byid0 = q0.kb == 64, byid1 = q1.kb == 64;
         P.hist[0][threadIdx.x] = 0u;
         P.hist[1][threadIdx.x] = 0u;
         __syncthreads();
         for (uint32_t j = threadIdx.x; j < cn; j += kPairThreads) {
             const bool s = ns > 1 && side[j] != 0;
             if (!(s ? a1 : a0)) continue;
-            RadixState q = q0;
-            int w = w0;
-            if (s) {
-                q = q1;
-                w = w1;
-            }
             const unsigned long long key = ord_key((s ? v1 : v0)[j]) - (s ? kmn1 : kmn0);
-            const uint32_t id = q.kb == 64 ? gid[j] : 0u;  // the id decides only below the key
-            if (q.match(key, id)) atomicAdd(&P.hist[s ? 1 : 0][q.digit(key, id, w)], 1u);
+            if (s ? byid1 : byid0) {
+                const RadixState q = s ? q1 : q0;
+                const uint32_t id = gid[j];
+                if (q.match(key, id))
+                    atomicAdd(&P.hist[s ? 1 : 0][q.digit(key, id, s ? w1 : w0)], 1u);
+            } else {
+                const unsigned long long d = (key >> (s ? k1.sh : k0.sh)) - (s ? k1.base : k0.base);
+                if (d < (s ? k1.lim : k0.lim)) atomicAdd(&P.hist[s ? 1 : 0][(uint32_t)d], 1u);
+            }
         }
         __syncthreads();
         // both histograms scanned at once: selection 0 in the low 16 bits, 1 in the high
@@ -1456,14 +1481,22 @@ __device__ void pair_select(PairShared &P, const double *v0, const double *v1,
     }
     // the <= 32 candidates of each selection, then their ranks by (key, id) in one warp each
     if (threadIdx.x < 2) P.ccnt[threadIdx.x] = 0u;
+    const KeyWindow g0 = key_window(q0, q0.width()), g1 = key_window(q1, q1.width());
+    const bool byid0 = q0.kb == 64, byid1 = q1.kb == 64;
     __syncthreads();
     for (uint32_t j = threadIdx.x; j < cn; j += kPairThreads) {
         const bool s = ns > 1 && side[j] != 0;
         if (s ? f1 : f0) continue;
-        const RadixState q = s ? q1 : q0;
         const unsigned long long key = ord_key((s ? v1 : v0)[j]);
-        const uint32_t id = q.kb == 64 ? gid[j] : 0u;
-        if (q.match(key - (s ? kmn1 : kmn0), id)) {
+        const unsigned long long rel = key - (s ? kmn1 : kmn0);
+        bool hit;
+        if (s ? byid1 : byid0) {
+            const RadixState q = s ? q1 : q0;
+            hit = q.match(rel, gid[j]);
+        } else {
+            hit = (rel >> (s ? g1.sh : g0.sh)) - (s ? g1.base : g0.base) < (s ? g1.lim : g0.lim);
+        }
+        if (hit) {
             const uint32_t k = atomicAdd(&P.ccnt[s ? 1 : 0], 1u);
             if (k < 32u) {
                 P.ckey[s ? 1 : 0][k] = key;
