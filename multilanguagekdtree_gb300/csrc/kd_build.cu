@@ -16,10 +16,11 @@
 //
 // Structure: levels whose segments exceed kLocalMax bodies run as multi-block passes
 // (bounding box -> split -> exact median select -> stable partition into the other
-// ping-pong buffer, which also reduces the children's bounding boxes); below that, one
-// thread block takes a whole segment into shared memory and finishes its subtree there
-// (per-dimension sorted lists: bounds and medians read off the lists, one segmented stable
-// partition of the lists per level).
+// ping-pong buffer, which also reduces the children's bounding boxes), except the last two
+// of them, which one block per segment does in shared memory with one read and one write of
+// the bodies (k_pair); below that, one thread block takes a whole segment into shared memory
+// and finishes its subtree there (per-dimension sorted lists: bounds and medians read off the
+// lists, one segmented stable partition of the lists per level).
 #include "kd_internal.cuh"
 
 namespace kd {
