@@ -441,15 +441,25 @@ int check_device(kd_ctx *c) {
 void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
     Plan &p = c->plan;
     const bool levels = !p.glevels.empty();
-    launch_init_work(c->bodies, c->work, (uint32_t)c->n, levels ? c->scr.bmin[0] : nullptr,
-                     levels ? c->scr.bmax[0] : nullptr, c->st);
-    c->launches += 3;  // init + local finish + upward pass
-    int cur = 0;
     // the last two levels (one when the root is the only multi-block segment) in one pass
     const size_t L = p.glevels.size();
     const size_t npair = L >= 2 && p.gmax[L - 2] <= kPairMax
                              ? 2
                              : (L >= 1 && p.gmax[L - 1] <= kPairMax ? 1 : 0);
+    // a multi-block level 0 reads the bodies' positions in place (original order: the body id
+    // is the position), so the first pass only reduces the root's bounding box
+    const bool direct0 = L > npair && p.gmax[0] > kMultiMin;
+    Work w0 = c->work;
+    if (direct0) {
+        w0.x[0] = c->bodies.x;
+        w0.y[0] = c->bodies.y;
+        w0.z[0] = c->bodies.z;
+        w0.id[0] = nullptr;
+    }
+    launch_init_work(c->bodies, c->work, (uint32_t)c->n, levels ? c->scr.bmin[0] : nullptr,
+                     levels ? c->scr.bmax[0] : nullptr, c->st, !direct0);
+    c->launches += 3;  // init + local finish + upward pass
+    int cur = 0;
     for (size_t l = 0; l + npair < L; ++l) {
         LevelArgs lv;
         lv.ids = c->d_glevels[l];
@@ -460,8 +470,8 @@ void enqueue_build(kd_ctx *c, bool want_d, bool want_f) {
         lv.med_pos = nullptr;
         lv.max_iters = c->select_passes;
         const uint32_t G_next = l + 1 < p.glevels.size() ? (uint32_t)p.glevels[l + 1].size() : 0u;
-        c->launches += launch_level(c->topo, lv, c->nout, c->work, cur, c->scr, (int)l, G_next,
-                                    c->st, true, p.gmax[l]);
+        c->launches += launch_level(c->topo, lv, c->nout, l == 0 ? w0 : c->work, cur, c->scr,
+                                    (int)l, G_next, c->st, true, p.gmax[l]);
         cur ^= 1;
     }
     if (npair) {

@@ -161,8 +161,9 @@ __device__ __forceinline__ unsigned long long warp_max(unsigned long long v) {
     const uint32_t ml = __reduce_max_sync(kFull, hi == mh ? lo : 0u);
     return ((unsigned long long)mh << 32) | ml;
 }
-// The build's first work arrays (positions and body ids in original order); with `bmin` set,
-// also the bounding box of the whole set (segment 0 of level 0) on ordered keys.
+// The build's first work arrays (positions and body ids in original order; skipped when wx is
+// null, for a level 0 that reads the bodies in place); with `bmin` set, also the bounding box
+// of the whole set (segment 0 of level 0) on ordered keys.
 __global__ __launch_bounds__(256) void k_init_work(Bodies b, double *wx, double *wy, double *wz,
                                                    uint32_t *wid, uint32_t n,
                                                    unsigned long long *bmin,
@@ -171,10 +172,12 @@ __global__ __launch_bounds__(256) void k_init_work(Bodies b, double *wx, double 
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += gridDim.x * blockDim.x) {
         const double x = b.x[i], y = b.y[i], z = b.z[i];
-        wx[i] = x;
-        wy[i] = y;
-        wz[i] = z;
-        wid[i] = i;
+        if (wx) {
+            wx[i] = x;
+            wy[i] = y;
+            wz[i] = z;
+            wid[i] = i;
+        }
         const unsigned long long k0 = ord_key(x), k1 = ord_key(y), k2 = ord_key(z);
         mn[0] = min(mn[0], k0); mx[0] = max(mx[0], k0);
         mn[1] = min(mn[1], k1); mx[1] = max(mx[1], k1);
@@ -205,14 +208,17 @@ __global__ __launch_bounds__(256) void k_init_work(Bodies b, double *wx, double 
 }
 
 void launch_init_work(const Bodies &b, Work &w, uint32_t n, unsigned long long *bmin,
-                      unsigned long long *bmax, cudaStream_t st) {
+                      unsigned long long *bmax, cudaStream_t st, bool copy) {
     int blocks = (int)((n + 255) / 256);
     if (blocks > sm_count() * 16) blocks = sm_count() * 16;  // a few thousand box atomics
     if (bmin) {
         cudaMemsetAsync(bmin, 0xff, sizeof(unsigned long long) * 3, st);
         cudaMemsetAsync(bmax, 0x00, sizeof(unsigned long long) * 3, st);
     }
-    k_init_work<<<blocks, 256, 0, st>>>(b, w.x[0], w.y[0], w.z[0], w.id[0], n, bmin, bmax);
+    if (copy)
+        k_init_work<<<blocks, 256, 0, st>>>(b, w.x[0], w.y[0], w.z[0], w.id[0], n, bmin, bmax);
+    else
+        k_init_work<<<blocks, 256, 0, st>>>(b, nullptr, nullptr, nullptr, nullptr, n, bmin, bmax);
 }
 
 __global__ void k_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx,
@@ -576,13 +582,21 @@ __device__ __forceinline__ bool goes_left(unsigned long long key, uint32_t id,
     return key < kmed || (key == kmed && id < idmed);
 }
 
+// Body ids of a segment: the work array's, or -- at a level 0 that reads the bodies in place,
+// in their original order -- the position itself.
+struct IdView {
+    const uint32_t *p;
+    uint32_t base;
+    __device__ __forceinline__ uint32_t operator[](uint32_t i) const { return p ? p[i] : base + i; }
+};
+
 // The last step of k_select when more than 32 candidates are left (a refinement that could
 // not narrow them): a bitonic sort of (key, id) and a pick at the wanted rank.
 template <typename Get>
 __device__ __forceinline__ void select_sorted(unsigned long long *skey, unsigned long long *sval,
                                               uint32_t c, uint32_t r, SegSel *sel, uint32_t seg,
                                               NodeOut no, uint32_t nid, const double *w,
-                                              const uint32_t *ids, Get &get,
+                                              const IdView &ids, Get &get,
                                               unsigned long long &s_kmed, uint32_t &s_idmed) {
     const uint32_t P = next_pow2(c);
     for (uint32_t j = threadIdx.x; j < P; j += blockDim.x) {
@@ -618,7 +632,7 @@ static_assert(kMultiMin <= (uint32_t)(kSmallSegTiles * kTile), "tile counters of
 __device__ __forceinline__ void tile_offsets(const Topology &t, const LevelArgs &lv,
                                              const Scratch &s, const SegSel &st, uint32_t seg,
                                              uint32_t nid, uint32_t start, const double *w,
-                                             const uint32_t *ids, unsigned long long kmed,
+                                             const IdView &ids, unsigned long long kmed,
                                              uint32_t idmed) {
     __shared__ uint32_t scnt[kSmallSegTiles];
     __shared__ uint32_t wsum[32];
@@ -703,7 +717,7 @@ __global__ __launch_bounds__(kSelThreads) void k_select(Topology t, LevelArgs lv
     const uint32_t start = t.start[nid];
     SegSel st = sel[seg];
     const double *w = pick(wx, wy, wz, st.sd) + start;
-    const uint32_t *ids = wid + start;
+    const IdView ids{wid ? wid + start : nullptr, start};
     uint32_t c = st.c, r = st.r;
     int src = lv.multi ? 0 : -1;  // -1: the candidates are the segment itself
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -893,7 +907,10 @@ __global__ __launch_bounds__(kTileThreads, 3) void k_part_scatter(
             cp_async8(&S.x[q], sx + k);
             cp_async8(&S.y[q], sy + k);
             cp_async8(&S.z[q], sz + k);
-            cp_async4(&S.id[q], sid + k);
+            if (sid)
+                cp_async4(&S.id[q], sid + k);
+            else
+                S.id[q] = k;  // a level 0 read in place: the position is the body id
         }
     }
     const SegSel s = sel[r.seg];

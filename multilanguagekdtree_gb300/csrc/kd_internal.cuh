@@ -243,9 +243,10 @@ __device__ __forceinline__ NodeP make_nodep(const NodeD &q) {
     return p;
 }
 
-// Work arrays of the build; with bmin/bmax set, also the level-0 bounding box into them.
+// Work arrays of the build (unless !copy: a level 0 that reads the bodies in place); with
+// bmin/bmax set, also the level-0 bounding box into them.
 void launch_init_work(const Bodies &b, Work &w, uint32_t n, unsigned long long *bmin,
-                      unsigned long long *bmax, cudaStream_t st);
+                      unsigned long long *bmax, cudaStream_t st, bool copy = true);
 // quickselect set-up: key[i] = vals[idx[i]], id[i] = idx[i]; flags an index >= n_vals
 void launch_gather_keys(const double *vals, uint64_t n_vals, const uint64_t *idx, uint32_t n,
                         double *key, uint32_t *id, uint32_t *err, cudaStream_t st);
