@@ -577,7 +577,8 @@ def run_ours(a, ws, rank, local):
 WALK_TRAFFIC_PER_BODY = 479.0
 BUILD_TRAFFIC_PER_BODY = 1094.0
 BUILD_TRAFFIC_NOTE = ("ncu dram read + write of the build's kernels in one 10M-ring step "
-                      "(1,094 B/body, cold caches per kernel), scaled by N")
+                      "(1,094 B/body, cold caches per kernel), scaled by N; captured while the "
+                      "first pass still copied the positions (~23 B/body more than now)")
 
 
 def tree_levels(n: int, leaf: int) -> int:
